@@ -1,0 +1,278 @@
+"""fen_gb300 — GB300-native incompressible projection step with FEN's interfaces.
+
+Python face of ``libfen_gb300.so`` (C ABI in ``include/fen_gpu.h``).  The names mirror the
+FEN Fortran modules the C ABI replaces:
+
+    grid_mod            Grid(...)                         (src/grid.f90:67-200)
+    solver_mod          Solver.init_solver / advance_solution / destroy_solver
+                                                           (src/solver.f90:34-99, 333)
+    navier_stokes_mod   set_timestep, module state v, p, phi, dv_o, S, maxdiv, maxCFL
+                                                           (src/navier_stokes.f90:17-45, 623)
+    poisson_mod         solve_poisson                      (src/poisson.f90:21-29)
+    fields_mod          divergence                         (src/fields.f90:120-153)
+
+Fields are exchanged as numpy arrays in FEN's layout f(0:nx+1, 0:ny+1, 0:nz+1) (x fastest),
+viewed in numpy as shape (nz+2, ny+2, nx+2); in 2D the z extent is 0:2 (3 planes).
+
+The CUDA library is required: there is no CPU fallback, and loading fails loudly when the
+shared library or a GPU is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["Grid", "Solver", "FenError", "PERIODIC", "WALL", "INFLOW", "OUTFLOW", "load_library"]
+
+PERIODIC, WALL, INFLOW, OUTFLOW = 0, 1, 2, 3
+BC_NAMES = {"Periodic": PERIODIC, "Wall": WALL, "Inflow": INFLOW, "Outflow": OUTFLOW}
+LEFT, RIGHT, BOTTOM, TOP, FRONT, BACK = range(6)
+U, V, W, P, PHI = 0, 1, 2, 3, 4
+DVO_X, DVO_Y, DVO_Z = 5, 6, 7
+S_X, S_Y, S_Z = 8, 9, 10
+FP64, MIXED = 0, 1
+SOLVER_NAMES = ["pp", "pn", "nn", "ppp", "ppn", "npn", "nnn", "pnp"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libfen_gb300.so")
+
+
+class FenError(RuntimeError):
+    pass
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("lx", ctypes.c_double), ("ly", ctypes.c_double), ("lz", ctypes.c_double),
+        ("origin", ctypes.c_double * 3), ("bc", ctypes.c_int * 6), ("aniso", ctypes.c_int),
+        ("density", ctypes.c_double), ("viscosity", ctypes.c_double), ("g", ctypes.c_double * 3),
+        ("cfl", ctypes.c_double), ("constant_cfl", ctypes.c_int), ("precision", ctypes.c_int),
+    ]
+
+
+class _Status(ctypes.Structure):
+    _fields_ = [
+        ("dt", ctypes.c_double), ("dt_o", ctypes.c_double), ("maxdiv", ctypes.c_double),
+        ("maxcfl", ctypes.c_double), ("maxvel", ctypes.c_double), ("dt_visc", ctypes.c_double),
+        ("nan_detected", ctypes.c_int), ("poisson_solver", ctypes.c_int),
+    ]
+
+
+_lib = None
+_EXPORTS = [
+    "fen_ctx_create", "fen_ctx_destroy", "fen_last_error", "fen_upload", "fen_download",
+    "fen_update_ghost_nodes", "fen_set_bc_values", "fen_set_bc_type", "fen_set_timestep",
+    "fen_set_dt_o", "fen_advance_solution", "fen_advance_n", "fen_get_status", "fen_solve_poisson",
+    "fen_divergence", "fen_explicit_terms", "fen_sync", "fen_kernel_launches", "fen_time_steps",
+    "fen_profile_step",
+]
+
+
+def load_library(path=None):
+    """Load libfen_gb300.so and declare the C ABI.  Raises FenError if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise FenError(f"{path} not built: run `python -m fen_gb300.build` (needs nvcc)")
+    L = ctypes.CDLL(path)
+    vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int
+    L.fen_ctx_create.argtypes = [ctypes.POINTER(_Params), ctypes.POINTER(vp)]
+    L.fen_ctx_destroy.argtypes = [vp]
+    L.fen_last_error.restype = ctypes.c_char_p
+    L.fen_upload.argtypes = [vp, ip, dp]
+    L.fen_download.argtypes = [vp, ip, dp]
+    L.fen_update_ghost_nodes.argtypes = [vp, ip]
+    L.fen_set_bc_values.argtypes = [vp, ip, ip, dp]
+    L.fen_set_bc_type.argtypes = [vp, ip, ip, ip]
+    L.fen_set_timestep.argtypes = [vp, ctypes.c_double, dp]
+    L.fen_set_dt_o.argtypes = [vp, ctypes.c_double]
+    L.fen_advance_solution.argtypes = [vp, ip, dp]
+    L.fen_advance_n.argtypes = [vp, ip, dp]
+    L.fen_get_status.argtypes = [vp, ctypes.POINTER(_Status)]
+    L.fen_solve_poisson.argtypes = [vp]
+    L.fen_divergence.argtypes = [vp, dp]
+    L.fen_explicit_terms.argtypes = [vp, dp]
+    L.fen_sync.argtypes = [vp]
+    L.fen_kernel_launches.argtypes = [vp]
+    L.fen_kernel_launches.restype = ctypes.c_longlong
+    L.fen_time_steps.argtypes = [vp, ip, ctypes.c_double, dp]
+    L.fen_profile_step.argtypes = [vp, ip, ctypes.c_double, dp]
+    if path == LIB_PATH:
+        _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Grid:
+    """grid%setup(Nx, Ny, Nz, Lx, Ly, Lz, x0, prow, pcol, bc) (src/grid.f90:67-200).
+
+    prow/pcol are accepted for interface parity and ignored: one device holds the domain.
+    ``bc`` is a list of 'Periodic' | 'Wall' | 'Inflow' | 'Outflow' (or the integer codes) for
+    left, right, bottom, top[, front, back]; all periodic when omitted (grid.f90:96-104).
+    ``aniso`` enables one spacing per axis (the reference uses delta = Lx/Nx everywhere).
+    """
+
+    def __init__(self, Nx, Ny, Nz, Lx, Ly, Lz, x0=(0.0, 0.0, 0.0), prow=1, pcol=1, bc=None, dim=None, aniso=False):
+        self.dim = dim if dim is not None else (2 if Nz == 1 else 3)
+        self.Nx, self.Ny, self.Nz = int(Nx), int(Ny), int(Nz) if self.dim == 3 else 1
+        self.Lx, self.Ly, self.Lz = float(Lx), float(Ly), float(Lz)
+        self.origin = tuple(float(v) for v in x0)
+        bc = list(bc) if bc is not None else ["Periodic"] * (2 * self.dim)
+        self.bc = [BC_NAMES[b] if isinstance(b, str) else int(b) for b in bc]
+        self.aniso = bool(aniso)
+        self.delta = self.Lx / float(np.float32(self.Nx))
+        if aniso:
+            self.deltas = (self.Lx / self.Nx, self.Ly / self.Ny, (self.Lz / self.Nz) if self.dim == 3 else self.delta)
+        else:
+            self.deltas = (self.delta,) * 3
+
+    @property
+    def shape(self):
+        """numpy shape (k, j, i) of a ghosted field."""
+        return ((self.Nz + 2) if self.dim == 3 else 3, self.Ny + 2, self.Nx + 2)
+
+
+class Solver:
+    """One solver instance: init_solver + the navier_stokes_mod/poisson_mod module state.
+
+    Module variables of navier_stokes_mod (density, viscosity, g, CFL, constant_CFL,
+    navier_stokes.f90:18-45) are constructor arguments.
+    """
+
+    def __init__(self, grid, density=1.0, viscosity=1.0, g=(0.0, 0.0, 0.0), CFL=1.0, constant_CFL=False,
+                 precision=FP64, lib=None):
+        self._L = load_library(lib)
+        self.grid = grid
+        p = _Params()
+        p.dim, p.nx, p.ny, p.nz = grid.dim, grid.Nx, grid.Ny, grid.Nz
+        p.lx, p.ly, p.lz = grid.Lx, grid.Ly, grid.Lz
+        p.origin = (ctypes.c_double * 3)(*grid.origin)
+        bc = grid.bc + [PERIODIC] * (6 - len(grid.bc))
+        p.bc = (ctypes.c_int * 6)(*bc)
+        p.aniso = int(grid.aniso)
+        p.density, p.viscosity = float(density), float(viscosity)
+        p.g = (ctypes.c_double * 3)(*[float(x) for x in g])
+        p.cfl, p.constant_cfl, p.precision = float(CFL), int(bool(constant_CFL)), int(precision)
+        self._h = ctypes.c_void_p()
+        self._check(self._L.fen_ctx_create(ctypes.byref(p), ctypes.byref(self._h)))
+        self.dt_o = None
+
+    # -- lifecycle -----------------------------------------------------------------------
+    def _check(self, rc):
+        if rc != 0:
+            msg = self._L.fen_last_error().decode()
+            raise FenError(f"fen error {rc}: {msg}")
+
+    def destroy_solver(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.fen_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy_solver()
+        except Exception:
+            pass
+
+    # -- fields ----------------------------------------------------------------------------
+    def zeros(self):
+        return np.zeros(self.grid.shape)
+
+    def set_field(self, fid, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        if a.shape != self.grid.shape:
+            raise ValueError(f"field shape {a.shape} != {self.grid.shape}")
+        self._check(self._L.fen_upload(self._h, fid, _dp(a)))
+
+    def get_field(self, fid):
+        a = self.zeros()
+        self._check(self._L.fen_download(self._h, fid, _dp(a)))
+        return a
+
+    def update_ghost_nodes(self, fid):
+        self._check(self._L.fen_update_ghost_nodes(self._h, fid))
+
+    def set_bc_values(self, fid, face, values):
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        self._check(self._L.fen_set_bc_values(self._h, fid, face, _dp(a)))
+
+    def set_bc_type(self, fid, face, t):
+        self._check(self._L.fen_set_bc_type(self._h, fid, face, t))
+
+    # -- navier_stokes_mod / solver_mod ----------------------------------------------------
+    def set_timestep(self, U):
+        dt = ctypes.c_double()
+        self._check(self._L.fen_set_timestep(self._h, float(U), ctypes.byref(dt)))
+        self.dt_o = dt.value
+        return dt.value
+
+    def set_dt_o(self, dt_o):
+        self._check(self._L.fen_set_dt_o(self._h, float(dt_o)))
+        self.dt_o = float(dt_o)
+
+    def advance_solution(self, step, dt):
+        d = ctypes.c_double(dt)
+        self._check(self._L.fen_advance_solution(self._h, int(step), ctypes.byref(d)))
+        return d.value
+
+    def advance_n(self, nsteps, dt):
+        d = ctypes.c_double(dt)
+        self._check(self._L.fen_advance_n(self._h, int(nsteps), ctypes.byref(d)))
+        return d.value
+
+    def status(self):
+        s = _Status()
+        self._check(self._L.fen_get_status(self._h, ctypes.byref(s)))
+        return {"dt": s.dt, "dt_o": s.dt_o, "maxdiv": s.maxdiv, "maxCFL": s.maxcfl, "maxvel": s.maxvel,
+                "dt_visc": s.dt_visc, "nan": bool(s.nan_detected), "poisson_solver": SOLVER_NAMES[s.poisson_solver]}
+
+    def print_solver_status(self, step, time, dt):
+        """print_navier_stokes_solver_status line (navier_stokes.f90:743-746)."""
+        s = self.status()
+        return "step: %7d time: %13.6E dt: %13.6E maxdiv: %13.6E maxCFL:  %13.6E" % (
+            step, time, dt, s["maxdiv"], s["maxCFL"])
+
+    # -- poisson_mod / fields_mod ----------------------------------------------------------
+    def solve_poisson(self, phi=None):
+        """solve_poisson(phi): solves in place on the device copy of phi; with an array
+        argument it uploads it first and returns the solution."""
+        if phi is not None:
+            self.set_field(PHI, phi)
+        self._check(self._L.fen_solve_poisson(self._h))
+        if phi is not None:
+            return self.get_field(PHI)
+
+    def divergence(self):
+        g = self.grid
+        out = np.zeros(g.Nx * g.Ny * g.Nz)
+        self._check(self._L.fen_divergence(self._h, _dp(out)))
+        return out.reshape(g.Nz, g.Ny, g.Nx)
+
+    def explicit_terms(self):
+        g = self.grid
+        out = np.zeros(3 * g.Nx * g.Ny * g.Nz)
+        self._check(self._L.fen_explicit_terms(self._h, _dp(out)))
+        return out.reshape(3, g.Nz, g.Ny, g.Nx)[: g.dim]
+
+    # -- measurement -------------------------------------------------------------------------
+    def kernel_launches(self):
+        return int(self._L.fen_kernel_launches(self._h))
+
+    def time_steps(self, nsteps, dt):
+        ms = ctypes.c_double()
+        self._check(self._L.fen_time_steps(self._h, int(nsteps), float(dt), ctypes.byref(ms)))
+        return ms.value
+
+    def profile_step(self, reps, dt):
+        out = np.zeros(8)
+        self._check(self._L.fen_profile_step(self._h, int(reps), float(dt), _dp(out)))
+        return out
+
+    def sync(self):
+        self._check(self._L.fen_sync(self._h))

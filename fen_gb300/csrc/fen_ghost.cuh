@@ -1,0 +1,172 @@
+// Ghost-cell fill (FEN src/scalar.f90:223-396 with src/halo.f90:12-43 on one device).
+//
+// The reference fills faces in the order left, right, bottom, top, front, back, each over
+// the full ghosted extent of the other axes, so edges and corners see the faces filled
+// before them, and a Dirichlet face-normal component also overwrites its last interior
+// plane (f(hi) = bc, scalar.f90:282-283, 331-332, 377-378).  The final value of every
+// written cell is therefore a composition of at most three face rules applied to ONE
+// interior value.  `Resolve` evaluates that composition directly, so one launch fills all
+// ghosts of several fields without ordering passes: threads write only ghost cells and
+// overwritten cells and read only interior cells that no thread writes.
+#pragma once
+#include "fen_types.cuh"
+
+namespace fen {
+
+template <typename T, int DIM>
+struct Resolve {
+  const T* f;
+  Layout L;
+  FieldBC bc;
+  double shift;  // subtracted from every interior value read (0 = none)
+
+  __device__ __forceinline__ T bcv(int face, int a, int b) const {
+    const double* p = bc.val[face];
+    if (!p) return T(0);
+    // face arrays cover the ghosted extents: left/right (j,k), bottom/top (i,k), front/back (i,j)
+    int na = (face < 2) ? L.n1 + 2 : L.n0 + 2;
+    if (DIM == 2 && face < 4) b = 0;  // 2D: single stored k plane
+    return (T)p[a + (long long)na * b];
+  }
+  __device__ __forceinline__ T state(int i, int j, int k) const {
+    T v = f[L.idx(i, j, kst<DIM>(k))];
+    return shift != 0.0 ? (T)(v - (T)shift) : v;
+  }
+  __device__ __forceinline__ T after_x(int i, int j, int k) const {
+    const int N = L.n0;
+    const bool nrm = (bc.c == 'x');
+    if (i == 0) {
+      const int t = bc.type[F_LEFT];
+      if (t == FT_PERIODIC) return state(N, j, k);
+      if (t == FT_DIRICHLET) return nrm ? bcv(F_LEFT, j, k) : (T)(T(2) * bcv(F_LEFT, j, k) - state(1, j, k));
+      return state(1, j, k);
+    }
+    if (i == N + 1) {
+      const int t = bc.type[F_RIGHT];
+      if (t == FT_PERIODIC) return state(1, j, k);
+      if (t == FT_DIRICHLET) return nrm ? bcv(F_RIGHT, j, k) : (T)(T(2) * bcv(F_RIGHT, j, k) - state(N, j, k));
+      return state(N, j, k);
+    }
+    if (i == N && nrm && bc.type[F_RIGHT] == FT_DIRICHLET) return bcv(F_RIGHT, j, k);
+    return state(i, j, k);
+  }
+  __device__ __forceinline__ T after_y(int i, int j, int k) const {
+    const int N = L.n1;
+    const bool nrm = (bc.c == 'y');
+    if (j == 0) {
+      const int t = bc.type[F_BOTTOM];
+      if (t == FT_PERIODIC) return after_x(i, N, k);
+      if (t == FT_DIRICHLET) return nrm ? bcv(F_BOTTOM, i, k) : (T)(T(2) * bcv(F_BOTTOM, i, k) - after_x(i, 1, k));
+      return after_x(i, 1, k);
+    }
+    if (j == N + 1) {
+      const int t = bc.type[F_TOP];
+      if (t == FT_PERIODIC) return after_x(i, 1, k);
+      if (t == FT_DIRICHLET) return nrm ? bcv(F_TOP, i, k) : (T)(T(2) * bcv(F_TOP, i, k) - after_x(i, N, k));
+      return after_x(i, N, k);
+    }
+    if (j == N && nrm && bc.type[F_TOP] == FT_DIRICHLET) return bcv(F_TOP, i, k);
+    return after_x(i, j, k);
+  }
+  __device__ __forceinline__ T after_z(int i, int j, int k) const {
+    if (DIM == 2) return after_y(i, j, k);
+    const int N = L.n2;
+    const bool nrm = (bc.c == 'z');
+    if (k == 0) {
+      const int t = bc.type[F_FRONT];
+      if (t == FT_PERIODIC) return after_y(i, j, N);
+      if (t == FT_DIRICHLET) return nrm ? bcv(F_FRONT, i, j) : (T)(T(2) * bcv(F_FRONT, i, j) - after_y(i, j, 1));
+      return after_y(i, j, 1);
+    }
+    if (k == N + 1) {
+      const int t = bc.type[F_BACK];
+      if (t == FT_PERIODIC) return after_y(i, j, 1);
+      if (t == FT_DIRICHLET) return nrm ? bcv(F_BACK, i, j) : (T)(T(2) * bcv(F_BACK, i, j) - after_y(i, j, N));
+      return after_y(i, j, N);
+    }
+    if (k == N && nrm && bc.type[F_BACK] == FT_DIRICHLET) return bcv(F_BACK, i, j);
+    return after_y(i, j, k);
+  }
+  // Final value of any cell after update_ghost_nodes.
+  __device__ __forceinline__ T at(int i, int j, int k) const { return after_z(i, j, k); }
+};
+
+// Number of cells one field's ghost fill writes (see ghost_target).
+struct GhostCount {
+  long long a, b, c;  // segments: x columns, y rows, z planes
+};
+
+template <int DIM>
+__host__ __device__ inline GhostCount ghost_count(const Layout& L, const FieldBC& bc) {
+  const int xov = (bc.c == 'x' && bc.type[F_RIGHT] == FT_DIRICHLET);
+  const int yov = (bc.c == 'y' && bc.type[F_TOP] == FT_DIRICHLET);
+  const int zov = (DIM == 3 && bc.c == 'z' && bc.type[F_BACK] == FT_DIRICHLET);
+  const long long nk = (DIM == 3) ? (L.n2 - zov) : 1;
+  GhostCount g;
+  g.a = (long long)(2 + xov) * (L.n1 - yov) * nk;
+  g.b = (long long)(2 + yov) * (L.n0 + 2) * nk;
+  g.c = (DIM == 3) ? (long long)(2 + zov) * (L.n0 + 2) * (L.n1 + 2) : 0;
+  return g;
+}
+
+// Maps a linear work index of one field to the (i, j, k) cell it writes.
+template <int DIM>
+__device__ __forceinline__ void ghost_target(const Layout& L, const FieldBC& bc, long long t, int& i, int& j, int& k) {
+  const int xov = (bc.c == 'x' && bc.type[F_RIGHT] == FT_DIRICHLET);
+  const int yov = (bc.c == 'y' && bc.type[F_TOP] == FT_DIRICHLET);
+  const int zov = (DIM == 3 && bc.c == 'z' && bc.type[F_BACK] == FT_DIRICHLET);
+  const long long nk = (DIM == 3) ? (L.n2 - zov) : 1;
+  const GhostCount g = ghost_count<DIM>(L, bc);
+  if (t < g.a) {  // x faces: j in [1, n1-yov], k in [1, nk]
+    const int w = 2 + xov;
+    const int s = (int)(t % w);
+    long long r = t / w;
+    j = 1 + (int)(r % (L.n1 - yov));
+    k = 1 + (int)(r / (L.n1 - yov));
+    i = (s == 0) ? 0 : (s == 1) ? L.n0 + 1 : L.n0;
+    return;
+  }
+  t -= g.a;
+  if (t < g.b) {  // y faces: i in [0, n0+1], k in [1, nk]
+    const int ni = L.n0 + 2;
+    i = (int)(t % ni);
+    long long r = t / ni;
+    const int w = 2 + yov;
+    const int s = (int)(r % w);
+    k = 1 + (int)(r / w);
+    j = (s == 0) ? 0 : (s == 1) ? L.n1 + 1 : L.n1;
+    return;
+  }
+  t -= g.b;  // z faces: i in [0, n0+1], j in [0, n1+1]
+  const int ni = L.n0 + 2, nj = L.n1 + 2;
+  i = (int)(t % ni);
+  long long r = t / ni;
+  j = (int)(r % nj);
+  const int s = (int)(r / nj);
+  k = (s == 0) ? 0 : (s == 1) ? L.n2 + 1 : L.n2;
+  (void)nk;
+}
+
+// Up to four fields per launch (blockIdx.y selects the field).
+template <typename T>
+struct GhostBatch {
+  T* f[4];
+  FieldBC bc[4];
+  long long n[4];
+  double shift[4];
+};
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) k_ghost_fill(Layout L, GhostBatch<T> G) {
+  const int q = blockIdx.y;
+  const long long total = G.n[q];
+  Resolve<T, DIM> R{G.f[q], L, G.bc[q], G.shift[q]};
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    ghost_target<DIM>(L, G.bc[q], t, i, j, k);
+    const T v = R.at(i, j, k);
+    G.f[q][L.idx(i, j, kst<DIM>(k))] = v;
+  }
+}
+
+}  // namespace fen

@@ -1,0 +1,684 @@
+// Projection-step kernels (FEN src/navier_stokes.f90, src/fields.f90, src/poisson.f90).
+#pragma once
+#include "fen_fft.cuh"
+#include "fen_ghost.cuh"
+#include "fen_types.cuh"
+
+namespace fen {
+
+// ------------------------------------------------------------------------------------
+// Predictor: compute_explicit_terms + predicted_velocity_field fused
+// (navier_stokes.f90:140-257, 261-353, 384-404; fields.f90:31-64, 175-206, 298-343).
+// dv = -div(uu) + mu lap(v)/rhof + S/rhof;  v* = v + dt(-grad p/rhof + A dv + B dv_o + g);
+// dv_o <- dv.  Operation order follows the reference; v* goes to separate buffers because
+// the reference computes all of dv before updating v.
+// ------------------------------------------------------------------------------------
+template <typename T>
+struct PredArgs {
+  const T *u, *v, *w, *p;
+  T *us, *vs, *ws;
+  T *dox, *doy, *doz;
+  const T *Sx, *Sy, *Sz;
+  double id[3], id2[3];
+  double mu, rhof, g[3];
+  double dt_host;
+  int iso, has_S, rhof_one, use_dev_dt;
+};
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) k_predictor(Layout L, const StepScalars* __restrict__ sc, PredArgs<T> a) {
+  const long long ncell = (long long)L.n0 * L.n1 * L.n2;
+  const T A = (T)sc->A, B = (T)sc->B;
+  const T dt = (T)(a.use_dev_dt ? sc->dt : a.dt_host);
+  const T idx = (T)a.id[0], idy = (T)a.id[1], idz = (T)a.id[2];
+  const T id2x = (T)a.id2[0], id2y = (T)a.id2[1], id2z = (T)a.id2[2];
+  const T mu = (T)a.mu, rhof = (T)a.rhof;
+  const long long sy = L.sx, sz = L.sp;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(t % L.n0);
+    const long long r = t / L.n0;
+    const int j = 1 + (int)(r % L.n1);
+    const int k = 1 + (int)(r / L.n1);
+    const long long c = L.idx(i, j, kst<DIM>(k));
+    const T* __restrict__ U = a.u;
+    const T* __restrict__ V = a.v;
+    const T* __restrict__ W = a.w;
+    const T uc = U[c], vc = V[c];
+    const T uip = U[c + 1], uim = U[c - 1], ujp = U[c + sy], ujm = U[c - sy];
+    const T vip = V[c + 1], vim = V[c - 1], vjp = V[c + sy], vjm = V[c - sy];
+    // u advection
+    const T q = (T)0.25;
+    T uuip = q * ((uip + uc) * (uip + uc));
+    T uuim = q * ((uim + uc) * (uim + uc));
+    T uvjp = (ujp + uc) * (vip + vc) * q;
+    T uvjm = (uc + ujm) * (V[c + 1 - sy] + vjm) * q;
+    T dvx = -((uuip - uuim) * idx) - (uvjp - uvjm) * idy;
+    // v advection
+    T vuip = (vip + vc) * (ujp + uc) * q;
+    T vuim = (vc + vim) * (U[c - 1 + sy] + uim) * q;
+    T vvjp = q * ((vjp + vc) * (vjp + vc));
+    T vvjm = q * ((vjm + vc) * (vjm + vc));
+    T dvy = -((vuip - vuim) * idx) - (vvjp - vvjm) * idy;
+    T dvz = 0, wc = 0, wkp = 0, wkm = 0;
+    T ukp = 0, ukm = 0, vkp = 0, vkm = 0;
+    if (DIM == 3) {
+      wc = W[c];
+      const T wip = W[c + 1], wim = W[c - 1], wjp = W[c + sy], wjm = W[c - sy];
+      wkp = W[c + sz]; wkm = W[c - sz];
+      ukp = U[c + sz]; ukm = U[c - sz]; vkp = V[c + sz]; vkm = V[c - sz];
+      T uwkp = (ukp + uc) * (wip + wc) * q;
+      T uwkm = (uc + ukm) * (W[c + 1 - sz] + wkm) * q;
+      dvx = dvx - (uwkp - uwkm) * idz;
+      T vwkp = (vkp + vc) * (wjp + wc) * q;
+      T vwkm = (vc + vkm) * (W[c + sy - sz] + wkm) * q;
+      dvy = dvy - (vwkp - vwkm) * idz;
+      T wuip = (wc + wip) * (uc + ukp) * q;
+      T wuim = (wc + wim) * (uim + U[c - 1 + sz]) * q;
+      T wvjp = (wc + wjp) * (vc + vkp) * q;
+      T wvjm = (wc + wjm) * (vjm + V[c - sy + sz]) * q;
+      T wwkp = (wc + wkp) * (wc + wkp) * q;
+      T wwkm = (wc + wkm) * (wc + wkm) * q;
+      dvz = -((wuip - wuim) * idx) - (wvjp - wvjm) * idy - (wwkp - wwkm) * idz;
+      // w laplacian: the three directions summed before scaling (fields.f90:335-337)
+      const T two = T(2) * wc;
+      T lw;
+      if (a.iso) lw = ((wip - two + wim) + (wjp - two + wjm) + (wkp - two + wkm)) * id2x;
+      else lw = (wip - two + wim) * id2x + (wjp - two + wjm) * id2y + (wkp - two + wkm) * id2z;
+      dvz = dvz + (a.rhof_one ? mu * lw : mu * lw / rhof);
+    }
+    // u, v laplacian (fields.f90:326-334)
+    {
+      const T two = T(2) * uc;
+      T l;
+      if (a.iso) {
+        l = ((uip - two + uim) + (ujp - two + ujm)) * id2x;
+        if (DIM == 3) l = l + (ukp - two + ukm) * id2x;
+      } else {
+        l = (uip - two + uim) * id2x + (ujp - two + ujm) * id2y;
+        if (DIM == 3) l = l + (ukp - two + ukm) * id2z;
+      }
+      dvx = dvx + (a.rhof_one ? mu * l : mu * l / rhof);
+    }
+    {
+      const T two = T(2) * vc;
+      T l;
+      if (a.iso) {
+        l = ((vip - two + vim) + (vjp - two + vjm)) * id2x;
+        if (DIM == 3) l = l + (vkp - two + vkm) * id2x;
+      } else {
+        l = (vip - two + vim) * id2x + (vjp - two + vjm) * id2y;
+        if (DIM == 3) l = l + (vkp - two + vkm) * id2z;
+      }
+      dvy = dvy + (a.rhof_one ? mu * l : mu * l / rhof);
+    }
+    if (a.has_S) {
+      dvx = dvx + (a.rhof_one ? a.Sx[c] : a.Sx[c] / rhof);
+      dvy = dvy + (a.rhof_one ? a.Sy[c] : a.Sy[c] / rhof);
+      if (DIM == 3) dvz = dvz + (a.rhof_one ? a.Sz[c] : a.Sz[c] / rhof);
+    }
+    // pressure gradient (fields.f90:55-58) and the AB2 update (navier_stokes.f90:169-198)
+    const T pc = a.p[c];
+    const T gpx = (a.p[c + 1] - pc) * (a.iso ? idx : idx);
+    const T gpy = (a.p[c + sy] - pc) * (a.iso ? idx : idy);
+    T rx = (a.rhof_one ? -gpx : -gpx / rhof) + A * dvx + B * a.dox[c] + (T)a.g[0];
+    T ry = (a.rhof_one ? -gpy : -gpy / rhof) + A * dvy + B * a.doy[c] + (T)a.g[1];
+    a.us[c] = uc + dt * rx;
+    a.vs[c] = vc + dt * ry;
+    a.dox[c] = dvx;
+    a.doy[c] = dvy;
+    if (DIM == 3) {
+      const T gpz = (a.p[c + sz] - pc) * (a.iso ? idx : idz);
+      T rz = (a.rhof_one ? -gpz : -gpz / rhof) + A * dvz + B * a.doz[c] + (T)a.g[2];
+      a.ws[c] = wc + dt * rz;
+      a.doz[c] = dvz;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Line transforms.  One kernel template covers every 1D stage of every solver:
+//   CONTIG = true : lines along x (contiguous), the first and last stages;
+//   CONTIG = false: lines along y or z (strided), a tile of consecutive columns per CTA.
+// ------------------------------------------------------------------------------------
+enum { OP_R2C = 0, OP_C2R, OP_C2C_F, OP_C2C_I, OP_C2C_SOLVE, OP_DCT2, OP_DCT3 };
+enum { LD_FIELD = 0, LD_DIV, LD_REAL, LD_CPLX };
+enum { ST_FIELD = 0, ST_REAL, ST_CPLX };
+
+template <typename T>
+struct LineArgs {
+  // geometry of the lines handled by this launch
+  int n;                  // real length (R2C/C2R/DCT) or complex length (C2C) along the axis
+  int nl;                 // lines per CTA
+  int nlines;             // lines per outer index (columns for strided, rows for contiguous)
+  // spectral input / output (element strides in units of their own type)
+  const void* in;
+  void* out;
+  long long in_line, in_pos, in_outer;     // address = line*in_line + pos*in_pos + outer*in_outer
+  long long out_line, out_pos, out_outer;
+  // fields (LD_FIELD / LD_DIV / ST_FIELD)
+  Layout L;
+  const T *fu, *fv, *fw;  // predicted velocity for LD_DIV
+  const T* fsrc;          // LD_FIELD source
+  T* fdst;                // ST_FIELD destination
+  double* partial;        // ST_FIELD: per-CTA line sums (mean removal), may be null
+  double scale;
+  const StepScalars* sc;  // LD_DIV scaling rho/dt
+  double id[3];
+  int iso, dim;
+  // OP_C2C_SOLVE eigenvalues: lam = lamA[col] + lamB[outer] + lamC[pos]
+  const double* lamA; const double* lamB; const double* lamC;
+  FFTPlan plan;
+  AxisTw tw;
+};
+
+// Global offset of (line, outer) of a contiguous launch: lines are x-rows j = 1..n1 of
+// plane k = outer + 1; returns the Fortran (j, k).
+template <int DIM>
+__device__ __forceinline__ void row_jk(int line, int outer, int& j, int& k) { j = line + 1; k = outer + 1; }
+
+template <typename T, int DIM>
+__device__ __forceinline__ T div_at(const LineArgs<T>& a, int i, int j, int k) {
+  const Layout& L = a.L;
+  const long long c = L.idx(i, j, kst<DIM>(k));
+  const T* U = a.fu; const T* V = a.fv; const T* W = a.fw;
+  T d;
+  if (a.iso) {
+    const T id = (T)a.id[0];
+    d = (U[c] - U[c - 1]) * id + (V[c] - V[c - L.sx]) * id;
+    if (DIM == 3) d = d + (W[c] - W[c - L.sp]) * id;
+  } else {
+    d = (U[c] - U[c - 1]) * (T)a.id[0] + (V[c] - V[c - L.sx]) * (T)a.id[1];
+    if (DIM == 3) d = d + (W[c] - W[c - L.sp]) * (T)a.id[2];
+  }
+  return d;
+}
+
+template <typename T, int DIM, bool CONTIG, int OP, int LD, int ST>
+__global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
+  typedef typename cpx<T>::t T2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = a.n;
+  const bool real_fft = (OP == OP_R2C || OP == OP_C2R || OP == OP_DCT2 || OP == OP_DCT3);
+  const int M = real_fft ? n / 2 : n;
+  const int nl = a.nl;
+  T2* bufA = reinterpret_cast<T2*>(smem_raw);
+  T2* bufB = bufA + (size_t)nl * M;
+  const int line0 = blockIdx.x * nl;
+  const int outer = blockIdx.y;
+  const int nlv = min(nl, a.nlines - line0);  // valid lines in this CTA
+  const int tid = threadIdx.x, nth = blockDim.x;
+  // position-major smem: element (l, p) at p*nl + l
+  auto S = [&](int l, int p) -> T2& { return bufA[(size_t)p * nl + l]; };
+  T* Sr = reinterpret_cast<T*>(bufA);  // real view: real slot r of line l at (r/2 * nl + l)*2 + (r&1)
+  auto RS = [&](int l, int r) -> T& { return Sr[((size_t)(r >> 1) * nl + l) * 2 + (r & 1)]; };
+
+  const T* inR = reinterpret_cast<const T*>(a.in);
+  const T2* inC = reinterpret_cast<const T2*>(a.in);
+
+  // ---------------- load ----------------
+  if (OP == OP_R2C || OP == OP_DCT2) {
+    // n reals per line -> packed complex (DCT2 reorders first: v_m = x_2m, v_{n-1-m} = x_2m+1)
+    const int work = nl * n;
+    for (int t = tid; t < work; t += nth) {
+      int l, i;
+      if (CONTIG) { l = t / n; i = t % n; } else { l = t % nl; i = t / nl; }
+      T x = 0;
+      if (l < nlv) {
+        if (LD == LD_FIELD || LD == LD_DIV) {
+          int j, k;
+          row_jk<DIM>(line0 + l, outer, j, k);
+          if (LD == LD_FIELD) x = a.fsrc[a.L.idx(i + 1, j, kst<DIM>(k))];
+          else x = div_at<T, DIM>(a, i + 1, j, k) * (T)a.sc->rho_over_dt;
+        } else {
+          x = inR[(long long)(line0 + l) * a.in_line + (long long)i * a.in_pos + (long long)outer * a.in_outer];
+        }
+      }
+      int r = i;
+      if (OP == OP_DCT2) r = (i & 1) ? (n - 1 - (i >> 1)) : (i >> 1);
+      RS(l, r) = x;
+    }
+  } else if (OP == OP_C2R || OP == OP_DCT3) {
+    // Hermitian half-spectrum X_0..X_M -> c2r pre-processed Z'_0..Z'_{M-1}
+    const int work = nl * M;
+    for (int t = tid; t < work; t += nth) {
+      int l, kk;
+      if (CONTIG) { l = t / M; kk = t % M; } else { l = t % nl; kk = t / nl; }
+      T2 z = mk<T2>(0, 0);
+      if (l < nlv) {
+        const long long base = (long long)(line0 + l) * a.in_line + (long long)outer * a.in_outer;
+        T2 xk, xm;
+        if (OP == OP_C2R) {
+          xk = inC[base + (long long)kk * a.in_pos];
+          xm = inC[base + (long long)(M - kk) * a.in_pos];
+        } else {
+          // V_k = (Y_k - i Y_{n-k}) exp(+i pi k / 2n), Y_n = 0  (Makhoul's DCT-III)
+          auto Vk = [&](int q) -> T2 {
+            const T yk = inR[base + (long long)q * a.in_pos];
+            const T yr = (q == 0) ? T(0) : inR[base + (long long)(n - q) * a.in_pos];
+            return cmulc(mk<T2>(yk, -yr), ldtw<T2>(a.tw.wD, q));
+          };
+          xk = Vk(kk);
+          xm = Vk(M - kk);
+        }
+        z = c2r_pre(xk, xm, M, kk, a.tw.wN);
+      }
+      S(l, kk) = z;
+    }
+  } else {  // complex in
+    const int work = nl * M;
+    for (int t = tid; t < work; t += nth) {
+      int l, p;
+      if (CONTIG) { l = t / M; p = t % M; } else { l = t % nl; p = t / nl; }
+      T2 z = mk<T2>(0, 0);
+      if (l < nlv) z = inC[(long long)(line0 + l) * a.in_line + (long long)p * a.in_pos + (long long)outer * a.in_outer];
+      S(l, p) = z;
+    }
+  }
+  __syncthreads();
+
+  // ---------------- transform ----------------
+  T2* res;
+  if (OP == OP_R2C || OP == OP_DCT2 || OP == OP_C2C_F || OP == OP_C2C_SOLVE)
+    res = smem_fft<-1>(bufA, bufB, nl, 1, nl, a.plan, a.tw.wM);
+  else
+    res = smem_fft<+1>(bufA, bufB, nl, 1, nl, a.plan, a.tw.wM);
+
+  if (OP == OP_C2C_SOLVE) {
+    // normalise and divide by the eigenvalue sum, zero mode -> 0 (poisson.f90:458-471, 991-1005)
+    const int work = nl * M;
+    for (int t = tid; t < work; t += nth) {
+      const int l = t % nl, p = t / nl;
+      if (l < nlv) {
+        const double lam = a.lamA[line0 + l] + (a.lamB ? a.lamB[outer] : 0.0) + a.lamC[p];
+        T2& z = res[(size_t)p * nl + l];
+        if (lam == 0.0) z = mk<T2>(0, 0);
+        else {
+          const T f = (T)(a.scale / lam);
+          z = mk<T2>(z.x * f, z.y * f);
+        }
+      }
+    }
+    __syncthreads();
+    T2* other = (res == bufA) ? bufB : bufA;
+    res = smem_fft<+1>(res, other, nl, 1, nl, a.plan, a.tw.wM);
+  }
+
+  // ---------------- store ----------------
+  const T scale = (T)a.scale;
+  const bool do_scale = (a.scale != 1.0) && (OP != OP_C2C_SOLVE);
+  T2* outC = reinterpret_cast<T2*>(a.out);
+  T* outR = reinterpret_cast<T*>(a.out);
+  auto R = [&](int l, int p) -> const T2& { return res[(size_t)p * nl + l]; };
+  if (OP == OP_R2C) {
+    const int work = nl * (M + 1);
+    for (int t = tid; t < work; t += nth) {
+      int l, kk;
+      if (CONTIG) { l = t / (M + 1); kk = t % (M + 1); } else { l = t % nl; kk = t / nl; }
+      if (l < nlv) {
+        T2 X = r2c_post(res + l, nl, M, kk, a.tw.wN);
+        if (do_scale) X = mk<T2>(X.x * scale, X.y * scale);
+        outC[(long long)(line0 + l) * a.out_line + (long long)kk * a.out_pos + (long long)outer * a.out_outer] = X;
+      }
+    }
+  } else if (OP == OP_DCT2) {
+    const int work = nl * (M + 1);
+    for (int t = tid; t < work; t += nth) {
+      int l, kk;
+      if (CONTIG) { l = t / (M + 1); kk = t % (M + 1); } else { l = t % nl; kk = t / nl; }
+      if (l < nlv) {
+        const T2 Vk = r2c_post(res + l, nl, M, kk, a.tw.wN);
+        const T2 qv = cmul(ldtw<T2>(a.tw.wD, kk), Vk);
+        const long long base = (long long)(line0 + l) * a.out_line + (long long)outer * a.out_outer;
+        T y0 = T(2) * qv.x, y1 = T(-2) * qv.y;
+        if (do_scale) { y0 = y0 * scale; y1 = y1 * scale; }
+        if (kk < n) outR[base + (long long)kk * a.out_pos] = y0;
+        if (kk >= 1 && kk <= M - 1) outR[base + (long long)(n - kk) * a.out_pos] = y1;
+      }
+    }
+  } else if (OP == OP_C2R || OP == OP_DCT3) {
+    double lsum = 0.0;
+    const int work = nl * n;
+    for (int t = tid; t < work; t += nth) {
+      int l, i;
+      if (CONTIG) { l = t / n; i = t % n; } else { l = t % nl; i = t / nl; }
+      if (l < nlv) {
+        int q = i;  // index into v (the c2r output)
+        if (OP == OP_DCT3) q = (i & 1) ? (n - 1 - (i >> 1)) : (i >> 1);
+        const T2 zz = R(l, q >> 1);
+        T x = (q & 1) ? zz.y : zz.x;
+        if (do_scale) x = x * scale;
+        if (ST == ST_FIELD) {
+          int j, k;
+          row_jk<DIM>(line0 + l, outer, j, k);
+          a.fdst[a.L.idx(i + 1, j, kst<DIM>(k))] = x;
+          lsum += (double)x;
+        } else {
+          outR[(long long)(line0 + l) * a.out_line + (long long)i * a.out_pos + (long long)outer * a.out_outer] = x;
+        }
+      }
+    }
+    if (ST == ST_FIELD && a.partial) {
+      // deterministic CTA sum (fixed tree order)
+      __shared__ double red[256];
+      red[tid] = lsum;
+      __syncthreads();
+      for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (tid < s) red[tid] += red[tid + s];
+        __syncthreads();
+      }
+      if (tid == 0) a.partial[(long long)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+    }
+  } else {  // complex out
+    const int work = nl * M;
+    for (int t = tid; t < work; t += nth) {
+      int l, p;
+      if (CONTIG) { l = t / M; p = t % M; } else { l = t % nl; p = t / nl; }
+      if (l < nlv) {
+        T2 z = R(l, p);
+        if (do_scale) z = mk<T2>(z.x * scale, z.y * scale);
+        outC[(long long)(line0 + l) * a.out_line + (long long)p * a.out_pos + (long long)outer * a.out_outer] = z;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Batched Thomas solve along one spectral axis (poisson.f90:348-385, 544-581, 1094-1135,
+// 1233-1274, 1372-1413).  One thread per (column, outer) system.  The pivots depend only on
+// the wavenumbers, so the forward-elimination coefficients c1 and the row factors are
+// tabulated once at set-up with the reference's arithmetic; each solve then runs the
+// right-hand-side recurrences.  FORM3 = the 3D solvers' reciprocal `factor` form, else the
+// 2D solvers' division form.  Arithmetic uses explicitly rounded operations (no FMA
+// contraction) so the zero-mode pivot cancels to exactly zero as in the reference.
+// ------------------------------------------------------------------------------------
+struct ThomasArgs {
+  void* x;                    // spectral data (complex or real), in place
+  long long s_col, s_row, s_outer;
+  int ncol, nouter, n;
+  const double* a;            // sub-diagonal a(row)
+  const double* c1;           // [sys][row] forward coefficients
+  const double* fac;          // [sys][row] reciprocal factor (FORM3) or divisor (2D form); last row: raw pivot
+  int form3;
+};
+
+template <typename V> struct ThomasOps;
+template <> struct ThomasOps<double> {
+  static __device__ __forceinline__ double sub_amul(double r, double a, double d) { return __dsub_rn(r, __dmul_rn(a, d)); }
+  static __device__ __forceinline__ double mul(double r, double f) { return __dmul_rn(r, f); }
+  static __device__ __forceinline__ double div(double r, double f) { return __ddiv_rn(r, f); }
+  static __device__ __forceinline__ double zero() { return 0.0; }
+};
+template <> struct ThomasOps<double2> {
+  static __device__ __forceinline__ double2 sub_amul(double2 r, double a, double2 d) {
+    return make_double2(__dsub_rn(r.x, __dmul_rn(a, d.x)), __dsub_rn(r.y, __dmul_rn(a, d.y)));
+  }
+  static __device__ __forceinline__ double2 mul(double2 r, double f) { return make_double2(__dmul_rn(r.x, f), __dmul_rn(r.y, f)); }
+  static __device__ __forceinline__ double2 div(double2 r, double f) { return make_double2(__ddiv_rn(r.x, f), __ddiv_rn(r.y, f)); }
+  static __device__ __forceinline__ double2 zero() { return make_double2(0.0, 0.0); }
+};
+
+// VS is the storage type (float/float2 in the mixed form), VC the FP64 compute type.
+template <typename VS, typename VC>
+__device__ __forceinline__ VC tconv(VS v);
+template <> __device__ __forceinline__ double tconv<double, double>(double v) { return v; }
+template <> __device__ __forceinline__ double2 tconv<double2, double2>(double2 v) { return v; }
+template <> __device__ __forceinline__ double tconv<float, double>(float v) { return (double)v; }
+template <> __device__ __forceinline__ double2 tconv<float2, double2>(float2 v) { return make_double2(v.x, v.y); }
+template <typename VC, typename VS>
+__device__ __forceinline__ VS tback(VC v);
+template <> __device__ __forceinline__ double tback<double, double>(double v) { return v; }
+template <> __device__ __forceinline__ double2 tback<double2, double2>(double2 v) { return v; }
+template <> __device__ __forceinline__ float tback<double, float>(double v) { return (float)v; }
+template <> __device__ __forceinline__ float2 tback<double2, float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
+
+template <typename VS, typename VC>
+__global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
+  typedef ThomasOps<VC> O;
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  const int outer = blockIdx.y;
+  if (col >= a.ncol) return;
+  VS* X = reinterpret_cast<VS*>(a.x) + (long long)col * a.s_col + (long long)outer * a.s_outer;
+  const long long sys = (long long)outer * a.ncol + col;
+  const long long ns = (long long)a.ncol * a.nouter;  // tables are [row][system]
+  const double* c1 = a.c1 + sys;
+  const double* f = a.fac + sys;
+  const int n = a.n;
+  // forward sweep: d1 overwrites the right-hand side
+  VC d = tconv<VS, VC>(X[0]);
+  d = a.form3 ? O::mul(d, f[0]) : O::div(d, f[0]);
+  X[0] = tback<VC, VS>(d);
+  for (int t = 1; t < n - 1; ++t) {
+    VC r = tconv<VS, VC>(X[(long long)t * a.s_row]);
+    r = O::sub_amul(r, a.a[t], d);
+    d = a.form3 ? O::mul(r, f[t * ns]) : O::div(r, f[t * ns]);
+    X[(long long)t * a.s_row] = tback<VC, VS>(d);
+  }
+  {
+    const double piv = f[(n - 1) * ns];
+    VC r = tconv<VS, VC>(X[(long long)(n - 1) * a.s_row]);
+    if (piv != 0.0) d = O::div(O::sub_amul(r, a.a[n - 1], d), piv);
+    else d = O::zero();
+  }
+  // backward sweep
+  VC xn = d;
+  X[(long long)(n - 1) * a.s_row] = tback<VC, VS>(xn);
+  for (int t = n - 2; t >= 0; --t) {
+    VC dt = tconv<VS, VC>(X[(long long)t * a.s_row]);
+    xn = O::sub_amul(dt, c1[t * ns], xn);
+    X[(long long)t * a.s_row] = tback<VC, VS>(xn);
+  }
+}
+
+// Tabulate c1 and the row factors for every (col, outer) system with the reference's
+// operation order.  lamA indexed by col, lamB by outer (nullptr in 2D).
+__global__ void k_thomas_tables(int ncol, int nouter, int n, const double* a, const double* b, const double* c,
+                                const double* lamA, const double* lamB, int form3, double* c1, double* fac) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  const int outer = blockIdx.y;
+  if (col >= ncol) return;
+  const long long sys = (long long)outer * ncol + col;
+  const long long ns = (long long)ncol * nouter;  // [row][system]
+  double* C1 = c1 + sys;
+  double* F = fac + sys;
+  const double mA = lamA[col];
+  const double mB = lamB ? lamB[outer] : 0.0;
+  if (form3) {
+    // factor = 1/(b + mwn_x + mwn_y - a*c1)   (poisson.f90:1096, 1105, 1114)
+    double fct = __ddiv_rn(1.0, __dadd_rn(__dadd_rn(b[0], mA), mB));
+    C1[(0) * ns] = __dmul_rn(c[0], fct);
+    F[(0) * ns] = fct;
+    for (int t = 1; t < n - 1; ++t) {
+      fct = __ddiv_rn(1.0, __dsub_rn(__dadd_rn(__dadd_rn(b[t], mA), mB), __dmul_rn(a[t], C1[(t - 1) * ns])));
+      C1[(t) * ns] = __dmul_rn(c[t], fct);
+      F[(t) * ns] = fct;
+    }
+    F[(n - 1) * ns] = __dsub_rn(__dadd_rn(__dadd_rn(b[n - 1], mA), mB), __dmul_rn(a[n - 1], C1[(n - 2) * ns]));
+    C1[(n - 1) * ns] = 0.0;
+  } else {
+    // c1 = c/(b - a*c1 + mwn);  d1 = (r - a*d1)/(b + mwn - a*c1)   (poisson.f90:350-366)
+    C1[(0) * ns] = __ddiv_rn(c[0], __dadd_rn(b[0], mA));
+    F[(0) * ns] = __dadd_rn(b[0], mA);
+    for (int t = 1; t < n - 1; ++t) {
+      C1[(t) * ns] = __ddiv_rn(c[t], __dadd_rn(__dsub_rn(b[t], __dmul_rn(a[t], C1[(t - 1) * ns])), mA));
+      F[(t) * ns] = __dsub_rn(__dadd_rn(b[t], mA), __dmul_rn(a[t], C1[(t - 1) * ns]));
+    }
+    F[(n - 1) * ns] = __dsub_rn(__dadd_rn(b[n - 1], mA), __dmul_rn(a[n - 1], C1[(n - 2) * ns]));
+    C1[(n - 1) * ns] = 0.0;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Correction and pressure update (navier_stokes.f90:505-566): v = v* - dt grad(phi)/rhof,
+// p = p + phi.  Ghosts of v and p are refilled afterwards.
+// ------------------------------------------------------------------------------------
+template <typename T>
+struct CorrArgs {
+  const T *us, *vs, *ws, *phi;
+  T *u, *v, *w, *p;
+  double id[3];
+  double dt_host;
+  int iso, use_dev_dt, rhof_one;
+  double rhof;
+};
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) k_correct(Layout L, const StepScalars* __restrict__ sc, CorrArgs<T> a) {
+  const long long ncell = (long long)L.n0 * L.n1 * L.n2;
+  const T dt = (T)(a.use_dev_dt ? sc->dt : a.dt_host);
+  const T f = a.rhof_one ? dt : (T)((double)dt / a.rhof);
+  const T idx = (T)a.id[0];
+  const T idy = a.iso ? idx : (T)a.id[1];
+  const T idz = a.iso ? idx : (T)a.id[2];
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(t % L.n0);
+    const long long r = t / L.n0;
+    const int j = 1 + (int)(r % L.n1);
+    const int k = 1 + (int)(r / L.n1);
+    const long long c = L.idx(i, j, kst<DIM>(k));
+    const T ph = a.phi[c];
+    a.u[c] = a.us[c] - (a.phi[c + 1] - ph) * idx * f;
+    a.v[c] = a.vs[c] - (a.phi[c + L.sx] - ph) * idy * f;
+    if (DIM == 3) a.w[c] = a.ws[c] - (a.phi[c + L.sp] - ph) * idz * f;
+    a.p[c] = a.p[c] + ph;
+  }
+}
+
+// Mean removal over the interior (poisson.f90:491-503, 1159-1171): every CTA sums the
+// per-line partials in the same order, then subtracts mean/float(nx*ny*nz).
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) k_mean_subtract(Layout L, const double* partial, int npart, double ncell_f,
+                                                       StepScalars* sc, T* phi) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int q = threadIdx.x; q < npart; q += blockDim.x) s += partial[q];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  const double m = red[0] / ncell_f;
+  if (blockIdx.x == 0 && threadIdx.x == 0) sc->mean = m;
+  const T mt = (T)m;
+  const long long ncell = (long long)L.n0 * L.n1 * L.n2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(t % L.n0);
+    const long long r = t / L.n0;
+    const int j = 1 + (int)(r % L.n1);
+    const int k = 1 + (int)(r / L.n1);
+    const long long c = L.idx(i, j, kst<DIM>(k));
+    phi[c] = phi[c] - mt;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Diagnostics (navier_stokes.f90:570-619): signed max of div(v) and max(|u|+|v|+|w|),
+// per-CTA partials reduced by k_finalize in a fixed order.
+// ------------------------------------------------------------------------------------
+template <typename T>
+struct CheckArgs {
+  const T *u, *v, *w;
+  double id[3];
+  int iso, want_div;
+  double* pdiv;
+  double* pvel;
+  int* nan_flag;
+};
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) k_checks(Layout L, CheckArgs<T> a) {
+  const long long ncell = (long long)L.n0 * L.n1 * L.n2;
+  T md = -INFINITY, mv = 0;
+  bool bad = false;
+  const T idx = (T)a.id[0];
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(t % L.n0);
+    const long long r = t / L.n0;
+    const int j = 1 + (int)(r % L.n1);
+    const int k = 1 + (int)(r / L.n1);
+    const long long c = L.idx(i, j, kst<DIM>(k));
+    const T uc = a.u[c], vc = a.v[c];
+    T vel = fabs(uc) + fabs(vc);
+    T d = 0;
+    if (a.want_div) {
+      if (a.iso) d = (uc - a.u[c - 1]) * idx + (vc - a.v[c - L.sx]) * idx;
+      else d = (uc - a.u[c - 1]) * (T)a.id[0] + (vc - a.v[c - L.sx]) * (T)a.id[1];
+    }
+    if (DIM == 3) {
+      const T wc = a.w[c];
+      vel = vel + fabs(wc);
+      if (a.want_div) d = d + (wc - a.w[c - L.sp]) * (a.iso ? idx : (T)a.id[2]);
+    }
+    if (vel != vel || d != d) bad = true;
+    if (vel > mv) mv = vel;
+    if (d > md) md = d;
+  }
+  __shared__ double r1[256], r2[256];
+  r1[threadIdx.x] = (double)md;
+  r2[threadIdx.x] = (double)mv;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      r1[threadIdx.x] = fmax(r1[threadIdx.x], r1[threadIdx.x + h]);
+      r2[threadIdx.x] = fmax(r2[threadIdx.x], r2[threadIdx.x + h]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    a.pdiv[blockIdx.x] = r1[0];
+    a.pvel[blockIdx.x] = r2[0];
+  }
+  if (bad) atomicOr(a.nan_flag, 1);
+}
+
+// Fold the check partials: maxdiv, maxvel, maxCFL = dt*maxvel/delta (navier_stokes.f90:593, 617).
+__global__ void k_finalize(const double* pdiv, const double* pvel, int np, StepScalars* sc, double delta, double dt_host,
+                           int use_dev_dt, const int* nan_flag) {
+  __shared__ double r1[256], r2[256];
+  double md = -INFINITY, mv = 0.0;
+  for (int q = threadIdx.x; q < np; q += blockDim.x) {
+    md = fmax(md, pdiv[q]);
+    mv = fmax(mv, pvel[q]);
+  }
+  r1[threadIdx.x] = md;
+  r2[threadIdx.x] = mv;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      r1[threadIdx.x] = fmax(r1[threadIdx.x], r1[threadIdx.x + h]);
+      r2[threadIdx.x] = fmax(r2[threadIdx.x], r2[threadIdx.x + h]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double dt = use_dev_dt ? sc->dt : dt_host;
+    sc->maxdiv = r1[0];
+    sc->maxvel = r2[0];
+    sc->maxCFL = dt * r2[0] / delta;
+    if (*nan_flag) sc->err = 1;
+  }
+}
+
+// Start-of-step scalars: update_timestep when constant_CFL (navier_stokes.f90:670-730),
+// then the AB2 coefficients (:157-158) and the Poisson right-hand-side scale (:118).
+__global__ void k_prologue(StepScalars* sc, int constant_cfl, double cfl, double delta, double density, double rhof) {
+  if (threadIdx.x != 0) return;
+  double dt;
+  if (constant_cfl) {
+    sc->dt_o = sc->dt;
+    const double mv = sc->maxvel;
+    if (mv > 0.0) sc->dt_conv = cfl * delta / mv;
+    else sc->dt_conv = 1.0;
+    dt = fmin(sc->dt_conv, sc->dt_visc);
+    if (dt > 1.1 * sc->dt_o) dt = 1.1 * sc->dt_o;
+    sc->dt = dt;
+  } else {
+    dt = sc->dt;  // written by the host before the step
+  }
+  sc->A = 1.0 + 0.5 * dt / sc->dt_o;
+  sc->B = -0.5 * dt / sc->dt_o;
+  sc->rho_over_dt = density / dt;
+  sc->dt_over_rhof = dt / rhof;
+}
+
+}  // namespace fen

@@ -1,0 +1,70 @@
+// Shared device types for the FEN projection-step kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fen {
+
+// Field boundary-condition types (FEN src/scalar.f90:17-22).
+enum { FT_PERIODIC = 0, FT_DIRICHLET = 1, FT_NEUMANN = 2 };
+// Faces in the reference order (scalar.f90:24-36).
+enum { F_LEFT = 0, F_RIGHT = 1, F_BOTTOM = 2, F_TOP = 3, F_FRONT = 4, F_BACK = 5 };
+
+// Ghosted field in HBM.  Fortran index (i, j, k), i in [0, n0+1], j in [0, n1+1] and, in
+// 3D, k in [0, n2+1] (gl = 1, scalar.f90:79-81).  Rows are padded to a multiple of four
+// elements and shifted by `off` = 3 so the first interior element of every row (i = 1)
+// starts on a 32-byte sector.  In 2D only the k = 1 plane is stored (storage plane 0):
+// FEN allocates z ghost planes there but never reads or fills them (scalar.f90:344).
+struct Layout {
+  int dim;
+  int n0, n1, n2;   // interior cells (n2 = 1 in 2D)
+  int sx;           // row pitch, elements
+  int sy;           // rows per plane (n1 + 2)
+  long long sp;     // plane pitch, elements
+  int off;
+  long long total;  // elements to allocate
+  __host__ __device__ __forceinline__ long long idx(int i, int j, int ks) const {
+    return (long long)off + i + (long long)sx * j + sp * ks;
+  }
+};
+
+// Storage plane of Fortran plane k.
+template <int DIM>
+__host__ __device__ __forceinline__ int kst(int k) { return DIM == 3 ? k : 0; }
+
+// Boundary description of one ghosted field.
+struct FieldBC {
+  int type[6];
+  const double* val[6];  // Dirichlet values over the ghosted face extents; nullptr = 0
+  int c;                 // location: 'c', 'x', 'y', 'z'
+};
+
+template <typename T> struct cpx;
+template <> struct cpx<double> { typedef double2 t; };
+template <> struct cpx<float> { typedef float2 t; };
+
+template <typename T2> __device__ __forceinline__ T2 mk(decltype(T2::x) a, decltype(T2::x) b) { T2 r; r.x = a; r.y = b; return r; }
+template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { return mk<T2>(a.x + b.x, a.y + b.y); }
+template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { return mk<T2>(a.x - b.x, a.y - b.y); }
+template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) { return mk<T2>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+// a * conj(b)
+template <typename T2> __device__ __forceinline__ T2 cmulc(T2 a, T2 b) { return mk<T2>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
+template <typename T2> __device__ __forceinline__ T2 cconj(T2 a) { return mk<T2>(a.x, -a.y); }
+// multiply by -i (forward) or +i (inverse)
+template <int DIR, typename T2> __device__ __forceinline__ T2 cmul_mi(T2 a) { return DIR < 0 ? mk<T2>(a.y, -a.x) : mk<T2>(-a.y, a.x); }
+
+// Per-step scalars kept on the device so a captured step needs no host round trip.
+struct StepScalars {
+  double dt, dt_o;          // navier_stokes.f90:24-33
+  double A, B;              // AB2 coefficients (:157-158)
+  double rho_over_dt;       // phi = div * rho / dt (:118)
+  double dt_over_rhof;      // correction factor (:533)
+  double maxvel;            // max(|u|+|v|+|w|) of the current velocity (:599-611)
+  double maxdiv, maxCFL;    // checks (:570-619)
+  double mean;              // Poisson mean removal (poisson.f90:491-503)
+  double dt_visc, dt_conv;
+  int err;                  // NaN detected in the reductions
+  int pad;
+};
+
+}  // namespace fen

@@ -1,0 +1,128 @@
+/*
+ * fen_gpu.h — C ABI of the GB300 projection-step library (libfen_gb300.so).
+ *
+ * Drop-in boundary for FEN's incompressible projection step: the Fortran modules
+ * solver_mod, navier_stokes_mod, poisson_mod and fields_mod keep their public interfaces
+ * and bind these entry points through iso_c_binding.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *   - Every entry point returns 0 on success or a negative FEN_ERR_* code; the message of
+ *     the last failure on the calling thread is returned by fen_last_error().
+ *   - Host field arrays use FEN's Fortran layout with one ghost layer:
+ *       f(0:nx+1, 0:ny+1, 0:nz+1), x fastest (src/scalar.f90:79-81);
+ *     in 2D the z extent is 0:2 and only plane k = 1 is read or written.
+ *   - One context = one grid + one solver instance on the current CUDA device, with one
+ *     stream.  Calls on one context must be serialised by the caller; distinct contexts are
+ *     independent.  Device state persists between calls; host arrays are never retained.
+ */
+#ifndef FEN_GPU_H
+#define FEN_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Physical boundary conditions (src/grid.f90:41-46). */
+enum { FEN_BC_PERIODIC = 0, FEN_BC_WALL = 1, FEN_BC_INFLOW = 2, FEN_BC_OUTFLOW = 3 };
+/* Faces in the reference order (src/scalar.f90:24-36). */
+enum { FEN_LEFT = 0, FEN_RIGHT = 1, FEN_BOTTOM = 2, FEN_TOP = 3, FEN_FRONT = 4, FEN_BACK = 5 };
+/* Field identifiers (module state of navier_stokes_mod, src/navier_stokes.f90:36-37). */
+enum {
+  FEN_U = 0, FEN_V = 1, FEN_W = 2, FEN_P = 3, FEN_PHI = 4,
+  FEN_DVO_X = 5, FEN_DVO_Y = 6, FEN_DVO_Z = 7,
+  FEN_S_X = 8, FEN_S_Y = 9, FEN_S_Z = 10
+};
+/* Arithmetic forms. */
+enum { FEN_FP64 = 0, FEN_MIXED = 1 };
+/* Error codes. */
+enum {
+  FEN_OK = 0,
+  FEN_ERR_ARG = -1,      /* invalid argument or size */
+  FEN_ERR_BC = -2,       /* boundary-condition combination without a Poisson solver */
+  FEN_ERR_CUDA = -3,     /* CUDA runtime failure */
+  FEN_ERR_NAN = -4,      /* NaN detected by the step diagnostics */
+  FEN_ERR_NOMEM = -5,    /* device allocation failed */
+  FEN_ERR_STATE = -6     /* call out of order (e.g. step before set_timestep) */
+};
+
+typedef struct fen_ctx fen_ctx;
+
+/* Grid + solver parameters: grid%setup (src/grid.f90:67-200) and the navier_stokes_mod
+ * module variables density, viscosity, g, CFL, constant_CFL (src/navier_stokes.f90:18-45). */
+typedef struct {
+  int dim;              /* 2 or 3 (the reference's -DDIM) */
+  int nx, ny, nz;       /* interior cells; nz = 1 in 2D */
+  double lx, ly, lz;    /* domain lengths */
+  double origin[3];
+  int bc[6];            /* FEN_BC_* per face (left, right, bottom, top, front, back) */
+  int aniso;            /* 0: delta = Lx/Nx on every axis (grid.f90:140); 1: Li/Ni per axis */
+  double density, viscosity;
+  double g[3];
+  double cfl;
+  int constant_cfl;
+  int precision;        /* FEN_FP64 or FEN_MIXED */
+} fen_params;
+
+/* Per-step diagnostics (navier_stokes.f90:24-33, 570-619). */
+typedef struct {
+  double dt, dt_o, maxdiv, maxcfl, maxvel, dt_visc;
+  int nan_detected;
+  int poisson_solver;   /* 0 pp, 1 pn, 2 nn, 3 ppp, 4 ppn, 5 npn, 6 nnn, 7 pnp */
+} fen_status;
+
+/* grid%setup + init_solver: allocate_navier_stokes_fields + init_poisson_solver
+ * (src/solver.f90:34-99, src/navier_stokes.f90:752-1067, src/poisson.f90:57-113). */
+int fen_ctx_create(const fen_params* params, fen_ctx** out);
+/* destroy_solver (src/solver.f90:333-357) + destroy_poisson_solver (poisson.f90:1456). */
+int fen_ctx_destroy(fen_ctx* ctx);
+const char* fen_last_error(void);
+
+/* Host <-> device transfer of one field (Fortran layout above).  fen_upload copies the
+ * whole ghosted array (interior and ghosts) like a Fortran assignment to v%x%f. */
+int fen_upload(fen_ctx* ctx, int field, const double* host);
+int fen_download(fen_ctx* ctx, int field, double* host);
+/* scalar%update_ghost_nodes (src/scalar.f90:223-396) on the device copy. */
+int fen_update_ghost_nodes(fen_ctx* ctx, int field);
+/* Dirichlet values of one face of one field: field%bc%left ... (scalar.f90:28-36).  The
+ * array covers the ghosted face extents as FEN allocates them (scalar.f90:89-95). */
+int fen_set_bc_values(fen_ctx* ctx, int field, int face, const double* values);
+/* Override a field boundary type (-1 halo is not used on one device): field%bc%type_* */
+int fen_set_bc_type(fen_ctx* ctx, int field, int face, int type);
+
+/* set_timestep (src/navier_stokes.f90:623-666): dt = min(CFL delta/U, dt_visc); dt_o = dt. */
+int fen_set_timestep(fen_ctx* ctx, double U, double* dt);
+/* Set dt_o explicitly (module variable navier_stokes_mod::dt_o, navier_stokes.f90:33). */
+int fen_set_dt_o(fen_ctx* ctx, double dt_o);
+/* advance_solution => navier_stokes_solver (src/navier_stokes.f90:50-136).  dt is
+ * intent(inout): updated when constant_cfl is set. */
+int fen_advance_solution(fen_ctx* ctx, int step, double* dt);
+/* nsteps consecutive navier_stokes_solver calls without host synchronisation between them
+ * (one captured CUDA graph replayed); dt as above after the last step. */
+int fen_advance_n(fen_ctx* ctx, int nsteps, double* dt);
+/* Diagnostics of the last step (maxdiv, maxCFL, dt, dt_o). */
+int fen_get_status(fen_ctx* ctx, fen_status* out);
+
+/* solve_poisson(phi) on the device copy of FEN_PHI (src/poisson.f90:21-29, 306-1451). */
+int fen_solve_poisson(fen_ctx* ctx);
+/* divergence(v, div) over the interior (src/fields.f90:120-153); out is nx*ny*nz, x fastest. */
+int fen_divergence(fen_ctx* ctx, double* out);
+/* compute_explicit_terms(dv) with the current v, p (src/navier_stokes.f90:217-257); the
+ * three components go to out (3 * nx*ny*nz, x fastest). */
+int fen_explicit_terms(fen_ctx* ctx, double* out);
+
+/* Synchronise the context stream. */
+int fen_sync(fen_ctx* ctx);
+/* Number of kernels this library launched on the context since creation. */
+long long fen_kernel_launches(fen_ctx* ctx);
+/* Time `nsteps` steps on the device with CUDA events on the context stream (graph replay,
+ * no host work inside the timed region); returns milliseconds. */
+int fen_time_steps(fen_ctx* ctx, int nsteps, double dt, double* ms);
+/* Per-stage device time of one step, measured with CUDA events on the context stream:
+ * out[0..7] = predictor, ghost(v*), forward transforms, spectral solve, inverse
+ * transform(s), correction, ghost(v,p,phi), checks (milliseconds, averaged over reps). */
+int fen_profile_step(fen_ctx* ctx, int reps, double dt, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FEN_GPU_H */

@@ -1,0 +1,116 @@
+"""Shared test cases: FEN's initial conditions and manufactured solutions.
+
+Field arrays are numpy (k, j, i) views of FEN's f(0:nx+1, 0:ny+1, 0:nz+1); MAC placement
+as in the reference test initialisers (test/small_test/navier_stokes/taylor_green_vortex/
+taylor_green_vortex.f90:94-102): u at (i d, (j-1/2) d), v at ((i-1/2) d, j d), p at cell
+centres, w at (., ., k d).
+"""
+import numpy as np
+
+from oracle import oracle as O
+
+PI = np.pi
+
+
+def coords(n, d, kind):
+    """Coordinates of ghosted indices 0..n+1: 'c' cell centre, 'f' face."""
+    i = np.arange(n + 2, dtype=np.float64)
+    return i * d if kind == "f" else (i - 0.5) * d
+
+
+def mac_grids(dim, n, d):
+    """Meshes (k, j, i) for u, v, w, p positions."""
+    out = {}
+    nz = n[2] if dim == 3 else 1
+    for name, kinds in {"u": "fcc", "v": "cfc", "w": "ccf", "p": "ccc"}.items():
+        x = coords(n[0], d[0], kinds[0])
+        y = coords(n[1], d[1], kinds[1])
+        z = coords(nz, d[2], kinds[2]) if dim == 3 else np.array([0.0, 0.5 * d[2], d[2]])
+        Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+        out[name] = (X, Y, Z)
+    return out
+
+
+def tgv2d_fields(n, L):
+    """2D Taylor-Green vortex: u = sin x cos y, v = -cos x sin y, p = (cos 2x + cos 2y)/4."""
+    d = L / n
+    g = mac_grids(2, (n, n, 1), (d, d, d))
+    X, Y, _ = g["u"]
+    u = np.sin(X) * np.cos(Y)
+    X, Y, _ = g["v"]
+    v = -np.cos(X) * np.sin(Y)
+    X, Y, _ = g["p"]
+    p = (np.cos(2 * X) + np.cos(2 * Y)) / 4
+    return u, v, p
+
+
+def tgv3d_fields(n, L):
+    """3D Taylor-Green vortex: u = sin x cos y cos z, v = -cos x sin y cos z, w = 0,
+    p = (cos 2x + cos 2y)(cos 2z + 2)/16."""
+    d = L / n
+    g = mac_grids(3, (n, n, n), (d, d, d))
+    X, Y, Z = g["u"]
+    u = np.sin(X) * np.cos(Y) * np.cos(Z)
+    X, Y, Z = g["v"]
+    v = -np.cos(X) * np.sin(Y) * np.cos(Z)
+    w = np.zeros_like(u)
+    X, Y, Z = g["p"]
+    p = (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2) / 16
+    return u, v, w, p
+
+
+def random_interior(shape, rng, dim):
+    a = np.zeros(shape)
+    if dim == 3:
+        a[1:-1, 1:-1, 1:-1] = rng.uniform(-1, 1, size=(shape[0] - 2, shape[1] - 2, shape[2] - 2))
+    else:
+        a[1, 1:-1, 1:-1] = rng.uniform(-1, 1, size=(shape[1] - 2, shape[2] - 2))
+    return a
+
+
+def interior(a, dim):
+    return a[1:-1, 1:-1, 1:-1] if dim == 3 else a[1, 1:-1, 1:-1]
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+# Manufactured Poisson solutions of test/small_test/poisson/convergence_rate/
+# convergence_rate.f90:167-223 (domain [0,1]^d, cell centres).
+def poisson_case(name):
+    s = lambda x: np.sin(2 * PI * x)
+    c = lambda x: np.cos(2 * PI * x)
+    cases = {
+        "pp": (2, [O.PERIODIC] * 4, lambda X, Y, Z: -8 * PI * PI * s(X) * c(Y), lambda X, Y, Z: s(X) * c(Y)),
+        "pn": (2, [O.PERIODIC, O.PERIODIC, O.WALL, O.WALL], lambda X, Y, Z: -4 * PI * PI * (s(X) + c(Y)),
+               lambda X, Y, Z: s(X) + c(Y)),
+        "nn": (2, [O.WALL] * 4, lambda X, Y, Z: -8 * PI * PI * c(X) * c(Y), lambda X, Y, Z: c(X) * c(Y)),
+        "ppp": (3, [O.PERIODIC] * 6, lambda X, Y, Z: -12 * PI * PI * s(X) * c(Y) * s(Z),
+                lambda X, Y, Z: s(X) * c(Y) * s(Z)),
+        "ppn": (3, [O.PERIODIC] * 4 + [O.WALL] * 2, lambda X, Y, Z: -4 * PI * PI * (s(X) + s(Y) + c(Z)),
+                lambda X, Y, Z: s(X) + s(Y) + c(Z)),
+        "npn": (3, [O.WALL, O.WALL, O.PERIODIC, O.PERIODIC, O.WALL, O.WALL],
+                lambda X, Y, Z: -12 * PI * PI * c(X) * c(Y) * c(Z), lambda X, Y, Z: c(X) * c(Y) * c(Z)),
+        "nnn": (3, [O.WALL] * 6, lambda X, Y, Z: -12 * PI * PI * c(X) * c(Y) * c(Z),
+                lambda X, Y, Z: c(X) * c(Y) * c(Z)),
+        # walls in y with x, z periodic (the channel's solver; beyond the reference's dispatch)
+        "pnp": (3, [O.PERIODIC, O.PERIODIC, O.WALL, O.WALL, O.PERIODIC, O.PERIODIC],
+                lambda X, Y, Z: -4 * PI * PI * (s(X) + c(Y) + s(Z)), lambda X, Y, Z: s(X) + c(Y) + s(Z)),
+    }
+    return cases[name]
+
+
+def poisson_rhs_grid(dim, N):
+    d = 1.0 / N
+    x = (np.arange(1, N + 1) - 0.5) * d
+    if dim == 2:
+        Y, X = np.meshgrid(x, x, indexing="ij")
+        return X, Y, np.zeros_like(X)
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    return X, Y, Z
+
+
+def convergence_slope(Ns, errs):
+    return -np.polyfit(np.log(np.asarray(Ns, float)), np.log(np.asarray(errs)), 1)[0]

@@ -1,0 +1,45 @@
+"""CPU checks of the C ABI: the library builds for sm_103a, loads, and exports every entry
+point declared in include/fen_gpu.h.  No compute call is made here."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "fen_gpu.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(fen_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("fen_ctx_create", "fen_advance_solution", "fen_solve_poisson", "fen_update_ghost_nodes"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(fen_lib):
+    missing = [s for s in declared_symbols() if not hasattr(fen_lib, s)]
+    assert not missing, missing
+
+
+def test_error_path_without_device(fen_lib):
+    import fen_gb300 as F
+
+    p = F._Params()
+    p.dim, p.nx, p.ny, p.nz = 5, 8, 8, 1
+    h = ctypes.c_void_p()
+    rc = fen_lib.fen_ctx_create(ctypes.byref(p), ctypes.byref(h))
+    assert rc == -1
+    assert b"dim" in fen_lib.fen_last_error()
+
+
+def test_python_api_fails_loudly_when_library_missing(tmp_path):
+    import fen_gb300 as F
+
+    with pytest.raises(F.FenError):
+        F.load_library(str(tmp_path / "missing.so"))
