@@ -1,0 +1,362 @@
+#!/usr/bin/env python3
+"""Benchmark: FEN projection step on GB300 — Mcell-steps/s.
+
+Workload (default): 3D Taylor-Green vortex, periodic [0, 2 pi]^3, 256^3 MAC grid, FP64,
+Re = 1600 (nu = 1/1600), dt from CFL = 0.5 (constant-CFL mode), fast direct Poisson solve
+by FFT in all three directions.  A "step" is one navier_stokes_solver time step
+(predictor, ghost fill, Poisson solve, correction, pressure update, diagnostics).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config tgv3d|tgv2d|channel]
+
+One JSON line on rank 0.  `value` is device time (CUDA events on the library's stream, K
+captured steps replayed back to back, inputs resident in HBM); `e2e` is the same metric
+through the C ABI with host buffers (pinned upload of u, v, w, p, K advance_solution calls
+each returning dt and the diagnostics to the host, download of u, v, w, p).
+Multi-GPU: the path does not shard (one grid per device); N ranks run N independent
+replicas (weak scaling) and `value` sums their cells over the slowest rank's time.
+`--impl reference` times the CPU restatement of the reference (the oracle port; the
+Fortran/MPI/FFTW reference cannot be built on these machines) on rank 0's host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+# Algorithmic words per cell-step (FP64 words; 3D / 2D), the compulsory reads and writes of
+# each stage counted once, complex half-spectra as one real word per cell.
+WORDS_3D = {"predictor": 13, "forward": 4, "spectral": 6, "inverse": 9 - 7, "correct": 7, "ghost": 0, "checks": 0}
+STAGES = ["predictor", "ghost_vstar", "forward_x", "spectral", "inverse_x", "correct", "ghost", "checks"]
+# bytes moved by each stage of this implementation per cell (FP64), used for the roofline
+STAGE_BYTES_3D = {
+    "predictor": 8 * 13,      # read u,v,w,p,dv_o(3); write v*(3), dv_o(3)
+    "forward_x": 8 * 4,       # read v*(3); write half-spectrum (16 B x 1/2 per cell)
+    "spectral": 8 * 6,        # y fwd, z fwd+solve+inv, y inv: 3 x (read + write) half-spectrum
+    "inverse_x": 8 * 2,       # read half-spectrum; write phi
+    "correct": 8 * 9,         # read v*(3), phi; read+write p; write v(3)
+}
+
+CONFIGS = {
+    "tgv3d": dict(dim=3, n=(256, 256, 256), L=(2 * np.pi,) * 3, nu=1.0 / 1600, cfl=0.5, constant_cfl=True,
+                  bc=["Periodic"] * 6, desc="3D Taylor-Green vortex 256^3, Re=1600, CFL=0.5, FP64, FFT x/y/z"),
+    "tgv2d": dict(dim=2, n=(128, 128, 1), L=(2 * np.pi, 2 * np.pi, 2 * np.pi / 128), nu=0.01, dt=1e-3,
+                  bc=["Periodic"] * 4, desc="2D Taylor-Green vortex 128^2, nu=0.01, dt=1e-3, FP64"),
+    "channel": dict(dim=3, n=(512, 256, 384), L=(4 * np.pi, 2.0, 4 * np.pi / 3), nu=1.0 / 180, cfl=0.5,
+                    constant_cfl=True, g=(1.0, 0.0, 0.0), aniso=True,
+                    bc=["Periodic", "Periodic", "Wall", "Wall", "Periodic", "Periodic"],
+                    desc="channel 512x256x384, Re_tau=180, walls in y, CFL=0.5, FP64, FFT x/z + Thomas y"),
+}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def init_fields(name, cfg, n, shape):
+    """Initial fields of workload `name` on an n-cell grid, Fortran layout (k, j, i) with ghosts."""
+    from tests import cases as C
+
+    L = cfg["L"]
+    if name == "tgv3d":
+        return dict(zip("uvwp", C.tgv3d_fields(n[0], L[0])))
+    if name == "tgv2d":
+        u, v, p = C.tgv2d_fields(n[0], L[0])
+        return {"u": u, "v": v, "p": p}
+    # channel: laminar Poiseuille u = (1 - y^2)/(2 nu) plus seeded uniform noise of 5% of
+    # the centreline velocity on u, v, w (PCG64 seed 1234, Fortran order)
+    rng = np.random.Generator(np.random.PCG64(1234))
+    dy = L[1] / n[1]
+    yc = -1.0 + (np.arange(n[1] + 2) - 0.5) * dy
+    Uc = 1.0 / (2 * cfg["nu"])
+    out = {}
+    for key in "uvw":
+        a = np.zeros(shape)
+        noise = rng.uniform(-1.0, 1.0, size=(n[2], n[1], n[0]))
+        a[1:-1, 1:-1, 1:-1] = 0.05 * Uc * noise
+        if key == "u":
+            a[1:-1, 1:-1, 1:-1] += ((1 - yc[1:-1] ** 2) / (2 * cfg["nu"]))[None, :, None]
+        out[key] = a
+    out["p"] = np.zeros(shape)
+    return out
+
+
+def start_velocity(name, cfg):
+    """Velocity scale given to set_timestep (navier_stokes.f90:641): U = 1 for the TGV,
+    the centreline velocity 1/(2 nu) for the channel."""
+    return 1.0 if name == "tgv3d" else 1.0 / (2 * cfg["nu"])
+
+
+def make_oracle(name, cfg, n, nthreads):
+    from oracle import oracle as O
+
+    bcmap = {"Periodic": O.PERIODIC, "Wall": O.WALL}
+    L = list(cfg["L"])
+    if name == "tgv2d":
+        L[2] = L[0] / n[0]
+    o = O.Oracle(cfg["dim"], n, L, bc=[bcmap[b] for b in cfg["bc"]], viscosity=cfg["nu"],
+                 g=cfg.get("g", (0, 0, 0)), cfl=cfg.get("cfl", 1.0), constant_cfl=cfg.get("constant_cfl", False),
+                 aniso=cfg.get("aniso", False), nthreads=nthreads)
+    f = init_fields(name, cfg, n, o.shape)
+    for key, fid in (("u", O.U), ("v", O.V), ("w", O.W), ("p", O.P)):
+        if key in f:
+            o.field(fid)[...] = f[key]
+            o.update_ghost_nodes(fid)
+    if cfg.get("constant_cfl"):
+        dt = o.set_timestep(start_velocity(name, cfg))
+    else:
+        dt = cfg["dt"]
+        o.dt_o = dt
+    return o, dt
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(name, cfg, max_seconds=20.0):
+    """Time the oracle port on the host cores on a bounded sample of the workload: the full
+    grid when a step fits the budget, else the same configuration on a coarser grid (the
+    metric is per cell)."""
+    nthreads = os.cpu_count() or 1
+    n = list(cfg["n"])
+    est = n[0] * n[1] * n[2] / (2e6 * nthreads)  # ~2 Mcell-steps/s per core
+    while est > max_seconds / 3 and n[0] > 32:
+        n = [x // 2 for x in n[:2]] + [n[2] // 2 if cfg["dim"] == 3 else 1]
+        est /= 8 if cfg["dim"] == 3 else 4
+    o, dt = make_oracle(name, cfg, n, nthreads)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        dt = o.step(dt)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > max_seconds or steps >= 50:
+            break
+    cells = n[0] * n[1] * n[2]
+    return {"value": round(cells * steps / el / 1e6, 3), "unit": "Mcell-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{steps} steps of {name} at {n[0]}x{n[1]}x{n[2]} ({el:.1f} s), CPU restatement (not FFTW)"}
+
+
+def run_reference(args, name, cfg):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    n = cfg["n"]
+    o, dt = make_oracle(name, cfg, n, nthreads)
+    for _ in range(args.warmup):
+        dt = o.step(dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dt = o.step(dt)
+    el = time.perf_counter() - t0
+    cells = n[0] * n[1] * n[2]
+    v = cells * args.steps / el / 1e6
+    line = {"impl": "reference", "metric": "Mcell-steps/s", "value": round(v, 3), "unit": "Mcell-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": cfg["desc"], "cells": cells, "flush": "inputs larger than L2"},
+            "cpu_baseline": {"value": round(v, 3), "unit": "Mcell-steps/s", "cores": nthreads, "kind": "port",
+                             "sample": f"{args.steps} timed steps of the full {n[0]}x{n[1]}x{n[2]} grid; FEN's "
+                                       "Fortran/MPI/FFTW build is not available here, so the oracle port runs"},
+            "e2e": {"value": round(v, 3), "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="tgv3d", choices=list(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=0, help="cubic/square override of the grid (profiling runs)")
+    args = ap.parse_args()
+    cfg_name = args.config
+    cfg = dict(CONFIGS[cfg_name])
+    if args.grid:
+        g0 = args.grid
+        cfg["n"] = (g0, g0, g0 if cfg["dim"] == 3 else 1) if cfg_name != "channel" else (2 * g0, g0, (3 * g0) // 2)
+        cfg["desc"] = cfg["desc"] + f" (grid override {cfg['n']})"
+    rank, world, local = env_rank()
+    if args.impl == "reference":
+        run_reference(args, cfg_name, cfg)
+        return
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+
+    import fen_gb300 as F
+
+    n, L = cfg["n"], cfg["L"]
+    g = F.Grid(n[0], n[1], n[2], L[0], L[1], L[2], bc=cfg["bc"], dim=cfg["dim"], aniso=cfg.get("aniso", False))
+    s = F.Solver(g, viscosity=cfg["nu"], g=cfg.get("g", (0, 0, 0)), CFL=cfg.get("cfl", 1.0),
+                 constant_CFL=cfg.get("constant_cfl", False))
+    fields = init_fields(cfg_name, cfg, n, g.shape)
+    fid = {"u": F.U, "v": F.V, "w": F.W, "p": F.P}
+    keys = [k for k in "uvwp" if k in fields]
+
+    def upload_all(src):
+        for k in keys:
+            s.set_field(fid[k], src[k])
+            s.update_ghost_nodes(fid[k])
+
+    def start_dt():
+        if cfg.get("constant_cfl"):
+            return s.set_timestep(start_velocity(cfg_name, cfg))
+        s.set_dt_o(cfg["dt"])
+        return cfg["dt"]
+
+    upload_all(fields)
+    dt = start_dt()
+    dt = s.advance_n(args.warmup, dt)
+    cells = n[0] * n[1] * n[2]
+
+    # ---- device-timed throughput (graph replay, inputs resident in HBM) ----
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    s.sync()
+    l0 = s.kernel_launches()
+    with ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]) if world == 1 else local) as clk:
+        ms = s.time_steps(args.steps, dt)
+    launches = s.kernel_launches() - l0
+    s.sync()
+    torch.cuda.synchronize()
+    if dist:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * cells * args.steps / (ms / 1e3) / 1e6
+    ms_per_step = ms / args.steps
+
+    # ---- per-stage device times for the roofline ----
+    st = s.profile_step(3, s.status()["dt"])
+    stage = dict(zip(STAGES, st))
+    peak, peak_kind = measured_peaks()
+    dom = max(STAGE_BYTES_3D, key=lambda k: stage.get(k, 0) if k in stage else 0)
+    bpc = STAGE_BYTES_3D[dom] if cfg["dim"] == 3 else STAGE_BYTES_3D[dom] * 0.7
+    achieved = bpc * cells / (stage[dom] / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "bytes_per_cell": bpc, "stage_ms": {k: round(v, 4) for k, v in stage.items()},
+                "note": "FP64 kernels are FP64-issue-bound on GB300 (1.19 TFLOP/s FP64 measured)"}
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    host = {k: torch.from_numpy(np.ascontiguousarray(fields[k])).pin_memory() for k in keys}
+    outb = {k: torch.empty(fields[k].shape, dtype=torch.float64).pin_memory() for k in keys}
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in keys:
+        s.set_field(fid[k], host[k].numpy())
+        s.update_ghost_nodes(fid[k])
+    dt2 = start_dt()
+    for step in range(1, args.steps + 1):
+        dt2 = s.advance_solution(step, dt2)
+    for k in keys:
+        outb[k].numpy()[...] = s.get_field(fid[k])
+    s.sync()
+    el = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([el], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el = float(t.item())
+    field_bytes = 8 * int(np.prod(g.shape)) if cfg["dim"] == 3 else 8 * (n[0] + 2) * (n[1] + 2)
+    e2e = {"value": round(world * cells * args.steps / el / 1e6, 3), "unit": "Mcell-steps/s",
+           "h2d_bytes_per_step": int(len(keys) * field_bytes / args.steps + 8),
+           "d2h_bytes_per_step": int(len(keys) * field_bytes / args.steps + 160)}
+
+    if rank == 0:
+        line = {"metric": "Mcell-steps/s", "value": round(value, 3), "unit": "Mcell-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic",
+                "config": {"workload": cfg["desc"], "cells": cells, "grid": list(n),
+                           "flush": "inputs larger than L2 (fields 137 MB each)" if cells > 1e6 else "L2-resident",
+                           "parallelism": f"replicas{world}"},
+                "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "clocks": clk.summary()}
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(cfg_name, cfg)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

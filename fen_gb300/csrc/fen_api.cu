@@ -117,7 +117,7 @@ struct fen_ctx {
   cudaGraphExec_t graph = nullptr;
   long long launches = 0;
   long long launches_per_step = 0;
-  double* stage_scratch = nullptr;  // for fen_divergence / fen_explicit_terms
+  double* stage_scratch = nullptr;  // host-layout staging for upload/download (one field)
 };
 
 namespace {
@@ -688,6 +688,33 @@ double* field_ptr(fen_ctx* c, int f) {
 
 int host_planes(fen_ctx* c) { return c->dim == 3 ? c->n[2] + 2 : 3; }
 
+// Copy one field between FEN's host layout and the padded HBM layout through a contiguous
+// staging buffer (one memcpy + one relayout kernel).  dir 0: host -> device, 1: back.
+int relayout(fen_ctx* c, double* dfield, double* host_rw, int dir) {
+  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
+  const int planes = (c->dim == 3) ? c->n[2] + 2 : 1;
+  const size_t cnt = (size_t)nxg * nyg * planes;
+  double* h = host_rw + (c->dim == 2 ? (size_t)nxg * nyg : 0);  // 2D: plane k = 1
+  if (!c->stage_scratch) {
+    int r;
+    if ((r = alloc(&c->stage_scratch, (long long)cnt))) return r;
+  }
+  const int grid = std::min(cdiv((long long)cnt, 256), 152 * 16);
+  if (dir == 0) {
+    CK(cudaMemcpyAsync(c->stage_scratch, h, cnt * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    k_relayout<double><<<grid, 256, 0, c->stream>>>(c->L, planes, c->stage_scratch, dfield, nullptr, nullptr, 0);
+    c->launches++;
+    CK(cudaGetLastError());
+  } else {
+    k_relayout<double><<<grid, 256, 0, c->stream>>>(c->L, planes, nullptr, nullptr, dfield, c->stage_scratch, 1);
+    c->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h, c->stage_scratch, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
 int pre_step(fen_ctx* c, double dt) {
   if (!c->have_dt) return fail(FEN_ERR_STATE, "set_timestep (or set_dt_o) must be called before advancing");
   // dt: previous dt for constant CFL, the step's dt otherwise
@@ -841,12 +868,8 @@ int fen_upload(fen_ctx* c, int f, const double* host) {
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   }
   if (!d || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
-  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
-  const double* src = host + (c->dim == 2 ? (size_t)nxg * nyg : 0);  // 2D: plane k = 1
-  const int rows = nyg * (c->dim == 3 ? c->n[2] + 2 : 1);
-  CK(cudaMemcpy2DAsync(d + c->L.off, c->L.sx * sizeof(double), src, nxg * sizeof(double), nxg * sizeof(double), rows,
-                       cudaMemcpyHostToDevice, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+  int r;
+  if ((r = relayout(c, d, const_cast<double*>(host), 0))) return r;
   if (f == FEN_U || f == FEN_V || f == FEN_W) c->vel_dirty = 1;
   return 0;
 }
@@ -862,12 +885,8 @@ int fen_download(fen_ctx* c, int f, double* host) {
     }
     return fail(FEN_ERR_ARG, "bad field id");
   }
-  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
-  double* dst = host + (c->dim == 2 ? (size_t)nxg * nyg : 0);
-  const int rows = nyg * (c->dim == 3 ? c->n[2] + 2 : 1);
-  CK(cudaMemcpy2DAsync(dst, nxg * sizeof(double), d + c->L.off, c->L.sx * sizeof(double), nxg * sizeof(double), rows,
-                       cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+  int r;
+  if ((r = relayout(c, d, host, 1))) return r;
   return 0;
 }
 

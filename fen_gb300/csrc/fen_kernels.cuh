@@ -681,4 +681,21 @@ __global__ void k_prologue(StepScalars* sc, int constant_cfl, double cfl, double
   sc->dt_over_rhof = dt / rhof;
 }
 
+// Host-layout <-> HBM-layout copies.  The host array is FEN's contiguous f(0:nx+1, 0:ny+1,
+// planes) (x fastest); one contiguous copy moves it to a staging buffer and this kernel
+// scatters rows into the padded layout (dir = 0) or gathers them back (dir = 1).
+template <typename T>
+__global__ void __launch_bounds__(256) k_relayout(Layout L, int planes, const double* __restrict__ src, T* dst_field,
+                                                  const T* __restrict__ src_field, double* dst, int dir) {
+  const int nxg = L.n0 + 2;
+  const long long total = (long long)nxg * (L.n1 + 2) * planes;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % nxg);
+    const long long row = t / nxg;  // j + (ny+2) * plane
+    const long long d = (long long)L.off + i + (long long)L.sx * row;
+    if (dir == 0) dst_field[d] = (T)src[t];
+    else dst[t] = (double)src_field[d];
+  }
+}
+
 }  // namespace fen

@@ -57,7 +57,7 @@ BC_SETS_3D = {
 def test_ghost_fill_bit_exact(fen_lib, name):
     dim = 2 if name in BC_SETS_2D else 3
     bc = (BC_SETS_2D if dim == 2 else BC_SETS_3D)[name]
-    n = (12, 10, 1) if dim == 2 else (8, 10, 6)
+    n = (12, 8, 1) if dim == 2 else (8, 12, 6)
     try:
         o, s = pair(dim, n, (1.0, 1.0, 1.0), bc=bc)
     except ValueError:
@@ -86,7 +86,7 @@ def test_ghost_fill_bit_exact(fen_lib, name):
 def test_explicit_terms(fen_lib, name):
     dim = 2 if name in BC_SETS_2D else 3
     bc = (BC_SETS_2D if dim == 2 else BC_SETS_3D)[name]
-    n = (16, 12, 1) if dim == 2 else (12, 8, 10)
+    n = (16, 12, 1) if dim == 2 else (12, 8, 6)
     o, s = pair(dim, n, (1.3, 0.9, 1.1), bc=bc, viscosity=0.03, aniso=True)
     rng = np.random.Generator(np.random.PCG64(9))
     for fid in ([O.U, O.V] if dim == 2 else [O.U, O.V, O.W]):
@@ -282,22 +282,28 @@ def test_step_lid_driven_walls(fen_lib):
     _compare_state(o, s, 2, RTOL_RUN)
 
 
-@pytest.mark.parametrize("name", ["pn_io"])
-def test_step_inflow_outflow(fen_lib, name):
-    # poiseuille_io form: Inflow/Outflow along y makes phi Dirichlet at the outflow face
-    N = 16
-    o, s = pair(2, (N, N, 1), (1.0, 1.0, 1.0 / N), bc=BC_SETS_2D[name], viscosity=0.1)
+def test_step_poiseuille_inflow_outflow(fen_lib):
+    # navier_stokes/poiseuille_io (poiseuille_io.f90:27-60): walls in x, Inflow at the
+    # bottom with v = -x(x-1)/2, Outflow at the top (phi Dirichlet there, b(ny) - c(ny) in
+    # the tridiagonal, poisson.f90:225-230); nu = 1 (module default); nn solver
+    Nx, Ny = 16, 64
+    Lx, Ly = 1.0, 4.0
+    bc = [O.WALL, O.WALL, O.INFLOW, O.OUTFLOW]
+    o, s = pair(2, (Nx, Ny, 1), (Lx, Ly, Ly / Ny), bc=bc)
+    assert s.status()["poisson_solver"] == "nn"
     vin = o.bc_values(O.V, 2)
-    vin[...] = 1.0
-    s.set_bc_values(F.V, F.BOTTOM, np.ones(vin.shape))
+    xc = (np.arange(Nx + 2) - 0.5) * (Lx / Nx)
+    vin[...] = (-0.5 * (xc ** 2 - xc))[None, :]
+    s.set_bc_values(F.V, F.BOTTOM, vin.copy())
     for fid in (O.U, O.V, O.P):
         o.update_ghost_nodes(fid)
         s.update_ghost_nodes(fid)
     dto = o.set_timestep(1.0)
     dtg = s.set_timestep(1.0)
-    for step in range(1, 21):
+    for step in range(1, 31):
         o.step(dto)
         s.advance_solution(step, dtg)
+    assert np.all(np.isfinite(o.field(O.V)))
     _compare_state(o, s, 2, RTOL_RUN)
 
 
@@ -331,10 +337,10 @@ def test_nan_is_reported_not_faulted(fen_lib):
     s.set_dt_o(1e-3)
     with pytest.raises(F.FenError, match="NaN"):
         s.advance_solution(1, 1e-3)
-    # the context stays usable
-    s.set_field(F.U, s.zeros())
-    s.set_field(F.V, s.zeros())
-    s.set_field(F.P, s.zeros())
+    # the context stays usable once the state (including the AB2 history dv_o, which
+    # carries the NaN as it would in the reference) is re-initialised
+    for fid in (F.U, F.V, F.P, F.DVO_X, F.DVO_Y):
+        s.set_field(fid, s.zeros())
     s.advance_solution(2, 1e-3)
 
 
