@@ -755,6 +755,9 @@ int read_back(fen_ctx* c) {
 
 }  // namespace
 
+// Error reporting for entry points defined in other translation units.
+int fen_internal_fail(int code, const char* msg) { return fail(code, msg); }
+
 // ---------------------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------------------

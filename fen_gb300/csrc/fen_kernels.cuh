@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
 
 // Tabulate c1 and the row factors for every (col, outer) system with the reference's
 // operation order.  lamA indexed by col, lamB by outer (nullptr in 2D).
-__global__ void k_thomas_tables(int ncol, int nouter, int n, const double* a, const double* b, const double* c,
+static __global__ void k_thomas_tables(int ncol, int nouter, int n, const double* a, const double* b, const double* c,
                                 const double* lamA, const double* lamB, int form3, double* c1, double* fac) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   const int outer = blockIdx.y;
@@ -632,7 +632,7 @@ __global__ void __launch_bounds__(256) k_checks(Layout L, CheckArgs<T> a) {
 }
 
 // Fold the check partials: maxdiv, maxvel, maxCFL = dt*maxvel/delta (navier_stokes.f90:593, 617).
-__global__ void k_finalize(const double* pdiv, const double* pvel, int np, StepScalars* sc, double delta, double dt_host,
+static __global__ void k_finalize(const double* pdiv, const double* pvel, int np, StepScalars* sc, double delta, double dt_host,
                            int use_dev_dt, const int* nan_flag) {
   __shared__ double r1[256], r2[256];
   double md = -INFINITY, mv = 0.0;
@@ -661,7 +661,7 @@ __global__ void k_finalize(const double* pdiv, const double* pvel, int np, StepS
 
 // Start-of-step scalars: update_timestep when constant_CFL (navier_stokes.f90:670-730),
 // then the AB2 coefficients (:157-158) and the Poisson right-hand-side scale (:118).
-__global__ void k_prologue(StepScalars* sc, int constant_cfl, double cfl, double delta, double density, double rhof) {
+static __global__ void k_prologue(StepScalars* sc, int constant_cfl, double cfl, double delta, double density, double rhof) {
   if (threadIdx.x != 0) return;
   double dt;
   if (constant_cfl) {

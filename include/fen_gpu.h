@@ -122,6 +122,22 @@ int fen_time_steps(fen_ctx* ctx, int nsteps, double dt, double* ms);
  * transform(s), correction, ghost(v,p,phi), checks (milliseconds, averaged over reps). */
 int fen_profile_step(fen_ctx* ctx, int reps, double dt, double* out);
 
+/* Allocation-free 2D periodic Poisson solve.  No counterpart in the reference: it serves
+ * callers that cannot allocate device memory (a host framework that owns every device
+ * allocation through its own pool, code running inside someone else's stream capture, or a
+ * solver embedded under a fixed memory budget).  It solves lap(phi) = rhs exactly as FEN's
+ * pp solver does (FFT in x and y, zero mode set to 0, mean removed) with grid spacing
+ * lx/nx on both axes.  rhs and phi are caller-owned device-accessible arrays of nx*ny
+ * doubles (interior only, x fastest); they may alias.  The call allocates nothing: its
+ * scratch lives in a static device array of about 8.5 MB that every GPU loading this library
+ * holds until exit, sized for nx, ny <= FEN_NOALLOC_MAX_N; larger sizes are rejected with
+ * FEN_ERR_ARG.  The first call on each device fetches that array's device address (make it
+ * before any stream capture).  All calls share the array, so calls that overlap on the GPU
+ * race and must be serialised.  Work is queued on `stream` (NULL = default stream) and the
+ * call returns after synchronising it. */
+#define FEN_NOALLOC_MAX_N 1024
+int fen_poisson_pp2d_noalloc(const double* rhs, double* phi, int nx, int ny, double lx, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
