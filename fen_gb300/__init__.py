@@ -48,6 +48,7 @@ class _Params(ctypes.Structure):
         ("origin", ctypes.c_double * 3), ("bc", ctypes.c_int * 6), ("aniso", ctypes.c_int),
         ("density", ctypes.c_double), ("viscosity", ctypes.c_double), ("g", ctypes.c_double * 3),
         ("cfl", ctypes.c_double), ("constant_cfl", ctypes.c_int), ("precision", ctypes.c_int),
+        ("refine", ctypes.c_int),
     ]
 
 
@@ -142,11 +143,14 @@ class Solver:
     """One solver instance: init_solver + the navier_stokes_mod/poisson_mod module state.
 
     Module variables of navier_stokes_mod (density, viscosity, g, CFL, constant_CFL,
-    navier_stokes.f90:18-45) are constructor arguments.
+    navier_stokes.f90:18-45) are constructor arguments.  ``precision`` selects the FP64 form
+    or the mixed form (``MIXED``: FP32 stencils/transforms, double-float state, FP64
+    tridiagonal and reductions); ``refine`` is the mixed form's number of iterative-
+    refinement solves per step.
     """
 
     def __init__(self, grid, density=1.0, viscosity=1.0, g=(0.0, 0.0, 0.0), CFL=1.0, constant_CFL=False,
-                 precision=FP64, lib=None):
+                 precision=FP64, refine=1, lib=None):
         self._L = load_library(lib)
         self.grid = grid
         p = _Params()
@@ -159,6 +163,7 @@ class Solver:
         p.density, p.viscosity = float(density), float(viscosity)
         p.g = (ctypes.c_double * 3)(*[float(x) for x in g])
         p.cfl, p.constant_cfl, p.precision = float(CFL), int(bool(constant_CFL)), int(precision)
+        p.refine = int(refine) if precision == MIXED else 0
         self._h = ctypes.c_void_p()
         self._check(self._L.fen_ctx_create(ctypes.byref(p), ctypes.byref(self._h)))
         self.dt_o = None

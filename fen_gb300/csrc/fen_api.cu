@@ -5,8 +5,16 @@
 // (src/poisson.f90:31-49), all resident in HBM, plus one CUDA stream and a captured graph
 // of one time step.  The step is the sequence of navier_stokes_solver
 // (navier_stokes.f90:50-136) as kernels; see fen_kernels.cuh.
+//
+// Two arithmetic forms share the plan:
+//   FP64  : every field and transform in FP64 (the reference's arithmetic);
+//   MIXED : state u, v, w, p as double-float pairs (fen_mixed.cuh); predictor, divergence,
+//           transforms, correction in FP32 instructions; tridiagonal solves, mean removal
+//           and the diagnostics reductions in FP64.  The FP64 arrays u, v, w, p then only
+//           stage host transfers.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -58,10 +66,14 @@ int field_type(int face, int pb, int comp) {
 
 double ffloat(long long n) { return (double)(float)n; }  // Fortran float(n)
 
+// One stage of the Poisson plan.  `la` is a precision-neutral descriptor; typed pointers
+// are attached at launch (fdst_v, invlam_v, loader inputs).
 struct Stage {
-  int kind;          // 0 = line transform, 1 = thomas, 2 = mean subtract
+  int kind;          // 0 = line transform, 1 = Thomas
   int op, ld, st, contig;
   LineArgs<double> la;
+  void* fdst_v;
+  void* invlam_v;
   dim3 grid;
   size_t smem;
   ThomasArgs ta;
@@ -72,6 +84,7 @@ struct Stage {
 
 struct fen_ctx {
   fen_params prm{};
+  int mixed = 0;
   int dim = 2;
   int n[3] = {1, 1, 1};
   double d[3] = {1, 1, 1};
@@ -82,11 +95,19 @@ struct fen_ctx {
   Layout L{};
   int ftype[5][6];
   double* bcval[5][6];
-  // state
+  // FP64 state (both forms) and FP64-form work fields
   double *u = nullptr, *v = nullptr, *w = nullptr, *p = nullptr, *phi = nullptr;
   double *us = nullptr, *vs = nullptr, *ws = nullptr;
   double* dvo[3] = {nullptr, nullptr, nullptr};
   double* S[3] = {nullptr, nullptr, nullptr};
+  // mixed-form FP32 fields: the state as hi/lo pairs, phi, the increment dt*rhs, dv_o, S
+  float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr, *p32 = nullptr, *phi32 = nullptr;
+  float *u32l = nullptr, *v32l = nullptr, *w32l = nullptr, *p32l = nullptr;
+  float *dphi32 = nullptr, *res32 = nullptr;  // refinement: correction of phi, residual
+  int refine = 0;
+  float* d32[3] = {nullptr, nullptr, nullptr};
+  float* dvo32[3] = {nullptr, nullptr, nullptr};
+  float* S32[3] = {nullptr, nullptr, nullptr};
   int has_S = 0;
   // poisson
   int solver = -1;
@@ -95,11 +116,13 @@ struct fen_ctx {
   double *c1 = nullptr, *fac = nullptr;
   void* specC = nullptr;
   void* specR = nullptr;
+  void* inv_lam = nullptr;
   std::vector<void*> twbufs;
-  AxisTw tw[3];
-  const double2* wfull[3] = {nullptr, nullptr, nullptr};  // exp(-2 pi i m/n), c2c stages
+  AxisTw tw[3], twf[3];
+  const double2* wfull[3] = {nullptr, nullptr, nullptr};   // exp(-2 pi i m/n), c2c stages
+  const double2* wfullf[3] = {nullptr, nullptr, nullptr};  // the same as float2
   FFTPlan plan_half[3], plan_full[3];
-  std::vector<Stage> stages;  // first stage loads from the field given at run time
+  std::vector<Stage> stages;
   int needs_mean = 0;
   double mean_div = 1;
   double* partial = nullptr;
@@ -110,7 +133,6 @@ struct fen_ctx {
   int* nan_flag = nullptr;
   StepScalars* sc = nullptr;
   StepScalars* sc_host = nullptr;  // pinned mirror
-  double dt_visc = 0, dt_o = 0;
   int have_dt = 0;
   int vel_dirty = 1;
   cudaStream_t stream = nullptr;
@@ -135,18 +157,26 @@ bool make_plan(int M, FFTPlan& P) {
   return m == 1 && P.nst <= kMaxStages;
 }
 
-int upload_table(fen_ctx* c, const std::vector<double2>& h, const double2** out) {
+template <typename V>
+int upload_vec(fen_ctx* c, const std::vector<V>& h, const double2** out) {
   void* d = nullptr;
-  CK(cudaMalloc(&d, std::max<size_t>(h.size(), 1) * sizeof(double2)));
-  CK(cudaMemcpy(d, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&d, std::max<size_t>(h.size(), 1) * sizeof(V)));
+  CK(cudaMemcpy(d, h.data(), h.size() * sizeof(V), cudaMemcpyHostToDevice));
   c->twbufs.push_back(d);
   *out = (const double2*)d;
   return 0;
 }
 
+int upload_table(fen_ctx* c, const std::vector<double2>& h, const double2** out64, const double2** out32) {
+  int r;
+  if ((r = upload_vec(c, h, out64))) return r;
+  std::vector<float2> f(h.size());
+  for (size_t q = 0; q < h.size(); ++q) f[q] = make_float2((float)h[q].x, (float)h[q].y);
+  return upload_vec(c, f, out32);
+}
+
 // Twiddles of one axis of real length n (periodic: r2c/c2c; Neumann: DCT).
 int make_axis(fen_ctx* c, int ax, int n) {
-  // complex FFT lengths used on this axis: n/2 (real transforms) and n (c2c)
   FFTPlan ph, pf;
   if (n % 2 != 0 || !make_plan(n / 2, ph) || !make_plan(n, pf))
     return fail(FEN_ERR_ARG, "grid size " + std::to_string(n) + " must be 2^a 3^b with a >= 1");
@@ -158,20 +188,12 @@ int make_axis(fen_ctx* c, int ax, int n) {
   for (int k = 0; k <= n / 2; ++k) { double a = 2.0 * M_PI * k / (double)n; wn[k] = make_double2(cos(a), -sin(a)); }
   for (int k = 0; k < n; ++k) { double a = M_PI * k / (2.0 * n); wd[k] = make_double2(cos(a), -sin(a)); }
   int r;
-  const double2 *pwh, *pwf, *pwn, *pwd;
-  if ((r = upload_table(c, wh, &pwh))) return r;
-  if ((r = upload_table(c, wf, &pwf))) return r;
-  if ((r = upload_table(c, wn, &pwn))) return r;
-  if ((r = upload_table(c, wd, &pwd))) return r;
-  // tw[ax] serves the real transforms (half-length FFT); c2c stages use wfull[ax]
-  c->tw[ax].wM = pwh;
-  c->tw[ax].wN = pwn;
-  c->tw[ax].wD = pwd;
-  c->wfull[ax] = pwf;
+  if ((r = upload_table(c, wh, &c->tw[ax].wM, &c->twf[ax].wM))) return r;
+  if ((r = upload_table(c, wf, &c->wfull[ax], &c->wfullf[ax]))) return r;
+  if ((r = upload_table(c, wn, &c->tw[ax].wN, &c->twf[ax].wN))) return r;
+  if ((r = upload_table(c, wd, &c->tw[ax].wD, &c->twf[ax].wD))) return r;
   return 0;
 }
-
-const double2* full_tw(fen_ctx* c, int ax) { return c->wfull[ax]; }
 
 // Modified wavenumbers (poisson.f90:141, 265).
 std::vector<double> mwn_host(int n, double delta, bool neumann) {
@@ -187,11 +209,15 @@ std::vector<double> mwn_host(int n, double delta, bool neumann) {
   return m;
 }
 
-int alloc(double** p, long long n) {
-  CK(cudaMalloc((void**)p, (size_t)std::max<long long>(n, 1) * sizeof(double)));
-  CK(cudaMemset(*p, 0, (size_t)std::max<long long>(n, 1) * sizeof(double)));
+template <typename T>
+int alloc(T** p, long long n) {
+  CK(cudaMalloc((void**)p, (size_t)std::max<long long>(n, 1) * sizeof(T)));
+  CK(cudaMemset(*p, 0, (size_t)std::max<long long>(n, 1) * sizeof(T)));
   return 0;
 }
+
+size_t cplx_size(fen_ctx* c) { return c->mixed ? sizeof(float2) : sizeof(double2); }
+size_t real_size(fen_ctx* c) { return c->mixed ? sizeof(float) : sizeof(double); }
 
 LineArgs<double> base_line(fen_ctx* c) {
   LineArgs<double> a;
@@ -218,9 +244,9 @@ Stage x_stage(fen_ctx* c, int op, int ld, int st) {
   s.la.nl = nl;
   s.la.nlines = c->n[1];
   s.la.plan = c->plan_half[0];
-  s.la.tw = c->tw[0];
+  s.la.tw = c->mixed ? c->twf[0] : c->tw[0];
   s.grid = dim3(cdiv(c->n[1], nl), c->dim == 3 ? c->n[2] : 1);
-  s.smem = 2 * (size_t)nl * M * sizeof(double2);
+  s.smem = 2 * (size_t)nl * M * cplx_size(c);
   return s;
 }
 
@@ -234,7 +260,9 @@ Stage s_stage(fen_ctx* c, int op, int ld, int st, int ax, int ncol, int nouter, 
   const int n = c->n[ax];
   const bool cc = (op == OP_C2C_F || op == OP_C2C_I || op == OP_C2C_SOLVE);
   const int M = cc ? n : n / 2;
-  const int nl = 8;
+  // tiles of 128-byte rows: 8 FP64 or 16 FP32 complex columns
+  int nl = c->mixed ? 16 : 8;
+  while (nl > 2 && 2 * (size_t)nl * M * cplx_size(c) > 200 * 1024) nl /= 2;
   s.la.n = n;
   s.la.nl = nl;
   s.la.nlines = ncol;
@@ -242,10 +270,10 @@ Stage s_stage(fen_ctx* c, int op, int ld, int st, int ax, int ncol, int nouter, 
   s.la.in_line = 1; s.la.in_pos = in_pos; s.la.in_outer = in_outer;
   s.la.out_line = 1; s.la.out_pos = out_pos; s.la.out_outer = out_outer;
   s.la.plan = cc ? c->plan_full[ax] : c->plan_half[ax];
-  s.la.tw = c->tw[ax];
-  if (cc) s.la.tw.wM = full_tw(c, ax);
+  s.la.tw = c->mixed ? c->twf[ax] : c->tw[ax];
+  if (cc) s.la.tw.wM = c->mixed ? c->wfullf[ax] : c->wfull[ax];
   s.grid = dim3(cdiv(ncol, nl), nouter);
-  s.smem = 2 * (size_t)nl * M * sizeof(double2);
+  s.smem = 2 * (size_t)nl * M * cplx_size(c);
   return s;
 }
 
@@ -281,25 +309,42 @@ int init_tridiag(fen_ctx* c, int ax, int ncol, int nouter, const double* lamA, c
   a[0] = 0.0;
   cc[n - 1] = 0.0;
   int r;
-  double *db, *dc;
-  if ((r = alloc(&c->ta, n))) return r;
-  if ((r = alloc(&db, n))) return r;
-  if ((r = alloc(&dc, n))) return r;
+  if ((r = alloc(&c->ta, n)) || (r = alloc(&c->tb, n)) || (r = alloc(&c->tc, n))) return r;
   CK(cudaMemcpy(c->ta, a.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(db, b.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(dc, cc.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->tb, b.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->tc, cc.data(), n * sizeof(double), cudaMemcpyHostToDevice));
   const long long nt = (long long)n * ncol * nouter;
-  if ((r = alloc(&c->c1, nt))) return r;
-  if ((r = alloc(&c->fac, nt))) return r;
-  k_thomas_tables<<<dim3(cdiv(ncol, 128), nouter), 128>>>(ncol, nouter, n, c->ta, db, dc, lamA, lamB, form3, c->c1, c->fac);
+  if ((r = alloc(&c->c1, nt)) || (r = alloc(&c->fac, nt))) return r;
+  k_thomas_tables<<<dim3(cdiv(ncol, 128), nouter), 128>>>(ncol, nouter, n, c->ta, c->tb, c->tc, lamA, lamB, form3, c->c1, c->fac);
   CK(cudaGetLastError());
   CK(cudaDeviceSynchronize());
-  c->tb = db;
-  c->tc = dc;
   return 0;
 }
 
-int launch_stage(fen_ctx* c, const Stage& s, int first_from_field, const double* field_src);
+// Tabulate scale/lam for a SOLVE stage (same arithmetic as the in-kernel division).
+int init_inv_lam(fen_ctx* c, Stage& s, int nouter) {
+  const long long total = (long long)s.la.nlines * s.la.n * nouter;
+  const int grid = std::min(cdiv(total, 256), 152 * 16);
+  if (c->mixed) {
+    float* t;
+    int r;
+    if ((r = alloc(&t, total))) return r;
+    k_inv_lam_table<float><<<grid, 256>>>(s.la.nlines, s.la.n, nouter, s.la.lamA, s.la.lamB, s.la.lamC, s.la.scale, t);
+    c->inv_lam = t;
+  } else {
+    double* t;
+    int r;
+    if ((r = alloc(&t, total))) return r;
+    k_inv_lam_table<double><<<grid, 256>>>(s.la.nlines, s.la.n, nouter, s.la.lamA, s.la.lamB, s.la.lamC, s.la.scale, t);
+    c->inv_lam = t;
+  }
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
+  s.invlam_v = c->inv_lam;
+  return 0;
+}
+
+int launch_stage(fen_ctx* c, const Stage& s, int first_from_field, const void* field_src, void* dst = nullptr);
 
 // With g_attr_only set, the launch helpers only raise the kernel's dynamic shared-memory
 // limit (done once per context, before any stream capture) instead of launching.
@@ -337,7 +382,7 @@ int init_poisson(fen_ctx* c) {
   c->needs_mean = (s == S_PP || s == S_PN || s == S_PPN || s == S_PNP);
   c->mean_div = ffloat((long long)nx * ny * nz);
   if (s == S_PP || s == S_PN || s == S_PPP || s == S_PPN || s == S_PNP) {
-    CK(cudaMalloc(&c->specC, (size_t)hp * ny * nz * sizeof(double2)));
+    CK(cudaMalloc(&c->specC, (size_t)hp * ny * nz * cplx_size(c)));
     void* C = c->specC;
     Stage x0 = x_stage(c, OP_R2C, LD_DIV, ST_CPLX);
     x0.la.out = C;
@@ -348,12 +393,14 @@ int init_poisson(fen_ctx* c) {
       Stage y = s_stage(c, OP_C2C_SOLVE, LD_CPLX, ST_CPLX, 1, h, 1, hp, 0, hp, 0, C, C);
       y.la.scale = 1.0 / ffloat((long long)nx * ny);  // :458
       y.la.lamA = c->mwn[0]; y.la.lamB = nullptr; y.la.lamC = c->mwn[1];
+      if ((r = init_inv_lam(c, y, 1))) return r;
       c->stages.push_back(y);
     } else if (s == S_PPP) {
       c->stages.push_back(s_stage(c, OP_C2C_F, LD_CPLX, ST_CPLX, 1, h, nz, hp, hp * ny, hp, hp * ny, C, C));
       Stage z = s_stage(c, OP_C2C_SOLVE, LD_CPLX, ST_CPLX, 2, h, ny, hp * ny, hp, hp * ny, hp, C, C);
       z.la.scale = 1.0 / ffloat((long long)nx * ny * nz);  // :992
       z.la.lamA = c->mwn[0]; z.la.lamB = c->mwn[1]; z.la.lamC = c->mwn[2];
+      if ((r = init_inv_lam(c, z, ny))) return r;
       c->stages.push_back(z);
       c->stages.push_back(s_stage(c, OP_C2C_I, LD_CPLX, ST_CPLX, 1, h, nz, hp, hp * ny, hp, hp * ny, C, C));
     } else if (s == S_PN) {
@@ -380,7 +427,7 @@ int init_poisson(fen_ctx* c) {
     c->stages.push_back(xi);
   } else {
     // DCT-based: nn (2D), npn, nnn
-    CK(cudaMalloc(&c->specR, (size_t)nx * ny * nz * sizeof(double)));
+    CK(cudaMalloc(&c->specR, (size_t)nx * ny * nz * real_size(c)));
     void* R = c->specR;
     const long long px = nx;
     Stage x0 = x_stage(c, OP_DCT2, LD_DIV, ST_REAL);
@@ -393,7 +440,7 @@ int init_poisson(fen_ctx* c) {
       c->stages.push_back(t_stage(c, R, 1, px, 0, nx, 1, ny, 0));
     } else if (s == S_NPN) {
       const int hy = ny / 2 + 1;
-      CK(cudaMalloc(&c->specC, (size_t)nx * hy * nz * sizeof(double2)));
+      CK(cudaMalloc(&c->specC, (size_t)nx * hy * nz * cplx_size(c)));
       void* C = c->specC;
       Stage y = s_stage(c, OP_R2C, LD_REAL, ST_CPLX, 1, nx, nz, px, px * ny, px, px * hy, R, C);
       y.la.scale = 1.0 / (double)ny;  // :1226
@@ -431,16 +478,50 @@ int init_poisson(fen_ctx* c) {
   c->npartial = (int)(last.grid.x * last.grid.y);
   if ((r = alloc(&c->partial, c->npartial))) return r;
   last.la.partial = c->needs_mean ? c->partial : nullptr;
-  last.la.fdst = c->phi;
+  last.fdst_v = c->mixed ? (void*)c->phi32 : (void*)c->phi;
   return 0;
 }
 
 // ---------------------------------------------------------------------------------------
 // Launch helpers
 // ---------------------------------------------------------------------------------------
-template <int DIM, bool CONTIG, int OP, int LD, int ST>
-int launch_line_t(fen_ctx* c, const Stage& s, const LineArgs<double>& a) {
-  auto kern = k_line<double, DIM, CONTIG, OP, LD, ST>;
+template <typename T>
+LineArgs<T> typed_args(const Stage& s);
+
+template <>
+LineArgs<double> typed_args<double>(const Stage& s) {
+  LineArgs<double> a = s.la;
+  a.fdst = (double*)s.fdst_v;
+  a.inv_lam = (const double*)s.invlam_v;
+  return a;
+}
+
+template <>
+LineArgs<float> typed_args<float>(const Stage& s) {
+  const LineArgs<double>& d = s.la;
+  LineArgs<float> a;
+  memset(&a, 0, sizeof(a));
+  a.n = d.n; a.nl = d.nl; a.nlines = d.nlines;
+  a.in = d.in; a.out = d.out;
+  a.in_line = d.in_line; a.in_pos = d.in_pos; a.in_outer = d.in_outer;
+  a.out_line = d.out_line; a.out_pos = d.out_pos; a.out_outer = d.out_outer;
+  a.L = d.L;
+  a.partial = d.partial;
+  a.scale = d.scale;
+  a.sc = d.sc;
+  for (int q = 0; q < 3; ++q) a.id[q] = d.id[q];
+  a.iso = d.iso; a.dim = d.dim;
+  a.lamA = d.lamA; a.lamB = d.lamB; a.lamC = d.lamC;
+  a.plan = d.plan;
+  a.tw = d.tw;
+  a.fdst = (float*)s.fdst_v;
+  a.inv_lam = (const float*)s.invlam_v;
+  return a;
+}
+
+template <typename T, int DIM, bool CONTIG, int OP, int LD, int ST>
+int launch_line_t(fen_ctx* c, const Stage& s, const LineArgs<T>& a) {
+  auto kern = k_line<T, DIM, CONTIG, OP, LD, ST>;
   if (s.smem > 200 * 1024) return fail(FEN_ERR_ARG, "transform length too large for one CTA");
   if (g_attr_only) {
     CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -452,78 +533,114 @@ int launch_line_t(fen_ctx* c, const Stage& s, const LineArgs<double>& a) {
   return 0;
 }
 
-template <int DIM>
-int launch_line_dim(fen_ctx* c, const Stage& s, const LineArgs<double>& a) {
+template <typename T, int DIM>
+int launch_line_dim(fen_ctx* c, const Stage& s, int ld, const LineArgs<T>& a) {
   if (s.contig) {
-    if (s.op == OP_R2C && s.ld == LD_DIV) return launch_line_t<DIM, true, OP_R2C, LD_DIV, ST_CPLX>(c, s, a);
-    if (s.op == OP_R2C && s.ld == LD_FIELD) return launch_line_t<DIM, true, OP_R2C, LD_FIELD, ST_CPLX>(c, s, a);
-    if (s.op == OP_DCT2 && s.ld == LD_DIV) return launch_line_t<DIM, true, OP_DCT2, LD_DIV, ST_REAL>(c, s, a);
-    if (s.op == OP_DCT2 && s.ld == LD_FIELD) return launch_line_t<DIM, true, OP_DCT2, LD_FIELD, ST_REAL>(c, s, a);
-    if (s.op == OP_C2R) return launch_line_t<DIM, true, OP_C2R, LD_CPLX, ST_FIELD>(c, s, a);
-    if (s.op == OP_DCT3) return launch_line_t<DIM, true, OP_DCT3, LD_REAL, ST_FIELD>(c, s, a);
+    if (s.op == OP_R2C && ld == LD_DIV) return launch_line_t<T, DIM, true, OP_R2C, LD_DIV, ST_CPLX>(c, s, a);
+    if (s.op == OP_R2C && ld == LD_DIVMIX) return launch_line_t<T, DIM, true, OP_R2C, LD_DIVMIX, ST_CPLX>(c, s, a);
+    if (s.op == OP_R2C && ld == LD_FIELD) return launch_line_t<T, DIM, true, OP_R2C, LD_FIELD, ST_CPLX>(c, s, a);
+    if (s.op == OP_DCT2 && ld == LD_DIV) return launch_line_t<T, DIM, true, OP_DCT2, LD_DIV, ST_REAL>(c, s, a);
+    if (s.op == OP_DCT2 && ld == LD_DIVMIX) return launch_line_t<T, DIM, true, OP_DCT2, LD_DIVMIX, ST_REAL>(c, s, a);
+    if (s.op == OP_DCT2 && ld == LD_FIELD) return launch_line_t<T, DIM, true, OP_DCT2, LD_FIELD, ST_REAL>(c, s, a);
+    if (s.op == OP_C2R) return launch_line_t<T, DIM, true, OP_C2R, LD_CPLX, ST_FIELD>(c, s, a);
+    if (s.op == OP_DCT3) return launch_line_t<T, DIM, true, OP_DCT3, LD_REAL, ST_FIELD>(c, s, a);
   } else {
-    if (s.op == OP_C2C_F) return launch_line_t<3, false, OP_C2C_F, LD_CPLX, ST_CPLX>(c, s, a);
-    if (s.op == OP_C2C_I) return launch_line_t<3, false, OP_C2C_I, LD_CPLX, ST_CPLX>(c, s, a);
-    if (s.op == OP_C2C_SOLVE) return launch_line_t<3, false, OP_C2C_SOLVE, LD_CPLX, ST_CPLX>(c, s, a);
-    if (s.op == OP_R2C) return launch_line_t<3, false, OP_R2C, LD_REAL, ST_CPLX>(c, s, a);
-    if (s.op == OP_C2R) return launch_line_t<3, false, OP_C2R, LD_CPLX, ST_REAL>(c, s, a);
-    if (s.op == OP_DCT2) return launch_line_t<3, false, OP_DCT2, LD_REAL, ST_REAL>(c, s, a);
-    if (s.op == OP_DCT3) return launch_line_t<3, false, OP_DCT3, LD_REAL, ST_REAL>(c, s, a);
+    if (s.op == OP_C2C_F) return launch_line_t<T, 3, false, OP_C2C_F, LD_CPLX, ST_CPLX>(c, s, a);
+    if (s.op == OP_C2C_I) return launch_line_t<T, 3, false, OP_C2C_I, LD_CPLX, ST_CPLX>(c, s, a);
+    if (s.op == OP_C2C_SOLVE) return launch_line_t<T, 3, false, OP_C2C_SOLVE, LD_CPLX, ST_CPLX>(c, s, a);
+    if (s.op == OP_R2C) return launch_line_t<T, 3, false, OP_R2C, LD_REAL, ST_CPLX>(c, s, a);
+    if (s.op == OP_C2R) return launch_line_t<T, 3, false, OP_C2R, LD_CPLX, ST_REAL>(c, s, a);
+    if (s.op == OP_DCT2) return launch_line_t<T, 3, false, OP_DCT2, LD_REAL, ST_REAL>(c, s, a);
+    if (s.op == OP_DCT3) return launch_line_t<T, 3, false, OP_DCT3, LD_REAL, ST_REAL>(c, s, a);
   }
   return fail(FEN_ERR_ARG, "unsupported transform stage");
 }
 
-int launch_stage(fen_ctx* c, const Stage& s, int first_from_field, const double* field_src) {
-  if (s.kind == 1) {
-    k_thomas<double2, double2><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
-    c->launches++;
-    CK(cudaGetLastError());
-    return 0;
-  }
-  LineArgs<double> a = s.la;
-  Stage st = s;
+template <typename T>
+int launch_stage_t(fen_ctx* c, const Stage& s, int first_from_field, const void* field_src, void* dst) {
+  LineArgs<T> a = typed_args<T>(s);
+  if (dst && s.st == ST_FIELD) a.fdst = (T*)dst;
+  for (int q = 0; q < 3; ++q) a.idp[q] = split_d(1.0 / c->d[q]);
+  int ld = s.ld;
   if (first_from_field) {
-    st.ld = LD_FIELD;
-    a.fsrc = field_src;
+    ld = LD_FIELD;
+    a.fsrc = (const T*)field_src;
   } else if (s.ld == LD_DIV) {
-    a.fu = c->us; a.fv = c->vs; a.fw = c->ws;
+    if (c->mixed) {
+      ld = LD_DIVMIX;
+      a.fu = (const T*)c->d32[0]; a.fv = (const T*)c->d32[1]; a.fw = (const T*)c->d32[2];
+      a.pu = DFField{c->u32, c->u32l}; a.pv = DFField{c->v32, c->v32l}; a.pw = DFField{c->w32, c->w32l};
+    } else {
+      a.fu = (const T*)c->us; a.fv = (const T*)c->vs; a.fw = (const T*)c->ws;
+    }
   }
-  return (c->dim == 3) ? launch_line_dim<3>(c, st, a) : launch_line_dim<2>(c, st, a);
+  return (c->dim == 3) ? launch_line_dim<T, 3>(c, s, ld, a) : launch_line_dim<T, 2>(c, s, ld, a);
 }
 
-int launch_thomas_real(fen_ctx* c, const Stage& s) {
-  k_thomas<double, double><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
+int launch_thomas(fen_ctx* c, const Stage& s) {
+  const bool real = (c->solver == S_NN || c->solver == S_NNN);
+  if (real) {
+    if (c->mixed) k_thomas<float, double><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
+    else k_thomas<double, double><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
+  } else {
+    if (c->mixed) k_thomas<float2, double2><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
+    else k_thomas<double2, double2><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
+  }
   c->launches++;
   CK(cudaGetLastError());
   return 0;
 }
 
-FieldBC field_bc(fen_ctx* c, int f) {
+int launch_stage(fen_ctx* c, const Stage& s, int first_from_field, const void* field_src, void* dst) {
+  if (s.kind == 1) return g_attr_only ? 0 : launch_thomas(c, s);
+  return c->mixed ? launch_stage_t<float>(c, s, first_from_field, field_src, dst)
+                  : launch_stage_t<double>(c, s, first_from_field, field_src, dst);
+}
+
+FieldBC field_bc(fen_ctx* c, int f, bool homogeneous = false) {
   FieldBC b;
   for (int q = 0; q < 6; ++q) {
     b.type[q] = c->ftype[f][q];
-    b.val[q] = c->bcval[f][q];
+    b.val[q] = homogeneous ? nullptr : c->bcval[f][q];
   }
   b.c = (f == FEN_U) ? 'x' : (f == FEN_V) ? 'y' : (f == FEN_W) ? 'z' : 'c';
   return b;
 }
 
 // Fill ghosts of up to four ghosted fields; `ids` give the bc set of each pointer.
-int ghost(fen_ctx* c, int nf, double* const* ptr, const int* ids) {
-  GhostBatch<double> G;
+// `homogeneous` uses zero Dirichlet values (increments of fields that satisfy the BCs).
+template <typename T>
+int ghost(fen_ctx* c, int nf, T* const* ptr, const int* ids, bool homogeneous = false) {
+  GhostBatch<T> G;
   memset(&G, 0, sizeof(G));
   long long mx = 0;
   for (int q = 0; q < nf; ++q) {
     G.f[q] = ptr[q];
-    G.bc[q] = field_bc(c, ids[q]);
+    G.bc[q] = field_bc(c, ids[q], homogeneous);
     GhostCount g = (c->dim == 3) ? ghost_count<3>(c->L, G.bc[q]) : ghost_count<2>(c->L, G.bc[q]);
     G.n[q] = g.a + g.b + g.c;
     G.shift[q] = 0.0;
     mx = std::max(mx, G.n[q]);
   }
   dim3 grid(std::min(cdiv(mx, 256), 4096), nf);
-  if (c->dim == 3) k_ghost_fill<double, 3><<<grid, 256, 0, c->stream>>>(c->L, G);
-  else k_ghost_fill<double, 2><<<grid, 256, 0, c->stream>>>(c->L, G);
+  if (c->dim == 3) k_ghost_fill<T, 3><<<grid, 256, 0, c->stream>>>(c->L, G);
+  else k_ghost_fill<T, 2><<<grid, 256, 0, c->stream>>>(c->L, G);
+  c->launches++;
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int launch_mean(fen_ctx* c, float* target32 = nullptr) {
+  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+  const int grid = std::min(cdiv(ncell, 256), 152 * 8);
+  if (c->mixed) {
+    float* t = target32 ? target32 : c->phi32;
+    if (c->dim == 3) k_mean_subtract<float, 3><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, t);
+    else k_mean_subtract<float, 2><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, t);
+  } else {
+    if (c->dim == 3) k_mean_subtract<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, c->phi);
+    else k_mean_subtract<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, c->phi);
+  }
   c->launches++;
   CK(cudaGetLastError());
   return 0;
@@ -531,39 +648,36 @@ int ghost(fen_ctx* c, int nf, double* const* ptr, const int* ids) {
 
 int run_poisson(fen_ctx* c, bool from_field) {
   int r;
-  for (size_t q = 0; q < c->stages.size(); ++q) {
-    const Stage& s = c->stages[q];
-    if (s.kind == 1) {
-      const bool real = (c->solver == S_NN || c->solver == S_NNN);
-      if ((r = real ? launch_thomas_real(c, s) : launch_stage(c, s, 0, nullptr))) return r;
-    } else {
-      if ((r = launch_stage(c, s, from_field && q == 0, c->phi))) return r;
-    }
-  }
-  if (c->needs_mean) {
-    const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
-    const int grid = std::min(cdiv(ncell, 256), 152 * 8);
-    if (c->dim == 3) k_mean_subtract<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, c->phi);
-    else k_mean_subtract<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, c->phi);
-    c->launches++;
-    CK(cudaGetLastError());
-  }
+  const void* src = c->mixed ? (const void*)c->phi32 : (const void*)c->phi;
+  for (size_t q = 0; q < c->stages.size(); ++q)
+    if ((r = launch_stage(c, c->stages[q], from_field && q == 0, src))) return r;
+  if (c->needs_mean && (r = launch_mean(c))) return r;
   return 0;
 }
 
-PredArgs<double> pred_args(fen_ctx* c) {
-  PredArgs<double> a;
+double rhof_of(fen_ctx* c) { return 0.5 * (c->prm.density + c->prm.density); }
+
+template <typename T>
+PredArgs<T> pred_args(fen_ctx* c) {
+  PredArgs<T> a;
   memset(&a, 0, sizeof(a));
-  a.u = c->u; a.v = c->v; a.w = c->w; a.p = c->p;
-  a.us = c->us; a.vs = c->vs; a.ws = c->ws;
-  a.dox = c->dvo[0]; a.doy = c->dvo[1]; a.doz = c->dvo[2];
-  a.Sx = c->S[0]; a.Sy = c->S[1]; a.Sz = c->S[2];
+  if (c->mixed) {
+    a.u = (const T*)c->u32; a.v = (const T*)c->v32; a.w = (const T*)c->w32; a.p = (const T*)c->p32;
+    a.us = (T*)c->d32[0]; a.vs = (T*)c->d32[1]; a.ws = (T*)c->d32[2];
+    a.dox = (T*)c->dvo32[0]; a.doy = (T*)c->dvo32[1]; a.doz = (T*)c->dvo32[2];
+    a.Sx = (const T*)c->S32[0]; a.Sy = (const T*)c->S32[1]; a.Sz = (const T*)c->S32[2];
+  } else {
+    a.u = (const T*)c->u; a.v = (const T*)c->v; a.w = (const T*)c->w; a.p = (const T*)c->p;
+    a.us = (T*)c->us; a.vs = (T*)c->vs; a.ws = (T*)c->ws;
+    a.dox = (T*)c->dvo[0]; a.doy = (T*)c->dvo[1]; a.doz = (T*)c->dvo[2];
+    a.Sx = (const T*)c->S[0]; a.Sy = (const T*)c->S[1]; a.Sz = (const T*)c->S[2];
+  }
   for (int q = 0; q < 3; ++q) {
     a.id[q] = 1.0 / c->d[q];
     a.id2[q] = 1.0 / (c->d[q] * c->d[q]);
   }
   a.mu = c->prm.viscosity;
-  a.rhof = 0.5 * (c->prm.density + c->prm.density);  // center_to_face of a constant density
+  a.rhof = rhof_of(c);  // center_to_face of a constant density
   a.rhof_one = (a.rhof == 1.0);
   for (int q = 0; q < 3; ++q) a.g[q] = c->prm.g[q];
   a.iso = c->iso;
@@ -572,7 +686,56 @@ PredArgs<double> pred_args(fen_ctx* c) {
   return a;
 }
 
+int launch_predictor(fen_ctx* c, const StepScalars* sc) {
+  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+  const int grid = std::min(cdiv(ncell, 256), 152 * 16);
+  if (c->mixed) {
+    PredDFArgs pa;
+    memset(&pa, 0, sizeof(pa));
+    pa.u = DFField{c->u32, c->u32l}; pa.v = DFField{c->v32, c->v32l};
+    pa.w = DFField{c->w32, c->w32l}; pa.p = DFField{c->p32, c->p32l};
+    pa.du = c->d32[0]; pa.dv = c->d32[1]; pa.dw = c->d32[2];
+    pa.dox = c->dvo32[0]; pa.doy = c->dvo32[1]; pa.doz = c->dvo32[2];
+    pa.Sx = c->S32[0]; pa.Sy = c->S32[1]; pa.Sz = c->S32[2];
+    for (int q = 0; q < 3; ++q) {
+      pa.id[q] = 1.0 / c->d[q];
+      pa.id2[q] = 1.0 / (c->d[q] * c->d[q]);
+    }
+    pa.mu = c->prm.viscosity;
+    pa.rhof = rhof_of(c);
+    pa.rhof_one = (pa.rhof == 1.0);
+    for (int q = 0; q < 3; ++q) pa.g[q] = c->prm.g[q];
+    pa.iso = c->iso;
+    pa.has_S = c->has_S;
+    if (c->dim == 3) k_predictor_df<3><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+    else k_predictor_df<2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+  } else {
+    PredArgs<double> pa = pred_args<double>(c);
+    if (c->dim == 3) k_predictor<double, 3><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+    else k_predictor<double, 2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+  }
+  c->launches++;
+  CK(cudaGetLastError());
+  return 0;
+}
+
 int launch_checks(fen_ctx* c, int want_div) {
+  if (c->mixed) {
+    CheckDFArgs a;
+    memset(&a, 0, sizeof(a));
+    a.u = DFField{c->u32, c->u32l}; a.v = DFField{c->v32, c->v32l}; a.w = DFField{c->w32, c->w32l};
+    for (int q = 0; q < 3; ++q) a.idp[q] = split_d(1.0 / c->d[q]);
+    a.want_div = want_div;
+    a.pdiv = c->pdiv; a.pvel = c->pvel; a.nan_flag = c->nan_flag;
+    if (c->dim == 3) k_checks_df<3><<<c->nred, 256, 0, c->stream>>>(c->L, a);
+    else k_checks_df<2><<<c->nred, 256, 0, c->stream>>>(c->L, a);
+    c->launches++;
+    CK(cudaGetLastError());
+    k_finalize<<<1, 256, 0, c->stream>>>(c->pdiv, c->pvel, c->nred, c->sc, c->dmin, 0.0, 1, c->nan_flag);
+    c->launches++;
+    CK(cudaGetLastError());
+    return 0;
+  }
   CheckArgs<double> a;
   memset(&a, 0, sizeof(a));
   a.u = c->u; a.v = c->v; a.w = c->w;
@@ -590,7 +753,50 @@ int launch_checks(fen_ctx* c, int want_div) {
   return 0;
 }
 
-const double rhof_of(fen_ctx* c) { return 0.5 * (c->prm.density + c->prm.density); }
+// Mixed form: the pair (hi, lo) arrays of a state field.
+bool pair_of(fen_ctx* c, int f, float** hi, float** lo, double** d) {
+  switch (f) {
+    case FEN_U: *hi = c->u32; *lo = c->u32l; *d = c->u; return true;
+    case FEN_V: *hi = c->v32; *lo = c->v32l; *d = c->v; return true;
+    case FEN_W: *hi = c->w32; *lo = c->w32l; *d = c->w; return true;
+    case FEN_P: *hi = c->p32; *lo = c->p32l; *d = c->p; return true;
+  }
+  return false;
+}
+
+// FP64 staging array <-> pairs (every stored element); dir 0: split, 1: join.
+int pair_convert(fen_ctx* c, int f, int dir) {
+  float *hi, *lo;
+  double* d;
+  if (!pair_of(c, f, &hi, &lo, &d)) return 0;
+  const int grid = std::min(cdiv(c->L.total, 256), 152 * 16);
+  if (dir == 0) k_split<<<grid, 256, 0, c->stream>>>(c->L.total, d, hi, lo);
+  else k_join<<<grid, 256, 0, c->stream>>>(c->L.total, hi, lo, d);
+  c->launches++;
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// Ghost fill of up to four pair fields.
+int ghost_pairs(fen_ctx* c, int nf, const int* ids) {
+  GhostDFBatch G;
+  memset(&G, 0, sizeof(G));
+  long long mx = 0;
+  for (int q = 0; q < nf; ++q) {
+    double* d;
+    pair_of(c, ids[q], &G.hi[q], &G.lo[q], &d);
+    G.bc[q] = field_bc(c, ids[q]);
+    GhostCount g = (c->dim == 3) ? ghost_count<3>(c->L, G.bc[q]) : ghost_count<2>(c->L, G.bc[q]);
+    G.n[q] = g.a + g.b + g.c;
+    mx = std::max(mx, G.n[q]);
+  }
+  dim3 grid(std::min(cdiv(mx, 256), 4096), nf);
+  if (c->dim == 3) k_ghost_fill_df<3><<<grid, 256, 0, c->stream>>>(c->L, G);
+  else k_ghost_fill_df<2><<<grid, 256, 0, c->stream>>>(c->L, G);
+  c->launches++;
+  CK(cudaGetLastError());
+  return 0;
+}
 
 // One navier_stokes_solver step as a launch sequence on c->stream.  `ev` (optional) gets
 // an event after each stage for fen_profile_step.
@@ -603,69 +809,99 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
   mark();
   k_prologue<<<1, 32, 0, c->stream>>>(c->sc, c->prm.constant_cfl, c->prm.cfl, c->dmin, c->prm.density, rhof_of(c));
   c->launches++;
-  PredArgs<double> pa = pred_args(c);
-  if (c->dim == 3) k_predictor<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, pa);
-  else k_predictor<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, pa);
-  c->launches++;
-  CK(cudaGetLastError());
+  if ((r = launch_predictor(c, c->sc))) return r;
   mark();  // 1: predictor
-  {
+  if (c->mixed) {
+    float* f[3] = {c->d32[0], c->d32[1], c->d32[2]};
+    int ids[3] = {FEN_U, FEN_V, FEN_W};
+    if ((r = ghost<float>(c, c->dim, f, ids, true))) return r;
+  } else {
     double* f[3] = {c->us, c->vs, c->ws};
     int ids[3] = {FEN_U, FEN_V, FEN_W};
-    if ((r = ghost(c, c->dim, f, ids))) return r;
+    if ((r = ghost<double>(c, c->dim, f, ids))) return r;
   }
-  mark();  // 2: ghost v*
-  // Poisson: forward transform(s), solve, inverse
+  mark();  // 2: ghost v* (or its increment)
   {
-    int r2;
     const size_t ns = c->stages.size();
     for (size_t q = 0; q < ns; ++q) {
-      const Stage& s = c->stages[q];
-      if (s.kind == 1) {
-        const bool real = (c->solver == S_NN || c->solver == S_NNN);
-        if ((r2 = real ? launch_thomas_real(c, s) : launch_stage(c, s, 0, nullptr))) return r2;
-      } else {
-        if ((r2 = launch_stage(c, s, 0, nullptr))) return r2;
-      }
-      if (q == 0) mark();           // 3: first (fused divergence) transform
-      if (q + 2 == ns) mark();      // 4: spectral middle stages
+      if ((r = launch_stage(c, c->stages[q], 0, nullptr))) return r;
+      if (q == 0) mark();       // 3: first (fused divergence) transform
+      if (q + 2 == ns) mark();  // 4: spectral middle stages
     }
-    if (ns < 3) mark();
-    if (c->needs_mean) {
-      const int g2 = std::min(cdiv(ncell, 256), 152 * 8);
-      if (c->dim == 3) k_mean_subtract<double, 3><<<g2, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, c->phi);
-      else k_mean_subtract<double, 2><<<g2, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, c->phi);
-      c->launches++;
-      CK(cudaGetLastError());
-    }
+    if (c->needs_mean && (r = launch_mean(c))) return r;
   }
   mark();  // 5: inverse x transform (+ mean)
-  {
+  if (c->mixed) {
+    float* f[1] = {c->phi32};
+    int ids[1] = {FEN_PHI};
+    if ((r = ghost<float>(c, 1, f, ids))) return r;
+    if (c->refine) {
+      // one iterative-refinement solve: r = b - L_h phi (double-float), L_h dphi = r (FP32)
+      ResidualArgs ra;
+      memset(&ra, 0, sizeof(ra));
+      ra.u = DFField{c->u32, c->u32l}; ra.v = DFField{c->v32, c->v32l}; ra.w = DFField{c->w32, c->w32l};
+      ra.du = c->d32[0]; ra.dv = c->d32[1]; ra.dw = c->d32[2];
+      ra.phi = c->phi32;
+      ra.r = c->res32;
+      for (int q = 0; q < 3; ++q) {
+        ra.idp[q] = split_d(1.0 / c->d[q]);
+        ra.id2p[q] = split_d(1.0 / (c->d[q] * c->d[q]));
+      }
+      if (c->dim == 3) k_residual_df<3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ra);
+      else k_residual_df<2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ra);
+      c->launches++;
+      CK(cudaGetLastError());
+      const size_t ns = c->stages.size();
+      for (size_t q = 0; q < ns; ++q)
+        if ((r = launch_stage(c, c->stages[q], q == 0, c->res32, c->dphi32))) return r;
+      if (c->needs_mean && (r = launch_mean(c, c->dphi32))) return r;
+      float* g[1] = {c->dphi32};
+      if ((r = ghost<float>(c, 1, g, ids))) return r;
+    }
+    CorrDFArgs ca;
+    memset(&ca, 0, sizeof(ca));
+    ca.du = c->d32[0]; ca.dv = c->d32[1]; ca.dw = c->d32[2]; ca.phi = c->phi32;
+    ca.dphi = c->refine ? c->dphi32 : nullptr;
+    ca.u = DFFieldW{c->u32, c->u32l}; ca.v = DFFieldW{c->v32, c->v32l};
+    ca.w = DFFieldW{c->w32, c->w32l}; ca.p = DFFieldW{c->p32, c->p32l};
+    for (int q = 0; q < 3; ++q) ca.id[q] = 1.0 / c->d[q];
+    ca.iso = c->iso;
+    ca.rhof = rhof_of(c);
+    if (c->dim == 3) k_correct_df<3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
+    else k_correct_df<2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
+    c->launches++;
+    CK(cudaGetLastError());
+  } else {
     double* f[1] = {c->phi};
     int ids[1] = {FEN_PHI};
-    if ((r = ghost(c, 1, f, ids))) return r;
+    if ((r = ghost<double>(c, 1, f, ids))) return r;
+    CorrArgs<double> ca;
+    memset(&ca, 0, sizeof(ca));
+    ca.us = c->us; ca.vs = c->vs; ca.ws = c->ws; ca.phi = c->phi;
+    ca.u = c->u; ca.v = c->v; ca.w = c->w; ca.p = c->p;
+    for (int q = 0; q < 3; ++q) ca.id[q] = 1.0 / c->d[q];
+    ca.iso = c->iso;
+    ca.use_dev_dt = 1;
+    ca.rhof = rhof_of(c);
+    ca.rhof_one = (ca.rhof == 1.0);
+    if (c->dim == 3) k_correct<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
+    else k_correct<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
+    c->launches++;
+    CK(cudaGetLastError());
   }
-  CorrArgs<double> ca;
-  memset(&ca, 0, sizeof(ca));
-  ca.us = c->us; ca.vs = c->vs; ca.ws = c->ws; ca.phi = c->phi;
-  ca.u = c->u; ca.v = c->v; ca.w = c->w; ca.p = c->p;
-  for (int q = 0; q < 3; ++q) ca.id[q] = 1.0 / c->d[q];
-  ca.iso = c->iso;
-  ca.use_dev_dt = 1;
-  ca.rhof = rhof_of(c);
-  ca.rhof_one = (ca.rhof == 1.0);
-  if (c->dim == 3) k_correct<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
-  else k_correct<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
-  c->launches++;
-  CK(cudaGetLastError());
   mark();  // 6: phi ghost + correction
   {
     double* f[4] = {c->u, c->v, c->w, c->p};
     int ids[4] = {FEN_U, FEN_V, FEN_W, FEN_P};
     double* f2[3] = {c->u, c->v, c->p};
     int ids2[3] = {FEN_U, FEN_V, FEN_P};
-    if (c->dim == 3) { if ((r = ghost(c, 4, f, ids))) return r; }
-    else { if ((r = ghost(c, 3, f2, ids2))) return r; }
+    if (c->mixed) {
+      if ((r = ghost_pairs(c, c->dim == 3 ? 4 : 3, c->dim == 3 ? ids : ids2))) return r;
+    } else if (c->dim == 3) {
+      if ((r = ghost<double>(c, 4, f, ids))) return r;
+    } else {
+      if ((r = ghost<double>(c, 3, f2, ids2))) return r;
+    }
   }
   mark();  // 7: ghosts
   if ((r = launch_checks(c, 1))) return r;
@@ -673,24 +909,12 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
   return 0;
 }
 
-double* field_ptr(fen_ctx* c, int f) {
-  switch (f) {
-    case FEN_U: return c->u;
-    case FEN_V: return c->v;
-    case FEN_W: return c->w;
-    case FEN_P: return c->p;
-    case FEN_PHI: return c->phi;
-    case FEN_DVO_X: case FEN_DVO_Y: case FEN_DVO_Z: return c->dvo[f - FEN_DVO_X];
-    case FEN_S_X: case FEN_S_Y: case FEN_S_Z: return c->S[f - FEN_S_X];
-  }
-  return nullptr;
-}
-
 int host_planes(fen_ctx* c) { return c->dim == 3 ? c->n[2] + 2 : 3; }
 
 // Copy one field between FEN's host layout and the padded HBM layout through a contiguous
 // staging buffer (one memcpy + one relayout kernel).  dir 0: host -> device, 1: back.
-int relayout(fen_ctx* c, double* dfield, double* host_rw, int dir) {
+template <typename T>
+int relayout(fen_ctx* c, T* dfield, double* host_rw, int dir) {
   const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
   const int planes = (c->dim == 3) ? c->n[2] + 2 : 1;
   const size_t cnt = (size_t)nxg * nyg * planes;
@@ -702,11 +926,11 @@ int relayout(fen_ctx* c, double* dfield, double* host_rw, int dir) {
   const int grid = std::min(cdiv((long long)cnt, 256), 152 * 16);
   if (dir == 0) {
     CK(cudaMemcpyAsync(c->stage_scratch, h, cnt * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    k_relayout<double><<<grid, 256, 0, c->stream>>>(c->L, planes, c->stage_scratch, dfield, nullptr, nullptr, 0);
+    k_relayout<T><<<grid, 256, 0, c->stream>>>(c->L, planes, c->stage_scratch, dfield, nullptr, nullptr, 0);
     c->launches++;
     CK(cudaGetLastError());
   } else {
-    k_relayout<double><<<grid, 256, 0, c->stream>>>(c->L, planes, nullptr, nullptr, dfield, c->stage_scratch, 1);
+    k_relayout<T><<<grid, 256, 0, c->stream>>>(c->L, planes, nullptr, nullptr, dfield, c->stage_scratch, 1);
     c->launches++;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h, c->stage_scratch, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -729,6 +953,13 @@ int pre_step(fen_ctx* c, double dt) {
   }
   c->vel_dirty = 0;
   return 0;
+}
+
+void drop_graph(fen_ctx* c) {
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
 }
 
 int capture_graph(fen_ctx* c) {
@@ -767,14 +998,19 @@ const char* fen_last_error(void) { return g_err.c_str(); }
 
 int fen_ctx_destroy(fen_ctx* c) {
   if (!c) return 0;
-  if (c->graph) cudaGraphExecDestroy(c->graph);
+  drop_graph(c);
   double* bufs[] = {c->u, c->v, c->w, c->p, c->phi, c->us, c->vs, c->ws, c->dvo[0], c->dvo[1], c->dvo[2],
                     c->S[0], c->S[1], c->S[2], c->mwn[0], c->mwn[1], c->mwn[2], c->ta, c->tb, c->tc, c->c1,
                     c->fac, c->partial, c->pdiv, c->pvel, c->stage_scratch};
   for (double* b : bufs) if (b) cudaFree(b);
+  float* fb[] = {c->u32, c->v32, c->w32, c->p32, c->u32l, c->v32l, c->w32l, c->p32l, c->phi32, c->d32[0],
+                 c->d32[1], c->d32[2], c->dvo32[0], c->dvo32[1], c->dvo32[2], c->S32[0], c->S32[1], c->S32[2],
+                 c->dphi32, c->res32};
+  for (float* b : fb) if (b) cudaFree(b);
   for (int f = 0; f < 5; ++f) for (int q = 0; q < 6; ++q) if (c->bcval[f][q]) cudaFree(c->bcval[f][q]);
   if (c->specC) cudaFree(c->specC);
   if (c->specR) cudaFree(c->specR);
+  if (c->inv_lam) cudaFree(c->inv_lam);
   for (void* b : c->twbufs) cudaFree(b);
   if (c->nan_flag) cudaFree(c->nan_flag);
   if (c->sc) cudaFree(c->sc);
@@ -789,13 +1025,19 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
   *out = nullptr;
   if (P->dim != 2 && P->dim != 3) return fail(FEN_ERR_ARG, "dim must be 2 or 3");
   if (P->nx < 2 || P->ny < 2 || (P->dim == 3 && P->nz < 2)) return fail(FEN_ERR_ARG, "grid sizes must be >= 2");
-  if (P->precision != FEN_FP64) return fail(FEN_ERR_ARG, "precision form not available in this build");
+  if (P->precision != FEN_FP64 && P->precision != FEN_MIXED) return fail(FEN_ERR_ARG, "unknown precision form");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(FEN_ERR_CUDA, "no CUDA device");
   fen_ctx* c = new fen_ctx();
   memset(c->ftype, 0, sizeof(c->ftype));
   memset(c->bcval, 0, sizeof(c->bcval));
   c->prm = *P;
+  c->mixed = (P->precision == FEN_MIXED);
+  if (P->refine < 0 || P->refine > 1) {
+    delete c;
+    return fail(FEN_ERR_ARG, "refine must be 0 or 1");
+  }
+  c->refine = c->mixed ? P->refine : 0;
   c->dim = P->dim;
   c->n[0] = P->nx; c->n[1] = P->ny; c->n[2] = (P->dim == 3) ? P->nz : 1;
   // grid%setup: delta = Lx/float(Nx) (grid.f90:140); per-axis spacing when aniso
@@ -837,9 +1079,20 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
   const int planes = (c->dim == 3) ? c->n[2] + 2 : 1;
   L.total = L.off + L.sp * planes + 4;
   int r = 0;
-  double** fl[] = {&c->u, &c->v, &c->w, &c->p, &c->phi, &c->us, &c->vs, &c->ws, &c->dvo[0], &c->dvo[1], &c->dvo[2]};
-  for (double** f : fl)
+  double** state[] = {&c->u, &c->v, &c->w, &c->p};
+  for (double** f : state)
     if ((r = alloc(f, L.total))) { fen_ctx_destroy(c); return r; }
+  if (c->mixed) {
+    float** fl[] = {&c->u32, &c->v32, &c->w32, &c->p32, &c->u32l, &c->v32l, &c->w32l, &c->p32l, &c->phi32,
+                    &c->d32[0], &c->d32[1], &c->d32[2], &c->dvo32[0], &c->dvo32[1], &c->dvo32[2]};
+    for (float** f : fl)
+      if ((r = alloc(f, L.total))) { fen_ctx_destroy(c); return r; }
+    if (c->refine && ((r = alloc(&c->dphi32, L.total)) || (r = alloc(&c->res32, L.total)))) { fen_ctx_destroy(c); return r; }
+  } else {
+    double** fl[] = {&c->phi, &c->us, &c->vs, &c->ws, &c->dvo[0], &c->dvo[1], &c->dvo[2]};
+    for (double** f : fl)
+      if ((r = alloc(f, L.total))) { fen_ctx_destroy(c); return r; }
+  }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { fen_ctx_destroy(c); return fail(FEN_ERR_CUDA, "stream"); }
   if (cudaMalloc((void**)&c->sc, sizeof(StepScalars)) != cudaSuccess ||
       cudaMallocHost((void**)&c->sc_host, sizeof(StepScalars)) != cudaSuccess) { fen_ctx_destroy(c); return fail(FEN_ERR_NOMEM, "scalars"); }
@@ -850,55 +1103,68 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
   if (cudaMalloc((void**)&c->nan_flag, sizeof(int)) != cudaSuccess) { fen_ctx_destroy(c); return fail(FEN_ERR_NOMEM, "flag"); }
   cudaMemset(c->nan_flag, 0, sizeof(int));
   if ((r = init_poisson(c))) { fen_ctx_destroy(c); return r; }
-  // dt_visc from set_timestep's formula needs only the grid; computed there.
   *out = c;
   return 0;
 }
 
 int fen_upload(fen_ctx* c, int f, const double* host) {
   if (!c || !host) return fail(FEN_ERR_ARG, "null argument");
-  double* d = field_ptr(c, f);
-  if (f >= FEN_S_X && f <= FEN_S_Z) {
-    if (!c->S[f - FEN_S_X]) {
-      int r;
-      if ((r = alloc(&c->S[f - FEN_S_X], c->L.total))) return r;
-    }
-    d = c->S[f - FEN_S_X];
-    // S is used in every component once any is set (dv += S/rhof, navier_stokes.f90:245-255)
-    for (int q = 0; q < 3; ++q)
-      if (!c->S[q]) { int r; if ((r = alloc(&c->S[q], c->L.total))) return r; }
-    c->has_S = 1;
-    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-  }
-  if (!d || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
+  if (f < FEN_U || f > FEN_S_Z || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
+  double* hrw = const_cast<double*>(host);
   int r;
-  if ((r = relayout(c, d, const_cast<double*>(host), 0))) return r;
+  if (f >= FEN_S_X && f <= FEN_S_Z) {
+    // S is used in every component once any is set (dv += S/rhof, navier_stokes.f90:245-255)
+    for (int q = 0; q < 3; ++q) {
+      if (c->mixed && !c->S32[q] && (r = alloc(&c->S32[q], c->L.total))) return r;
+      if (!c->mixed && !c->S[q] && (r = alloc(&c->S[q], c->L.total))) return r;
+    }
+    c->has_S = 1;
+    drop_graph(c);
+    return c->mixed ? relayout<float>(c, c->S32[f - FEN_S_X], hrw, 0) : relayout<double>(c, c->S[f - FEN_S_X], hrw, 0);
+  }
+  if (f >= FEN_DVO_X && f <= FEN_DVO_Z)
+    return c->mixed ? relayout<float>(c, c->dvo32[f - FEN_DVO_X], hrw, 0) : relayout<double>(c, c->dvo[f - FEN_DVO_X], hrw, 0);
+  if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, hrw, 0) : relayout<double>(c, c->phi, hrw, 0);
+  double* d = (f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p;
+  if ((r = relayout<double>(c, d, hrw, 0))) return r;
+  if (c->mixed && (r = pair_convert(c, f, 0))) return r;
   if (f == FEN_U || f == FEN_V || f == FEN_W) c->vel_dirty = 1;
+  CK(cudaStreamSynchronize(c->stream));
   return 0;
 }
 
 int fen_download(fen_ctx* c, int f, double* host) {
   if (!c || !host) return fail(FEN_ERR_ARG, "null argument");
-  double* d = field_ptr(c, f);
-  if (!d || (f == FEN_W && c->dim == 2)) {
-    if (f >= FEN_S_X && f <= FEN_S_Z) {
+  if (f < FEN_U || f > FEN_S_Z || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
+  if (f >= FEN_S_X && f <= FEN_S_Z) {
+    if (!c->has_S) {
       const size_t nh = (size_t)(c->n[0] + 2) * (c->n[1] + 2) * host_planes(c);
       memset(host, 0, nh * sizeof(double));
       return 0;
     }
-    return fail(FEN_ERR_ARG, "bad field id");
+    return c->mixed ? relayout<float>(c, c->S32[f - FEN_S_X], host, 1) : relayout<double>(c, c->S[f - FEN_S_X], host, 1);
   }
+  if (f >= FEN_DVO_X && f <= FEN_DVO_Z)
+    return c->mixed ? relayout<float>(c, c->dvo32[f - FEN_DVO_X], host, 1) : relayout<double>(c, c->dvo[f - FEN_DVO_X], host, 1);
+  if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, host, 1) : relayout<double>(c, c->phi, host, 1);
+  double* d = (f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p;
   int r;
-  if ((r = relayout(c, d, host, 1))) return r;
-  return 0;
+  if (c->mixed && (r = pair_convert(c, f, 1))) return r;
+  return relayout<double>(c, d, host, 1);
 }
 
 int fen_update_ghost_nodes(fen_ctx* c, int f) {
   if (!c) return fail(FEN_ERR_ARG, "null argument");
   if (f < FEN_U || f > FEN_PHI || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "field has no ghost nodes");
-  double* p[1] = {field_ptr(c, f)};
   int ids[1] = {f};
-  int r = ghost(c, 1, p, ids);
+  int r;
+  if (f == FEN_PHI) {
+    if (c->mixed) { float* p[1] = {c->phi32}; r = ghost<float>(c, 1, p, ids); }
+    else { double* p[1] = {c->phi}; r = ghost<double>(c, 1, p, ids); }
+  } else {
+    double* p[1] = {(f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p};
+    r = c->mixed ? ghost_pairs(c, 1, ids) : ghost<double>(c, 1, p, ids);
+  }
   if (r) return r;
   CK(cudaStreamSynchronize(c->stream));
   return 0;
@@ -919,14 +1185,14 @@ int fen_set_bc_values(fen_ctx* c, int f, int face, const double* vals) {
     if ((r = alloc(&c->bcval[f][face], (long long)na * nbd))) return r;
   }
   CK(cudaMemcpy(c->bcval[f][face], src, (size_t)na * nbd * sizeof(double), cudaMemcpyHostToDevice));
-  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  drop_graph(c);
   return 0;
 }
 
 int fen_set_bc_type(fen_ctx* c, int f, int face, int t) {
   if (!c || f < FEN_U || f > FEN_PHI || face < 0 || face >= 6 || t < 0 || t > 2) return fail(FEN_ERR_ARG, "bad argument");
   c->ftype[f][face] = t;
-  if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+  drop_graph(c);
   return 0;
 }
 
@@ -938,8 +1204,6 @@ int fen_set_timestep(fen_ctx* c, double U, double* dt) {
   double dt_visc = 0.125 * dl * dl * c->prm.density / c->prm.viscosity;
   if (c->dim == 3) dt_visc = (1.0 / 6.0) * dl * dl * c->prm.density / c->prm.viscosity;
   *dt = std::min(dt_conv, dt_visc);
-  c->dt_visc = dt_visc;
-  c->dt_o = *dt;
   c->sc_host->dt = *dt;
   c->sc_host->dt_o = *dt;
   c->sc_host->dt_visc = dt_visc;
@@ -1017,10 +1281,8 @@ int fen_solve_poisson(fen_ctx* c) {
 
 int fen_divergence(fen_ctx* c, double* out) {
   if (!c || !out) return fail(FEN_ERR_ARG, "null argument");
-  // divergence of the current v into phi's scratch via the fused loader of the first
-  // transform is not reusable here; compute on the host-visible path with the check kernel
-  // arithmetic instead (fields.f90:120-153).
-  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+  // divergence_of_vector of the FP64 velocity (fields.f90:120-153), evaluated on the host
+  // from a download (a test and post-processing aid, not on the step path)
   std::vector<double> hu((size_t)(c->n[0] + 2) * (c->n[1] + 2) * host_planes(c));
   std::vector<double> hv(hu.size()), hw(hu.size());
   int r;
@@ -1044,34 +1306,30 @@ int fen_divergence(fen_ctx* c, double* out) {
         }
         out[t++] = d;
       }
-  (void)ncell;
   return 0;
 }
 
 int fen_explicit_terms(fen_ctx* c, double* out) {
   if (!c || !out) return fail(FEN_ERR_ARG, "null argument");
-  // Run the predictor with A = 1, B = 0, dt = 1 on a copy of dv_o, then read dv_o back:
-  // dv_o <- dv is exactly compute_explicit_terms (navier_stokes.f90:217-257).
+  // Run the predictor with A = 1, B = 0, dt = 1 and read dv_o back: dv_o <- dv is exactly
+  // compute_explicit_terms (navier_stokes.f90:217-257).  dv_o is restored afterwards.
   int r;
   const long long tot = c->L.total;
-  std::vector<double*> save(3, nullptr);
+  const size_t es = c->mixed ? sizeof(float) : sizeof(double);
+  std::vector<void*> save(3, nullptr);
   for (int q = 0; q < c->dim; ++q) {
-    if ((r = alloc(&save[q], tot))) return r;
-    CK(cudaMemcpyAsync(save[q], c->dvo[q], tot * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMalloc(&save[q], tot * es));
+    void* src = c->mixed ? (void*)c->dvo32[q] : (void*)c->dvo[q];
+    CK(cudaMemcpyAsync(save[q], src, tot * es, cudaMemcpyDeviceToDevice, c->stream));
   }
   StepScalars s = *c->sc_host;
   s.A = 1.0; s.B = 0.0; s.dt = 1.0;
   StepScalars* dsc;
   CK(cudaMalloc((void**)&dsc, sizeof(StepScalars)));
   CK(cudaMemcpyAsync(dsc, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream));
-  PredArgs<double> pa = pred_args(c);
-  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
-  const int grid = std::min(cdiv(ncell, 256), 152 * 16);
-  if (c->dim == 3) k_predictor<double, 3><<<grid, 256, 0, c->stream>>>(c->L, dsc, pa);
-  else k_predictor<double, 2><<<grid, 256, 0, c->stream>>>(c->L, dsc, pa);
-  c->launches++;
-  CK(cudaGetLastError());
+  if ((r = launch_predictor(c, dsc))) return r;
   const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
+  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
   std::vector<double> h((size_t)nxg * nyg * host_planes(c));
   for (int q = 0; q < c->dim; ++q) {
     if ((r = fen_download(c, FEN_DVO_X + q, h.data()))) return r;
@@ -1081,7 +1339,8 @@ int fen_explicit_terms(fen_ctx* c, double* out) {
       for (int j = 1; j <= c->n[1]; ++j)
         for (int i = 1; i <= c->n[0]; ++i)
           out[(size_t)q * ncell + t++] = h[(size_t)i + (size_t)nxg * ((size_t)j + (size_t)nyg * k)];
-    CK(cudaMemcpyAsync(c->dvo[q], save[q], tot * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    void* dst = c->mixed ? (void*)c->dvo32[q] : (void*)c->dvo[q];
+    CK(cudaMemcpyAsync(dst, save[q], tot * es, cudaMemcpyDeviceToDevice, c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
   for (int q = 0; q < c->dim; ++q) cudaFree(save[q]);

@@ -22,18 +22,23 @@ struct FFTPlan {
   int R[kMaxStages];           // radices, 4s first, then 2, then 3
 };
 
-// Twiddle tables of one transform axis (device pointers, FP64 values computed on the host
-// with libm cos/sin; FP32 kernels convert on load).
+// Twiddle tables of one transform axis (device pointers; values computed on the host in
+// FP64 with libm cos/sin, stored as double2 for FP64 kernels and rounded to float2 for FP32).
 struct AxisTw {
   const double2* wM;   // exp(-2 pi i m / M),      m < M   (complex FFT of length M = n/2)
   const double2* wN;   // exp(-2 pi i k / n),      k <= n/2 (real-FFT packing)
   const double2* wD;   // exp(-i pi k / (2n)),     k < n   (DCT packing)
 };
 
+// Twiddle load.  FP64 kernels read double2 tables; FP32 kernels are handed float2 tables
+// through the same pointer slot (no FP64 conversion inside the transform loops).
 template <typename T2>
-__device__ __forceinline__ T2 ldtw(const double2* p, int m) {
-  double2 w = __ldg(p + m);
-  return mk<T2>((decltype(T2::x))w.x, (decltype(T2::x))w.y);
+__device__ __forceinline__ T2 ldtw(const double2* p, int m);
+template <>
+__device__ __forceinline__ double2 ldtw<double2>(const double2* p, int m) { return __ldg(p + m); }
+template <>
+__device__ __forceinline__ float2 ldtw<float2>(const double2* p, int m) {
+  return __ldg(reinterpret_cast<const float2*>(p) + m);
 }
 
 // In-register DFT of size R (R = 2, 3, 4), sign DIR (-1 forward, +1 backward).

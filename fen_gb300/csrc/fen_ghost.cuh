@@ -13,9 +13,17 @@
 
 namespace fen {
 
-template <typename T, int DIM>
-struct Resolve {
+// Interior value source: a plain array (the default) or any functor returning T for an
+// element index (the mixed form reads hi + lo pairs through one).
+template <typename T>
+struct PtrSrc {
   const T* f;
+  __device__ __forceinline__ T operator()(long long i) const { return f[i]; }
+};
+
+template <typename T, int DIM, typename Src = PtrSrc<T>>
+struct Resolve {
+  Src f;
   Layout L;
   FieldBC bc;
   double shift;  // subtracted from every interior value read (0 = none)
@@ -29,7 +37,7 @@ struct Resolve {
     return (T)p[a + (long long)na * b];
   }
   __device__ __forceinline__ T state(int i, int j, int k) const {
-    T v = f[L.idx(i, j, kst<DIM>(k))];
+    T v = f(L.idx(i, j, kst<DIM>(k)));
     return shift != 0.0 ? (T)(v - (T)shift) : v;
   }
   __device__ __forceinline__ T after_x(int i, int j, int k) const {
@@ -160,7 +168,7 @@ template <typename T, int DIM>
 __global__ void __launch_bounds__(256) k_ghost_fill(Layout L, GhostBatch<T> G) {
   const int q = blockIdx.y;
   const long long total = G.n[q];
-  Resolve<T, DIM> R{G.f[q], L, G.bc[q], G.shift[q]};
+  Resolve<T, DIM> R{PtrSrc<T>{G.f[q]}, L, G.bc[q], G.shift[q]};
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
     ghost_target<DIM>(L, G.bc[q], t, i, j, k);

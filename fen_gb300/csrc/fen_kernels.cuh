@@ -2,6 +2,7 @@
 #pragma once
 #include "fen_fft.cuh"
 #include "fen_ghost.cuh"
+#include "fen_mixed.cuh"
 #include "fen_types.cuh"
 
 namespace fen {
@@ -25,7 +26,8 @@ struct PredArgs {
   int iso, has_S, rhof_one, use_dev_dt;
 };
 
-template <typename T, int DIM>
+// DELTA = true (mixed form) writes the increment dt*rhs instead of v + dt*rhs.
+template <typename T, int DIM, bool DELTA = false>
 __global__ void __launch_bounds__(256) k_predictor(Layout L, const StepScalars* __restrict__ sc, PredArgs<T> a) {
   const long long ncell = (long long)L.n0 * L.n1 * L.n2;
   const T A = (T)sc->A, B = (T)sc->B;
@@ -122,14 +124,14 @@ __global__ void __launch_bounds__(256) k_predictor(Layout L, const StepScalars* 
     const T gpy = (a.p[c + sy] - pc) * (a.iso ? idx : idy);
     T rx = (a.rhof_one ? -gpx : -gpx / rhof) + A * dvx + B * a.dox[c] + (T)a.g[0];
     T ry = (a.rhof_one ? -gpy : -gpy / rhof) + A * dvy + B * a.doy[c] + (T)a.g[1];
-    a.us[c] = uc + dt * rx;
-    a.vs[c] = vc + dt * ry;
+    a.us[c] = DELTA ? dt * rx : uc + dt * rx;
+    a.vs[c] = DELTA ? dt * ry : vc + dt * ry;
     a.dox[c] = dvx;
     a.doy[c] = dvy;
     if (DIM == 3) {
       const T gpz = (a.p[c + sz] - pc) * (a.iso ? idx : idz);
       T rz = (a.rhof_one ? -gpz : -gpz / rhof) + A * dvz + B * a.doz[c] + (T)a.g[2];
-      a.ws[c] = wc + dt * rz;
+      a.ws[c] = DELTA ? dt * rz : wc + dt * rz;
       a.doz[c] = dvz;
     }
   }
@@ -141,7 +143,7 @@ __global__ void __launch_bounds__(256) k_predictor(Layout L, const StepScalars* 
 //   CONTIG = false: lines along y or z (strided), a tile of consecutive columns per CTA.
 // ------------------------------------------------------------------------------------
 enum { OP_R2C = 0, OP_C2R, OP_C2C_F, OP_C2C_I, OP_C2C_SOLVE, OP_DCT2, OP_DCT3 };
-enum { LD_FIELD = 0, LD_DIV, LD_REAL, LD_CPLX };
+enum { LD_FIELD = 0, LD_DIV, LD_REAL, LD_CPLX, LD_DIVMIX };
 enum { ST_FIELD = 0, ST_REAL, ST_CPLX };
 
 template <typename T>
@@ -157,7 +159,9 @@ struct LineArgs {
   long long out_line, out_pos, out_outer;
   // fields (LD_FIELD / LD_DIV / ST_FIELD)
   Layout L;
-  const T *fu, *fv, *fw;  // predicted velocity for LD_DIV
+  const T *fu, *fv, *fw;  // predicted velocity for LD_DIV (the FP32 increment for LD_DIVMIX)
+  DFField pu, pv, pw;     // pair velocity of the mixed form (LD_DIVMIX)
+  F2 idp[3];              // 1/delta per axis as float pairs (LD_DIVMIX)
   const T* fsrc;          // LD_FIELD source
   T* fdst;                // ST_FIELD destination
   double* partial;        // ST_FIELD: per-CTA line sums (mean removal), may be null
@@ -167,6 +171,8 @@ struct LineArgs {
   int iso, dim;
   // OP_C2C_SOLVE eigenvalues: lam = lamA[col] + lamB[outer] + lamC[pos]
   const double* lamA; const double* lamB; const double* lamC;
+  // optional tabulated scale/lam for OP_C2C_SOLVE, [(outer * n + pos) * nlines + col]
+  const T* inv_lam;
   FFTPlan plan;
   AxisTw tw;
 };
@@ -224,11 +230,16 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
       if (CONTIG) { l = t / n; i = t % n; } else { l = t % nl; i = t / nl; }
       T x = 0;
       if (l < nlv) {
-        if (LD == LD_FIELD || LD == LD_DIV) {
+        if (LD == LD_FIELD || LD == LD_DIV || LD == LD_DIVMIX) {
           int j, k;
           row_jk<DIM>(line0 + l, outer, j, k);
           if (LD == LD_FIELD) x = a.fsrc[a.L.idx(i + 1, j, kst<DIM>(k))];
-          else x = div_at<T, DIM>(a, i + 1, j, k) * (T)a.sc->rho_over_dt;
+          else if (LD == LD_DIV) x = div_at<T, DIM>(a, i + 1, j, k) * (T)a.sc->rho_over_dt;
+          else {
+            const F2 dd = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
+                                      a.idp, i + 1, j, k);
+            x = (T)(dd.hi + dd.lo) * (T)a.sc->rho_over_dt;
+          }
         } else {
           x = inR[(long long)(line0 + l) * a.in_line + (long long)i * a.in_pos + (long long)outer * a.in_outer];
         }
@@ -289,12 +300,17 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     for (int t = tid; t < work; t += nth) {
       const int l = t % nl, p = t / nl;
       if (l < nlv) {
-        const double lam = a.lamA[line0 + l] + (a.lamB ? a.lamB[outer] : 0.0) + a.lamC[p];
         T2& z = res[(size_t)p * nl + l];
-        if (lam == 0.0) z = mk<T2>(0, 0);
-        else {
-          const T f = (T)(a.scale / lam);
+        if (a.inv_lam) {
+          const T f = a.inv_lam[((long long)outer * M + p) * a.nlines + line0 + l];
           z = mk<T2>(z.x * f, z.y * f);
+        } else {
+          const double lam = a.lamA[line0 + l] + (a.lamB ? a.lamB[outer] : 0.0) + a.lamC[p];
+          if (lam == 0.0) z = mk<T2>(0, 0);
+          else {
+            const T f = (T)(a.scale / lam);
+            z = mk<T2>(z.x * f, z.y * f);
+          }
         }
       }
     }
@@ -679,6 +695,22 @@ static __global__ void k_prologue(StepScalars* sc, int constant_cfl, double cfl,
   sc->B = -0.5 * dt / sc->dt_o;
   sc->rho_over_dt = density / dt;
   sc->dt_over_rhof = dt / rhof;
+}
+
+// Tabulated scale/lam of the all-periodic spectral divide with the SOLVE kernel's formula
+// (so FP64 results are bit-identical to computing it in place); zero mode -> 0.
+template <typename T>
+__global__ void k_inv_lam_table(int ncol, int n, int nouter, const double* lamA, const double* lamB, const double* lamC,
+                                double scale, T* out) {
+  const long long total = (long long)ncol * n * nouter;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int col = (int)(t % ncol);
+    const long long r = t / ncol;
+    const int p = (int)(r % n);
+    const int outer = (int)(r / n);
+    const double lam = lamA[col] + (lamB ? lamB[outer] : 0.0) + lamC[p];
+    out[t] = (lam == 0.0) ? T(0) : (T)(scale / lam);
+  }
 }
 
 // Host-layout <-> HBM-layout copies.  The host array is FEN's contiguous f(0:nx+1, 0:ny+1,

@@ -61,6 +61,7 @@ typedef struct {
   double cfl;
   int constant_cfl;
   int precision;        /* FEN_FP64 or FEN_MIXED */
+  int refine;           /* FEN_MIXED: iterative-refinement solves per step (0 or 1) */
 } fen_params;
 
 /* Per-step diagnostics (navier_stokes.f90:24-33, 570-619). */

@@ -1,0 +1,127 @@
+"""GPU tests of the mixed-precision form against the FP64 form and the oracle.
+
+The mixed form keeps the state as double-float pairs and runs stencils and transforms with
+FP32 instructions; the tridiagonal solves, mean removal and reductions stay FP64.  Its
+error against the FP64 path is stated here per field (relative L2, p mean-free).
+"""
+import numpy as np
+import pytest
+
+import fen_gb300 as F
+from oracle import oracle as O
+from tests import cases as C
+
+pytestmark = pytest.mark.gpu
+
+# FP32 transforms: a single Poisson solve agrees with FP64 to about 1e-6 relative L2.
+RTOL_POISSON = 1e-5
+
+
+def _solver(dim, n, L, bc, prec, **kw):
+    g = F.Grid(n[0], n[1], n[2] if dim == 3 else 1, L[0], L[1], L[2], bc=bc, dim=dim, aniso=kw.pop("aniso", False))
+    return F.Solver(g, precision=prec, **kw)
+
+
+@pytest.mark.parametrize("name", ["pp", "pn", "nn", "ppp", "ppn", "npn", "nnn", "pnp"])
+def test_mixed_poisson_vs_oracle(fen_lib, name):
+    dim, bc, _, _ = C.poisson_case(name)
+    n = {"pp": (32, 24, 1), "pn": (24, 32, 1), "nn": (32, 16, 1)}.get(name, (16, 24, 12))
+    o = O.Oracle(dim, n, (1.0, 1.0, 1.0), bc=bc)
+    s = _solver(dim, n, (1.0, 1.0, 1.0), bc, F.MIXED)
+    rng = np.random.Generator(np.random.PCG64(31))
+    rhs = C.random_interior(s.grid.shape, rng, dim)
+    r = C.interior(rhs, dim)
+    r -= r.mean()
+    o.field(O.PHI)[...] = rhs
+    o.solve_poisson()
+    got = C.interior(s.solve_poisson(rhs), dim)
+    want = C.interior(o.field(O.PHI), dim)
+    assert C.rel_l2(got, want) < RTOL_POISSON
+
+
+def _run_pair(dim, n, L, bc, init, nsteps, U=1.0, **kw):
+    out = []
+    for prec in (F.FP64, F.MIXED):
+        s = _solver(dim, n, L, bc, prec, **dict(kw))
+        for fid, a in init.items():
+            s.set_field(fid, a)
+            s.update_ghost_nodes(fid)
+        dt = s.set_timestep(U) if kw.get("constant_CFL") else None
+        if dt is None:
+            dt = 1e-3
+            s.set_dt_o(dt)
+        s.advance_n(nsteps, dt)
+        out.append(s)
+    return out
+
+
+def _errors(s64, s32, dim):
+    errs = {}
+    for fid in ([F.U, F.V, F.P] if dim == 2 else [F.U, F.V, F.W, F.P]):
+        a = C.interior(s32.get_field(fid), dim)
+        b = C.interior(s64.get_field(fid), dim)
+        if fid == F.P:
+            a, b = a - a.mean(), b - b.mean()
+        errs[fid] = C.rel_l2(a, b)
+    return errs
+
+
+def test_mixed_tgv3d_matches_fp64(fen_lib):
+    N, L = 32, 2 * np.pi
+    u, v, w, p = C.tgv3d_fields(N, L)
+    init = {F.U: u, F.V: v, F.W: w, F.P: p}
+    s64, s32 = _run_pair(3, (N, N, N), (L, L, L), ["Periodic"] * 6, init, 100, viscosity=1 / 1600, CFL=0.5,
+                         constant_CFL=True)
+    e = _errors(s64, s32, 3)
+    for fid in (F.U, F.V, F.W, F.P):
+        assert e[fid] < 1e-6, e
+    assert abs(s32.status()["maxdiv"]) < 1e-5
+
+
+def test_mixed_channel_matches_fp64(fen_lib):
+    n = (32, 16, 24)
+    L = (4 * np.pi, 2.0, 4 * np.pi / 3)
+    bc = ["Periodic", "Periodic", "Wall", "Wall", "Periodic", "Periodic"]
+    rng = np.random.Generator(np.random.PCG64(1234))
+    shape = (n[2] + 2, n[1] + 2, n[0] + 2)
+    dy = L[1] / n[1]
+    yc = -1.0 + (np.arange(n[1] + 2) - 0.5) * dy
+    init = {}
+    for fid in (F.U, F.V, F.W):
+        a = np.zeros(shape)
+        a[1:-1, 1:-1, 1:-1] = 0.05 * 90.0 * rng.uniform(-1, 1, size=(n[2], n[1], n[0]))
+        if fid == F.U:
+            a[1:-1, 1:-1, 1:-1] += ((1 - yc[1:-1] ** 2) * 90.0)[None, :, None]
+        init[fid] = a
+    s64, s32 = _run_pair(3, n, L, bc, init, 200, viscosity=1 / 180, g=(1.0, 0.0, 0.0), CFL=0.5, constant_CFL=True,
+                         aniso=True, U=90.0)
+    e = _errors(s64, s32, 3)
+    for fid in (F.U, F.V, F.W):
+        assert e[fid] < 1e-6, e
+    assert e[F.P] < 1e-5, e
+
+
+def test_mixed_ghost_pairs_keep_fp64_values(fen_lib):
+    # pairs carry ~48 bits: an FP64 upload, ghost fill and download round-trip to ~1e-14
+    n = (12, 8, 6)
+    bc = ["Periodic", "Periodic", "Wall", "Wall", "Periodic", "Periodic"]
+    s32 = _solver(3, n, (1.0, 1.0, 1.0), bc, F.MIXED)
+    s64 = _solver(3, n, (1.0, 1.0, 1.0), bc, F.FP64)
+    rng = np.random.Generator(np.random.PCG64(8))
+    for fid in (F.U, F.V, F.W, F.P):
+        a = rng.standard_normal(s32.grid.shape)
+        for s in (s32, s64):
+            s.set_field(fid, a)
+            s.update_ghost_nodes(fid)
+        got, want = s32.get_field(fid), s64.get_field(fid)
+        assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+
+
+def test_mixed_nan_reported(fen_lib):
+    s = _solver(2, (16, 16, 1), (1.0, 1.0, 1.0 / 16), ["Periodic"] * 4, F.MIXED)
+    a = s.zeros()
+    a[1, 3, 3] = np.nan
+    s.set_field(F.U, a)
+    s.set_dt_o(1e-3)
+    with pytest.raises(F.FenError, match="NaN"):
+        s.advance_solution(1, 1e-3)
