@@ -66,7 +66,8 @@ _EXPORTS = [
     "fen_update_ghost_nodes", "fen_set_bc_values", "fen_set_bc_type", "fen_set_timestep",
     "fen_set_dt_o", "fen_advance_solution", "fen_advance_n", "fen_get_status", "fen_solve_poisson",
     "fen_divergence", "fen_explicit_terms", "fen_sync", "fen_kernel_launches", "fen_time_steps",
-    "fen_profile_step",
+    "fen_profile_step", "fen_save_state", "fen_load_state", "fen_save_fields", "fen_adjoint_setup",
+    "fen_adjoint_forward", "fen_adjoint_backward",
 ]
 
 
@@ -101,6 +102,12 @@ def load_library(path=None):
     L.fen_kernel_launches.restype = ctypes.c_longlong
     L.fen_time_steps.argtypes = [vp, ip, ctypes.c_double, dp]
     L.fen_profile_step.argtypes = [vp, ip, ctypes.c_double, dp]
+    L.fen_save_state.argtypes = [vp, ctypes.c_char_p]
+    L.fen_load_state.argtypes = [vp, ctypes.c_char_p]
+    L.fen_save_fields.argtypes = [vp, ctypes.c_char_p, ip]
+    L.fen_adjoint_setup.argtypes = [vp, ip, ip]
+    L.fen_adjoint_forward.argtypes = [vp, ctypes.c_double]
+    L.fen_adjoint_backward.argtypes = [vp, dp, dp, dp, dp, dp]
     if path == LIB_PATH:
         _lib = L
     return L
@@ -264,6 +271,38 @@ class Solver:
         out = np.zeros(3 * g.Nx * g.Ny * g.Nz)
         self._check(self._L.fen_explicit_terms(self._h, _dp(out)))
         return out.reshape(3, g.Nz, g.Ny, g.Nx)[: g.dim]
+
+    # -- solver_mod checkpoint / snapshots (solver.f90:103-329) ---------------------------
+    def save_state(self, step, directory="data", path=None):
+        """save_state(step): data/state_<step:7>.raw in FEN's raw layout; returns the path."""
+        path = path or os.path.join(directory, "state_%07d.raw" % step)
+        self._check(self._L.fen_save_state(self._h, path.encode()))
+        return path
+
+    def load_state(self, step, directory="data", path=None):
+        path = path or os.path.join(directory, "state_%07d.raw" % step)
+        self._check(self._L.fen_load_state(self._h, path.encode()))
+        return path
+
+    def save_fields(self, step, directory="data"):
+        self._check(self._L.fen_save_fields(self._h, directory.encode(), int(step)))
+
+    # -- discrete adjoint (2D periodic FP64) ------------------------------------------------
+    def adjoint_setup(self, nsteps, every):
+        self._check(self._L.fen_adjoint_setup(self._h, int(nsteps), int(every)))
+
+    def adjoint_forward(self, dt):
+        """Run the configured rollout from the current state, keeping checkpoints."""
+        self._check(self._L.fen_adjoint_forward(self._h, float(dt)))
+
+    def adjoint_backward(self, lam_u, lam_v):
+        """Gradient w.r.t. the initial (u, v) of a loss with sensitivity (lam_u, lam_v) to
+        the final (u, v).  Returns (g_u, g_v, times_ms) with times = (backward, forward)."""
+        lu = np.ascontiguousarray(lam_u, dtype=np.float64)
+        lv = np.ascontiguousarray(lam_v, dtype=np.float64)
+        gu, gv, ms = self.zeros(), self.zeros(), np.zeros(2)
+        self._check(self._L.fen_adjoint_backward(self._h, _dp(lu), _dp(lv), _dp(gu), _dp(gv), _dp(ms)))
+        return gu, gv, ms
 
     # -- measurement -------------------------------------------------------------------------
     def kernel_launches(self):

@@ -17,12 +17,14 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cerrno>
 #include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "../../include/fen_gpu.h"
+#include "fen_adjoint.cuh"
 #include "fen_kernels.cuh"
 #include "fen_types.cuh"
 
@@ -140,6 +142,17 @@ struct fen_ctx {
   long long launches = 0;
   long long launches_per_step = 0;
   double* stage_scratch = nullptr;  // host-layout staging for upload/download (one field)
+  // discrete adjoint (2D periodic FP64): checkpoints, recomputed step inputs, adjoint fields
+  struct Adjoint {
+    int nsteps = 0, every = 0, nckpt = 0;
+    double dt = 0;
+    std::vector<double*> ckpt;    // nckpt+1 checkpoints x 5 fields (u, v, p, dv_o x, dv_o y)
+    std::vector<double*> inputs;  // every x 2 fields (u, v at the start of each step)
+    double *uh = nullptr, *vh = nullptr, *ph = nullptr, *dou = nullptr, *dov = nullptr;
+    double *fh = nullptr, *bh = nullptr, *ush = nullptr, *vsh = nullptr, *dhu = nullptr, *dhv = nullptr;
+    double fwd_ms = 0, bwd_ms = 0;
+    bool ready = false;
+  } adj;
 };
 
 namespace {
@@ -1015,6 +1028,11 @@ int fen_ctx_destroy(fen_ctx* c) {
   if (c->nan_flag) cudaFree(c->nan_flag);
   if (c->sc) cudaFree(c->sc);
   if (c->sc_host) cudaFreeHost(c->sc_host);
+  for (double* b : c->adj.ckpt) if (b) cudaFree(b);
+  for (double* b : c->adj.inputs) if (b) cudaFree(b);
+  double* ab[] = {c->adj.uh, c->adj.vh, c->adj.ph, c->adj.dou, c->adj.dov, c->adj.fh, c->adj.bh, c->adj.ush,
+                  c->adj.vsh, c->adj.dhu, c->adj.dhv};
+  for (double* b : ab) if (b) cudaFree(b);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return 0;
@@ -1345,6 +1363,294 @@ int fen_explicit_terms(fen_ctx* c, double* out) {
   CK(cudaStreamSynchronize(c->stream));
   for (int q = 0; q < c->dim; ++q) cudaFree(save[q]);
   cudaFree(dsc);
+  return 0;
+}
+
+// ---- checkpoint / restart (solver.f90:103-329) ----------------------------------------
+namespace {
+// Interior of one field (x fastest) through a ghosted host download.
+int interior_get(fen_ctx* c, int f, std::vector<double>& out) {
+  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
+  std::vector<double> h((size_t)nxg * nyg * host_planes(c));
+  int r;
+  if ((r = fen_download(c, f, h.data()))) return r;
+  const int K = (c->dim == 3) ? c->n[2] : 1;
+  out.resize((size_t)c->n[0] * c->n[1] * K);
+  size_t t = 0;
+  for (int k = 1; k <= K; ++k)
+    for (int j = 1; j <= c->n[1]; ++j)
+      for (int i = 1; i <= c->n[0]; ++i) out[t++] = h[(size_t)i + (size_t)nxg * ((size_t)j + (size_t)nyg * k)];
+  return 0;
+}
+
+int interior_set(fen_ctx* c, int f, const double* in) {
+  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
+  std::vector<double> h((size_t)nxg * nyg * host_planes(c), 0.0);
+  const int K = (c->dim == 3) ? c->n[2] : 1;
+  size_t t = 0;
+  for (int k = 1; k <= K; ++k)
+    for (int j = 1; j <= c->n[1]; ++j)
+      for (int i = 1; i <= c->n[0]; ++i) h[(size_t)i + (size_t)nxg * ((size_t)j + (size_t)nyg * k)] = in[t++];
+  return fen_upload(c, f, h.data());
+}
+
+// save_state / load_state field order (solver.f90:195-208, 277-292).
+std::vector<int> state_order(fen_ctx* c) {
+  std::vector<int> o = {FEN_P, FEN_U, FEN_V, FEN_DVO_X, FEN_DVO_Y};
+  if (c->dim == 3) { o.push_back(FEN_W); o.push_back(FEN_DVO_Z); }
+  return o;
+}
+}  // namespace
+
+int fen_save_state(fen_ctx* c, const char* path) {
+  if (!c || !path) return fail(FEN_ERR_ARG, "null argument");
+  FILE* fp = fopen(path, "wb");
+  if (!fp) return fail(FEN_ERR_ARG, std::string("cannot open ") + path + ": " + strerror(errno));
+  std::vector<double> buf;
+  for (int f : state_order(c)) {
+    int r;
+    if ((r = interior_get(c, f, buf))) { fclose(fp); return r; }
+    if (fwrite(buf.data(), sizeof(double), buf.size(), fp) != buf.size()) { fclose(fp); return fail(FEN_ERR_ARG, "short write"); }
+  }
+  fclose(fp);
+  return 0;
+}
+
+int fen_load_state(fen_ctx* c, const char* path) {
+  if (!c || !path) return fail(FEN_ERR_ARG, "null argument");
+  FILE* fp = fopen(path, "rb");
+  if (!fp) return fail(FEN_ERR_ARG, std::string("cannot open ") + path + ": " + strerror(errno));
+  const size_t cnt = (size_t)c->n[0] * c->n[1] * ((c->dim == 3) ? c->n[2] : 1);
+  std::vector<double> buf(cnt);
+  for (int f : state_order(c)) {
+    if (fread(buf.data(), sizeof(double), cnt, fp) != cnt) { fclose(fp); return fail(FEN_ERR_ARG, "state file too short"); }
+    int r;
+    if ((r = interior_set(c, f, buf.data()))) { fclose(fp); return r; }
+  }
+  fclose(fp);
+  // ghost nodes of p and v (solver.f90:293-294)
+  int r;
+  if ((r = fen_update_ghost_nodes(c, FEN_P)) || (r = fen_update_ghost_nodes(c, FEN_U)) ||
+      (r = fen_update_ghost_nodes(c, FEN_V)))
+    return r;
+  if (c->dim == 3 && (r = fen_update_ghost_nodes(c, FEN_W))) return r;
+  return 0;
+}
+
+int fen_save_fields(fen_ctx* c, const char* dir, int step) {
+  if (!c || !dir) return fail(FEN_ERR_ARG, "null argument");
+  char sn[16];
+  snprintf(sn, sizeof(sn), "%07d", step);
+  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
+  const int K = (c->dim == 3) ? c->n[2] : 1;
+  std::vector<double> h((size_t)nxg * nyg * host_planes(c)), out((size_t)c->n[0] * c->n[1] * K);
+  const char* names[4] = {"vx_", "vy_", "vz_", "p_"};
+  const int fids[4] = {FEN_U, FEN_V, FEN_W, FEN_P};
+  const long long so[3] = {1, nxg, (long long)nxg * nyg};
+  for (int q = 0; q < 4; ++q) {
+    if (q == 2 && c->dim == 2) continue;
+    int r;
+    if ((r = fen_download(c, fids[q], h.data()))) return r;
+    size_t t = 0;
+    for (int k = 1; k <= K; ++k)
+      for (int j = 1; j <= c->n[1]; ++j)
+        for (int i = 1; i <= c->n[0]; ++i) {
+          const size_t ci = (size_t)i + (size_t)nxg * ((size_t)j + (size_t)nyg * k);
+          // face_to_center (fields.f90:210-252) for the velocity components
+          out[t++] = (q < 3) ? 0.5 * (h[ci] + h[ci - so[q]]) : h[ci];
+        }
+    const std::string path = std::string(dir) + "/" + names[q] + sn + ".raw";
+    FILE* fp = fopen(path.c_str(), "wb");
+    if (!fp) return fail(FEN_ERR_ARG, "cannot open " + path);
+    const size_t wr = fwrite(out.data(), sizeof(double), out.size(), fp);
+    fclose(fp);
+    if (wr != out.size()) return fail(FEN_ERR_ARG, "short write");
+  }
+  return 0;
+}
+
+// ---- discrete adjoint (fen_adjoint.cuh) ------------------------------------------------
+namespace {
+int adj_copy(fen_ctx* c, double* dst, const double* src) {
+  CK(cudaMemcpyAsync(dst, src, c->L.total * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  return 0;
+}
+
+int adj_save(fen_ctx* c, int q) {
+  double* src[5] = {c->u, c->v, c->p, c->dvo[0], c->dvo[1]};
+  for (int f = 0; f < 5; ++f) {
+    int r;
+    if ((r = adj_copy(c, c->adj.ckpt[5 * q + f], src[f]))) return r;
+  }
+  return 0;
+}
+
+int adj_restore(fen_ctx* c, int q) {
+  double* dst[5] = {c->u, c->v, c->p, c->dvo[0], c->dvo[1]};
+  for (int f = 0; f < 5; ++f) {
+    int r;
+    if ((r = adj_copy(c, dst[f], c->adj.ckpt[5 * q + f]))) return r;
+  }
+  return 0;
+}
+
+// Periodic ghost fill of adjoint fields (copies, so the stencils gather wrapped values).
+int adj_ghost(fen_ctx* c, double* a, double* b) {
+  double* f[2] = {a, b};
+  int ids[2] = {FEN_U, FEN_V};
+  return b ? ghost<double>(c, 2, f, ids) : ghost<double>(c, 1, f, ids + 0);
+}
+
+// One adjoint step with the stored forward input (u, v) of that step.
+int adj_step(fen_ctx* c, const double* u, const double* v) {
+  auto& A = c->adj;
+  int r;
+  const int grid = std::min(cdiv((long long)c->n[0] * c->n[1], 256), 152 * 16);
+  const double idx = 1.0 / c->d[0], idy = 1.0 / c->d[1];
+  const double rhof = rhof_of(c), rho = c->prm.density, dt = A.dt;
+  const double Acoef = 1.0 + 0.5 * dt / c->sc_host->dt_o, Bcoef = -0.5 * dt / c->sc_host->dt_o;
+  // phi^ = p'^ + dt/rhof D v'^
+  if ((r = adj_ghost(c, A.uh, A.vh))) return r;
+  k_adj_div2<<<grid, 256, 0, c->stream>>>(c->L, A.ph, A.uh, A.vh, dt / rhof, idx, idy, A.fh);
+  c->launches++;
+  // b^ = P phi^ (the forward's Poisson plan, loaded from phi^, written to b^)
+  for (size_t q = 0; q < c->stages.size(); ++q)
+    if ((r = launch_stage(c, c->stages[q], q == 0, A.fh, A.bh))) return r;
+  if (c->needs_mean) {
+    const int g2 = std::min(cdiv((long long)c->n[0] * c->n[1], 256), 152 * 8);
+    k_mean_subtract<double, 2><<<g2, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, A.bh);
+    c->launches++;
+  }
+  {
+    double* f[1] = {A.bh};
+    int ids[1] = {FEN_PHI};
+    if ((r = ghost<double>(c, 1, f, ids))) return r;
+  }
+  // v*^ = v'^ - rho/dt G b^
+  k_adj_grad2<<<grid, 256, 0, c->stream>>>(c->L, A.uh, A.vh, A.bh, rho / dt, idx, idy, A.ush, A.vsh);
+  c->launches++;
+  // p^ = p'^ + dt/rhof D v*^
+  if ((r = adj_ghost(c, A.ush, A.vsh))) return r;
+  k_adj_div2<<<grid, 256, 0, c->stream>>>(c->L, A.ph, A.ush, A.vsh, dt / rhof, idx, idy, A.ph);
+  c->launches++;
+  // dv^ = dv_o'^ + dt A v*^, dv_o^ = dt B v*^
+  k_adj_dv2<<<grid, 256, 0, c->stream>>>(c->L, A.ush, A.vsh, A.dou, A.dov, dt * Acoef, dt * Bcoef, A.dhu, A.dhv);
+  c->launches++;
+  // v^ = v*^ + N'^T dv^ + mu/rhof L dv^
+  if ((r = adj_ghost(c, A.dhu, A.dhv))) return r;
+  k_adj_state2<<<grid, 256, 0, c->stream>>>(c->L, u, v, A.ush, A.vsh, A.dhu, A.dhv, idx, idy, idx * idx, idy * idy,
+                                           c->prm.viscosity / rhof, A.uh, A.vh);
+  c->launches++;
+  CK(cudaGetLastError());
+  return 0;
+}
+}  // namespace
+
+int fen_adjoint_setup(fen_ctx* c, int nsteps, int every) {
+  if (!c || nsteps < 1 || every < 1) return fail(FEN_ERR_ARG, "bad argument");
+  if (c->dim != 2 || c->mixed || c->solver != S_PP || c->prm.constant_cfl || c->has_S)
+    return fail(FEN_ERR_ARG, "the adjoint covers 2D periodic FP64 runs with fixed dt and no source field");
+  auto& A = c->adj;
+  for (double* b : A.ckpt) if (b) cudaFree(b);
+  for (double* b : A.inputs) if (b) cudaFree(b);
+  A.ckpt.clear();
+  A.inputs.clear();
+  A.nsteps = nsteps;
+  A.every = std::min(every, nsteps);
+  A.nckpt = (nsteps + A.every - 1) / A.every;
+  int r;
+  A.ckpt.assign(5 * (A.nckpt + 1), nullptr);
+  for (auto& b : A.ckpt) if ((r = alloc(&b, c->L.total))) return r;
+  A.inputs.assign(2 * A.every, nullptr);
+  for (auto& b : A.inputs) if ((r = alloc(&b, c->L.total))) return r;
+  double** ab[] = {&A.uh, &A.vh, &A.ph, &A.dou, &A.dov, &A.fh, &A.bh, &A.ush, &A.vsh, &A.dhu, &A.dhv};
+  for (double** b : ab)
+    if (!*b && (r = alloc(b, c->L.total))) return r;
+  A.ready = false;
+  return 0;
+}
+
+int fen_adjoint_forward(fen_ctx* c, double dt) {
+  if (!c || c->adj.nsteps < 1) return fail(FEN_ERR_STATE, "fen_adjoint_setup first");
+  auto& A = c->adj;
+  // the adjoint applies one (A, B) pair to every step, which holds when dt_o == dt
+  if (!(dt > 0.0) || c->sc_host->dt_o != dt) return fail(FEN_ERR_ARG, "the adjoint rollout needs dt_o == dt (fen_set_dt_o)");
+  int r;
+  if ((r = pre_step(c, dt))) return r;
+  if ((r = capture_graph(c))) return r;
+  A.dt = dt;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, c->stream));
+  for (int s = 0; s < A.nsteps; ++s) {
+    if (s % A.every == 0 && (r = adj_save(c, s / A.every))) return r;
+    CK(cudaGraphLaunch(c->graph, c->stream));
+  }
+  c->launches += c->launches_per_step * A.nsteps;
+  if ((r = adj_save(c, A.nckpt))) return r;  // final state, restored after the backward sweep
+  CK(cudaEventRecord(e1, c->stream));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  A.fwd_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if ((r = read_back(c))) return r;
+  if (c->sc_host->err) return fail(FEN_ERR_NAN, "NaN in the velocity field");
+  A.ready = true;
+  return 0;
+}
+
+int fen_adjoint_backward(fen_ctx* c, const double* lam_u, const double* lam_v, double* g_u, double* g_v, double* ms) {
+  if (!c || !lam_u || !lam_v || !g_u || !g_v) return fail(FEN_ERR_ARG, "null argument");
+  auto& A = c->adj;
+  if (!A.ready) return fail(FEN_ERR_STATE, "fen_adjoint_forward first");
+  int r;
+  // adjoint of the final state: (lam_u, lam_v), p^ = 0, dv_o^ = 0
+  if ((r = relayout<double>(c, A.uh, const_cast<double*>(lam_u), 0)) || (r = relayout<double>(c, A.vh, const_cast<double*>(lam_v), 0)))
+    return r;
+  CK(cudaMemsetAsync(A.ph, 0, c->L.total * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(A.dou, 0, c->L.total * sizeof(double), c->stream));
+  CK(cudaMemsetAsync(A.dov, 0, c->L.total * sizeof(double), c->stream));
+  // ghost entries of the seed carry no sensitivity: the first adjoint step overwrites them
+  // with periodic copies of the interior
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, c->stream));
+  for (int seg = A.nckpt - 1; seg >= 0; --seg) {
+    const int s0 = seg * A.every, s1 = std::min(A.nsteps, s0 + A.every);
+    if ((r = adj_restore(c, seg))) return r;
+    for (int s = s0; s < s1; ++s) {
+      if ((r = adj_copy(c, A.inputs[2 * (s - s0)], c->u)) || (r = adj_copy(c, A.inputs[2 * (s - s0) + 1], c->v))) return r;
+      CK(cudaGraphLaunch(c->graph, c->stream));
+    }
+    c->launches += c->launches_per_step * (s1 - s0);
+    for (int s = s1 - 1; s >= s0; --s)
+      if ((r = adj_step(c, A.inputs[2 * (s - s0)], A.inputs[2 * (s - s0) + 1]))) return r;
+  }
+  CK(cudaEventRecord(e1, c->stream));
+  CK(cudaEventSynchronize(e1));
+  float f = 0;
+  CK(cudaEventElapsedTime(&f, e0, e1));
+  A.bwd_ms = f;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if ((r = adj_restore(c, A.nckpt))) return r;
+  // gradient: interior of v^ at step 0 (ghost entries zero)
+  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
+  if ((r = relayout<double>(c, A.uh, g_u, 1)) || (r = relayout<double>(c, A.vh, g_v, 1))) return r;
+  for (double* g : {g_u, g_v}) {
+    double* h = g + (size_t)nxg * nyg;  // plane k = 1
+    for (int j = 0; j < nyg; ++j)
+      for (int i = 0; i < nxg; ++i)
+        if (i == 0 || j == 0 || i == nxg - 1 || j == nyg - 1) h[i + (size_t)nxg * j] = 0.0;
+  }
+  if (ms) {
+    ms[0] = A.bwd_ms;
+    ms[1] = A.fwd_ms;
+  }
   return 0;
 }
 

@@ -111,6 +111,27 @@ int fen_divergence(fen_ctx* ctx, double* out);
  * three components go to out (3 * nx*ny*nz, x fastest). */
 int fen_explicit_terms(fen_ctx* ctx, double* out);
 
+/* save_state / load_state (src/solver.f90:160-329): raw FP64 global interiors, x fastest,
+ * no header, in the order p, u, v, dv_o%x, dv_o%y[, w, dv_o%z]; load_state refreshes the
+ * ghost nodes of p and v.  FEN names the file data/state_<step:7>.raw. */
+int fen_save_state(fen_ctx* ctx, const char* path);
+int fen_load_state(fen_ctx* ctx, const char* path);
+/* save_fields (src/solver.f90:103-156): <dir>/vx_<step:7>.raw, vy_, [vz_], p_ with the
+ * velocity interpolated to cell centres (face_to_center, src/fields.f90:210-252). */
+int fen_save_fields(fen_ctx* ctx, const char* dir, int step);
+
+/* Discrete adjoint of the step (no counterpart in FEN, which has no differentiation): 2D
+ * periodic FP64 contexts with fixed dt.  fen_adjoint_setup sizes an nsteps rollout with a
+ * checkpoint every `every` steps; fen_adjoint_forward runs the rollout from the current
+ * state (which ends at step nsteps); fen_adjoint_backward takes the sensitivity of a scalar
+ * loss to the final (u, v) and returns its gradient with respect to the initial (u, v),
+ * recomputing each checkpoint segment.  Arrays use the host field layout; ghost entries of
+ * the gradient are zero.  ms (optional, 2 doubles): backward and forward device times. */
+int fen_adjoint_setup(fen_ctx* ctx, int nsteps, int every);
+int fen_adjoint_forward(fen_ctx* ctx, double dt);
+int fen_adjoint_backward(fen_ctx* ctx, const double* lam_u, const double* lam_v, double* g_u, double* g_v,
+                         double* ms);
+
 /* Synchronise the context stream. */
 int fen_sync(fen_ctx* ctx);
 /* Number of kernels this library launched on the context since creation. */

@@ -1,0 +1,68 @@
+"""Checkpoint/restart through the C ABI (FEN test/small_test/io: test_NS.f90 + run.sh).
+
+The reference runs 10 steps saving at step 5, restarts from step 5, runs to 10 and requires
+the two state files to be identical (`diff`, io/run.sh:7-11).  Same here, in both forms.
+"""
+import numpy as np
+import pytest
+
+import fen_gb300 as F
+from tests import cases as C
+
+pytestmark = pytest.mark.gpu
+
+
+def _init(s, N, L):
+    d = L / N
+    g = C.mac_grids(3, (N, N, N), (d, d, d))
+    X, Y, _ = g["u"]
+    s.set_field(F.U, -np.cos(X) * np.sin(Y))
+    X, Y, _ = g["v"]
+    s.set_field(F.V, np.sin(X) * np.cos(Y))
+    X, _, Z = g["w"]
+    s.set_field(F.W, np.sin(X) * np.cos(Z))
+    X, Y, _ = g["p"]
+    s.set_field(F.P, -0.25 * (np.cos(2 * X) + np.cos(2 * Y)))
+    for fid in (F.U, F.V, F.W, F.P):
+        s.update_ghost_nodes(fid)
+
+
+@pytest.mark.parametrize("prec", [F.FP64, F.MIXED])
+def test_restart_is_bitwise(fen_lib, tmp_path, prec):
+    N, L = 16, 2 * np.pi
+    g = F.Grid(N, N, N, L, L, L)
+    s = F.Solver(g, precision=prec)
+    _init(s, N, L)
+    dt = s.set_timestep(2.0)
+    for step in range(1, 11):
+        dt = s.advance_solution(step, dt)
+        if step == 5:
+            s.save_state(step, str(tmp_path))
+    full = s.save_state(10, str(tmp_path))
+    r = F.Solver(g, precision=prec)
+    _init(r, N, L)
+    dt = r.set_timestep(2.0)
+    r.load_state(5, str(tmp_path))
+    for step in range(6, 11):
+        dt = r.advance_solution(step, dt)
+    again = r.save_state(20, str(tmp_path))
+    a = np.fromfile(full)
+    b = np.fromfile(again)
+    assert a.size == 7 * N ** 3
+    assert np.array_equal(a, b)
+
+
+def test_save_fields_layout(fen_lib, tmp_path):
+    N, L = 8, 2 * np.pi
+    g = F.Grid(N, N, 1, L, L, L / N)
+    s = F.Solver(g)
+    u, v, p = C.tgv2d_fields(N, L)
+    for fid, a in ((F.U, u), (F.V, v), (F.P, p)):
+        s.set_field(fid, a)
+        s.update_ghost_nodes(fid)
+    s.save_fields(3, str(tmp_path))
+    ufull = s.get_field(F.U)[1]
+    vx = np.fromfile(tmp_path / "vx_0000003.raw").reshape(N, N)
+    assert np.allclose(vx, 0.5 * (ufull[1:-1, 1:-1] + ufull[1:-1, :-2]), rtol=0, atol=1e-15)
+    pr = np.fromfile(tmp_path / "p_0000003.raw").reshape(N, N)
+    assert np.array_equal(pr, s.get_field(F.P)[1, 1:-1, 1:-1])
