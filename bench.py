@@ -17,6 +17,11 @@ Multi-GPU: the path does not shard (one grid per device); N ranks run N independ
 replicas (weak scaling) and `value` sums their cells over the slowest rank's time.
 `--impl reference` times the CPU restatement of the reference (the oracle port; the
 Fortran/MPI/FFTW reference cannot be built on these machines) on rank 0's host cores.
+
+At N=1 the line also carries `forms`: the mixed-precision form against the FP64 path on the
+channel workload (throughput of each and the mixed form's relative L2 error after the same
+steps), and the discrete adjoint on 2D decaying turbulence (backward/forward time ratio and
+the gradient's agreement with central differences).  `--no-forms` skips them.
 """
 import argparse
 import json
@@ -200,6 +205,102 @@ def cpu_baseline(name, cfg, max_seconds=20.0):
             "sample": f"{steps} steps of {name} at {n[0]}x{n[1]}x{n[2]} ({el:.1f} s), CPU restatement (not FFTW)"}
 
 
+def form_mixed(F, steps):
+    """Channel flow (512x256x384, Re_tau = 180, CFL = 0.5): the mixed form against the FP64
+    path over the same `steps` steps from the same initial field.  Returns both throughputs
+    and the mixed form's relative L2 error per field (p mean-free)."""
+    cfg = CONFIGS["channel"]
+    n, L = cfg["n"], cfg["L"]
+    cells = n[0] * n[1] * n[2]
+    out, ref = {}, {}
+    for prec, name in ((F.FP64, "fp64"), (F.MIXED, "mixed")):
+        g = F.Grid(n[0], n[1], n[2], L[0], L[1], L[2], bc=cfg["bc"], aniso=True)
+        s = F.Solver(g, viscosity=cfg["nu"], g=cfg["g"], CFL=cfg["cfl"], constant_CFL=True, precision=prec)
+        fields = init_fields("channel", cfg, n, g.shape)
+        for k, fid in (("u", F.U), ("v", F.V), ("w", F.W), ("p", F.P)):
+            s.set_field(fid, fields[k])
+            s.update_ghost_nodes(fid)
+        dt = s.set_timestep(start_velocity("channel", cfg))
+        ms = s.time_steps(steps, dt)
+        out[name] = round(cells * steps / (ms / 1e3) / 1e6, 3)
+        res = {k: s.get_field(fid)[1:-1, 1:-1, 1:-1] for k, fid in (("u", F.U), ("v", F.V), ("w", F.W), ("p", F.P))}
+        if name == "fp64":
+            ref = res
+        else:
+            err = {}
+            for k in "uvwp":
+                a, b = res[k], ref[k]
+                if k == "p":
+                    a, b = a - a.mean(), b - b.mean()
+                err[k] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+            out["rel_l2_vs_fp64"] = err
+        s.destroy_solver()
+        del s
+    out["speedup"] = round(out["mixed"] / out["fp64"], 3)
+    out["unit"] = "Mcell-steps/s"
+    out["workload"] = f"channel 512x256x384, {steps} steps from Poiseuille + 5% noise, CFL 0.5"
+    return out
+
+
+def form_adjoint(F, ndir=16, nsteps=500, every=50):
+    """Adjoint of a 2D decaying-turbulence rollout (256^2 periodic, nu = 2e-3, dt = 2e-3 =
+    dt_o, 500 steps, checkpoints every 50): backward/forward time ratio and the agreement
+    of the gradient with central differences along `ndir` seeded unit directions,
+    eps = 1e-6 |u0|."""
+    from tests import cases as C
+
+    n, L, nu, dt = 256, 2 * np.pi, 2e-3, 2e-3
+    u0, v0 = C.decaying_turbulence_2d(n, L, 1)
+    tu, tv = C.decaying_turbulence_2d(n, L, 2)
+    g = F.Grid(n, n, 1, L, L, L / n)
+
+    def load(s, u, v):
+        for fid, a in ((F.U, u), (F.V, v), (F.P, None), (F.DVO_X, None), (F.DVO_Y, None)):
+            f = s.zeros()
+            if a is not None:
+                f[1, 1:-1, 1:-1] = a
+            s.set_field(fid, f)
+            if fid in (F.U, F.V, F.P):
+                s.update_ghost_nodes(fid)
+        s.set_dt_o(dt)
+
+    def loss(s):
+        uT, vT = s.get_field(F.U)[1, 1:-1, 1:-1], s.get_field(F.V)[1, 1:-1, 1:-1]
+        return 0.5 * (np.sum((uT - tu) ** 2) + np.sum((vT - tv) ** 2)), uT, vT
+
+    s = F.Solver(g, viscosity=nu)
+    s.adjoint_setup(nsteps, every)
+    ratios = []
+    for _ in range(3):
+        load(s, u0, v0)
+        s.adjoint_forward(dt)
+        J, uT, vT = loss(s)
+        lu, lv = s.zeros(), s.zeros()
+        lu[1, 1:-1, 1:-1], lv[1, 1:-1, 1:-1] = uT - tu, vT - tv
+        gu, gv, ms = s.adjoint_backward(lu, lv)
+        ratios.append(ms[0] / ms[1])
+    gu, gv = gu[1, 1:-1, 1:-1], gv[1, 1:-1, 1:-1]
+    f = F.Solver(g, viscosity=nu)
+    rng = np.random.Generator(np.random.PCG64(3))
+    eps = 1e-6 * np.sqrt(np.sum(u0 ** 2) + np.sum(v0 ** 2))
+    worst = 0.0
+    for _ in range(ndir):
+        du, dv = rng.standard_normal((n, n)), rng.standard_normal((n, n))
+        nrm = np.sqrt(np.sum(du ** 2) + np.sum(dv ** 2))
+        du, dv = du / nrm, dv / nrm
+        Jpm = []
+        for sgn in (1.0, -1.0):
+            load(f, u0 + sgn * eps * du, v0 + sgn * eps * dv)
+            f.advance_n(nsteps, dt)
+            Jpm.append(loss(f)[0])
+        fd = (Jpm[0] - Jpm[1]) / (2 * eps)
+        ad = float(np.sum(gu * du) + np.sum(gv * dv))
+        worst = max(worst, abs(fd - ad) / abs(ad))
+    return {"ratio_backward_over_forward": round(statistics.median(ratios), 3), "forward_ms": round(ms[1], 3),
+            "backward_ms": round(ms[0], 3), "fd_directions": ndir, "fd_max_rel_err": worst,
+            "workload": "2D decaying turbulence 256^2, nu=2e-3, dt=2e-3, 500 steps, checkpoints every 50, FP64"}
+
+
 def run_reference(args, name, cfg):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -235,6 +336,8 @@ def main():
     ap.add_argument("--config", default="tgv3d", choices=list(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=0, help="cubic/square override of the grid (profiling runs)")
+    ap.add_argument("--no-forms", action="store_true", help="skip the mixed-precision and adjoint measurements")
+    ap.add_argument("--form-steps", type=int, default=500, help="channel steps of the mixed-vs-FP64 comparison")
     args = ap.parse_args()
     cfg_name = args.config
     cfg = dict(CONFIGS[cfg_name])
@@ -352,6 +455,9 @@ def main():
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "clocks": clk.summary()}
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(cfg_name, cfg)
+        if world == 1 and not args.no_forms:
+            s.destroy_solver()
+            line["forms"] = {"mixed": form_mixed(F, args.form_steps), "adjoint": form_adjoint(F)}
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

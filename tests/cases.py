@@ -114,3 +114,40 @@ def poisson_rhs_grid(dim, N):
 
 def convergence_slope(Ns, errs):
     return -np.polyfit(np.log(np.asarray(Ns, float)), np.log(np.asarray(errs)), 1)[0]
+
+
+def decaying_turbulence_2d(n, L, seed, kpeak=8.0):
+    """Seeded 2D periodic velocity (u, v) interiors of shape (n, n) (axis 1 = x) with energy
+    spectrum E(k) ~ k^4 exp(-(k/kpeak)^2), unit kinetic energy 1/2 <u^2 + v^2> = 1, and zero
+    discrete divergence.
+
+    A Gaussian streamfunction psi at the cell corners (i delta, j delta) with |psi_k|^2 ~
+    k exp(-(k/kpeak)^2) gives E(k) ~ k |u_k|^2 ~ k^3 |psi_k|^2; u = (psi(i,j) - psi(i,j-1))/delta
+    and v = -(psi(i,j) - psi(i-1,j))/delta on the MAC faces are then divergence-free to
+    rounding, and the discrete projection below removes what rounding leaves."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    d = L / n
+    k = np.fft.fftfreq(n, 1.0 / n)
+    kk = np.sqrt(k[None, :] ** 2 + k[:, None] ** 2)
+    amp = np.sqrt(kk * np.exp(-((kk / kpeak) ** 2)))
+    amp[0, 0] = 0.0
+    spec = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * amp
+    psi = np.fft.ifft2(spec).real
+    u = (psi - np.roll(psi, 1, axis=0)) / d
+    v = -(psi - np.roll(psi, 1, axis=1)) / d
+    s = 1.0 / np.sqrt(0.5 * np.mean(u ** 2 + v ** 2))
+    return project_pp_2d(u * s, v * s, d)
+
+
+def project_pp_2d(u, v, d):
+    """Discrete projection of a periodic MAC velocity: v - G P D v with the 5-point
+    Laplacian's modified wavenumbers (the pp solver's operator)."""
+    n1, n0 = u.shape
+    div = ((u - np.roll(u, 1, axis=1)) + (v - np.roll(v, 1, axis=0))) / d
+    kx = 2.0 * (np.cos(2.0 * np.pi * np.arange(n0) / n0) - 1.0) / d ** 2
+    ky = 2.0 * (np.cos(2.0 * np.pi * np.arange(n1) / n1) - 1.0) / d ** 2
+    lam = kx[None, :] + ky[:, None]
+    dh = np.fft.fft2(div)
+    ph = np.where(lam == 0.0, 0.0, dh / np.where(lam == 0.0, 1.0, lam))
+    phi = np.fft.ifft2(ph).real
+    return u - (np.roll(phi, -1, axis=1) - phi) / d, v - (np.roll(phi, -1, axis=0) - phi) / d

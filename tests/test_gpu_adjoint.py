@@ -168,3 +168,13 @@ def test_adjoint_rejects_unsupported_contexts(fen_lib):
     s2.set_dt_o(1e-3)
     with pytest.raises(F.FenError, match="dt_o"):
         s2.adjoint_forward(2e-3)
+
+
+def test_decaying_turbulence_gradient_16_directions(fen_lib):
+    # 256^2, nu = 2e-3, dt = 2e-3, 500 steps, checkpoints every 50; central differences with
+    # eps = 1e-6 |u0| along 16 seeded unit directions agree with the adjoint to 1e-6
+    import bench
+
+    out = bench.form_adjoint(F)
+    assert out["fd_max_rel_err"] <= 1e-6, out
+    assert out["ratio_backward_over_forward"] <= 3.0, out
