@@ -22,7 +22,7 @@ import os
 
 import numpy as np
 
-__all__ = ["Grid", "Solver", "FenError", "PERIODIC", "WALL", "INFLOW", "OUTFLOW", "load_library"]
+__all__ = ["Grid", "Solver", "Ensemble", "FenError", "PERIODIC", "WALL", "INFLOW", "OUTFLOW", "load_library"]
 
 PERIODIC, WALL, INFLOW, OUTFLOW = 0, 1, 2, 3
 BC_NAMES = {"Periodic": PERIODIC, "Wall": WALL, "Inflow": INFLOW, "Outflow": OUTFLOW}
@@ -67,7 +67,10 @@ _EXPORTS = [
     "fen_set_dt_o", "fen_advance_solution", "fen_advance_n", "fen_get_status", "fen_solve_poisson",
     "fen_divergence", "fen_explicit_terms", "fen_sync", "fen_kernel_launches", "fen_time_steps",
     "fen_profile_step", "fen_save_state", "fen_load_state", "fen_save_fields", "fen_adjoint_setup",
-    "fen_adjoint_forward", "fen_adjoint_backward",
+    "fen_adjoint_forward", "fen_adjoint_backward", "fen_ensemble_create", "fen_ensemble_destroy",
+    "fen_ensemble_upload", "fen_ensemble_download", "fen_ensemble_set_timestep", "fen_ensemble_advance",
+    "fen_ensemble_status", "fen_ensemble_config", "fen_ensemble_set_config", "fen_ensemble_tune",
+    "fen_ensemble_launches", "fen_ensemble_smem_bytes",
 ]
 
 
@@ -108,6 +111,22 @@ def load_library(path=None):
     L.fen_adjoint_setup.argtypes = [vp, ip, ip]
     L.fen_adjoint_forward.argtypes = [vp, ctypes.c_double]
     L.fen_adjoint_backward.argtypes = [vp, dp, dp, dp, dp, dp]
+    cip = ctypes.POINTER(ctypes.c_int)
+    L.fen_ensemble_create.argtypes = [ctypes.c_int, cip, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_int, ctypes.POINTER(vp)]
+    L.fen_ensemble_destroy.argtypes = [vp]
+    L.fen_ensemble_upload.argtypes = [vp, ctypes.c_int, dp, dp, dp]
+    L.fen_ensemble_download.argtypes = [vp, ctypes.c_int, dp, dp, dp]
+    L.fen_ensemble_set_timestep.argtypes = [vp, ctypes.c_double]
+    L.fen_ensemble_advance.argtypes = [vp, ctypes.c_int, dp]
+    L.fen_ensemble_status.argtypes = [vp, ctypes.c_int, dp]
+    L.fen_ensemble_config.argtypes = [vp, cip, cip, cip, cip, cip]
+    L.fen_ensemble_set_config.argtypes = [vp, ctypes.c_int, cip]
+    L.fen_ensemble_tune.argtypes = [vp, ctypes.c_int, ctypes.c_char_p]
+    L.fen_ensemble_launches.argtypes = [vp]
+    L.fen_ensemble_launches.restype = ctypes.c_longlong
+    L.fen_ensemble_smem_bytes.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.fen_ensemble_smem_bytes.restype = ctypes.c_size_t
     if path == LIB_PATH:
         _lib = L
     return L
@@ -320,3 +339,106 @@ class Solver:
 
     def sync(self):
         self._check(self._L.fen_sync(self._h))
+
+
+class Ensemble:
+    """Batched ensemble of independent 2D periodic runs advanced by one persistent launch.
+
+    No counterpart in FEN, which runs one grid per program; each run follows FEN's 2D
+    periodic projection step (navier_stokes_solver, navier_stokes.f90:50-136, pp Poisson
+    solver) with density 1, constant-CFL time stepping and the forcing
+    S_x = forcing[0] sin(forcing[1] y).  Fields are FP32 on the device, reductions FP64.
+    Arrays exchanged with the host are interiors of shape (N, N), axis 1 = x.
+    """
+
+    def __init__(self, n, viscosity, length=2 * np.pi, CFL=0.4, forcing=(1.0, 4), lib=None):
+        self._L = lib or load_library()
+        n = np.ascontiguousarray(n, dtype=np.int32)
+        nu = np.ascontiguousarray(viscosity, dtype=np.float64)
+        if n.shape != nu.shape or n.ndim != 1:
+            raise ValueError("n and viscosity must be 1D arrays of the same length")
+        self.n = n.copy()
+        self.nruns = len(n)
+        self.length = float(length)
+        self._h = ctypes.c_void_p()
+        rc = self._L.fen_ensemble_create(int(self.nruns), n.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(nu),
+                                         self.length, float(CFL), float(forcing[0]), int(forcing[1]),
+                                         ctypes.byref(self._h))
+        self._check(rc)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise FenError(f"fen error {rc}: {self._L.fen_last_error().decode()}")
+
+    def destroy(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._L.fen_ensemble_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def upload(self, run, u, v, p=None):
+        N = int(self.n[run])
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (u, v)]
+        for a in arrs:
+            if a.shape != (N, N):
+                raise ValueError(f"run {run}: expected shape {(N, N)}, got {a.shape}")
+        pp = None if p is None else np.ascontiguousarray(p, dtype=np.float64)
+        self._check(self._L.fen_ensemble_upload(self._h, int(run), _dp(arrs[0]), _dp(arrs[1]),
+                                                _dp(pp) if pp is not None else None))
+
+    def download(self, run):
+        N = int(self.n[run])
+        u, v, p = np.zeros((N, N)), np.zeros((N, N)), np.zeros((N, N))
+        self._check(self._L.fen_ensemble_download(self._h, int(run), _dp(u), _dp(v), _dp(p)))
+        return u, v, p
+
+    def set_timestep(self, U):
+        self._check(self._L.fen_ensemble_set_timestep(self._h, float(U)))
+
+    def advance(self, nsteps):
+        """Advance every run by nsteps steps (one launch); returns the device time in ms."""
+        ms = ctypes.c_double()
+        self._check(self._L.fen_ensemble_advance(self._h, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    def status(self, run):
+        o = np.zeros(8)
+        self._check(self._L.fen_ensemble_status(self._h, int(run), _dp(o)))
+        return {"time": o[0], "dt": o[1], "dt_o": o[2], "maxvel": o[3], "ke": o[4], "maxdiv": o[5],
+                "nan": bool(o[6]), "viscosity": o[7]}
+
+    def config(self):
+        ci = ctypes.c_int
+        t, nc, ncl = ci(), ci(), ci()
+        sizes = (ci * 64)()
+        groups = (ci * 64)()
+        self._check(self._L.fen_ensemble_config(self._h, ctypes.byref(t), sizes, groups, ctypes.byref(nc),
+                                                ctypes.byref(ncl)))
+        return {"threads": t.value, "clusters": ncl.value,
+                "groups": {int(sizes[c]): int(groups[c]) for c in range(nc.value)}}
+
+    def set_config(self, threads, groups=None):
+        """groups: {N: CTAs per run} for every grid size of the ensemble."""
+        arr = None
+        if groups is not None:
+            order = list(self.config()["groups"].keys())
+            arr = (ctypes.c_int * len(order))(*[int(groups[N]) for N in order])
+        self._check(self._L.fen_ensemble_set_config(self._h, int(threads), arr))
+
+    def tune(self, steps=20, cache=None):
+        self._check(self._L.fen_ensemble_tune(self._h, int(steps), cache.encode() if cache else None))
+        return self.config()
+
+    def launches(self):
+        return int(self._L.fen_ensemble_launches(self._h))
+
+
+def ensemble_smem_bytes(n, groups, lib=None):
+    """Shared memory per CTA of an n x n run held by `groups` CTAs (0 if invalid)."""
+    L = lib or load_library()
+    return int(L.fen_ensemble_smem_bytes(int(n), int(groups)))

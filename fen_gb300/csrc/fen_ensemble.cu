@@ -1,0 +1,1074 @@
+// Batched ensemble of independent 2D periodic runs in one persistent launch.
+//
+// FEN advances one grid per program (navier_stokes_solver, navier_stokes.f90:50-136, with
+// the pp Poisson solver, poisson.f90:416-505).  Here hundreds of 2D periodic runs of uneven
+// sizes N x N advance together in FP32 (reductions in FP64) inside ONE kernel launch:
+//
+//  * The launch is persistent: clusters of 8 CTAs (one CTA per SM) take "packs" from a
+//    global counter.  A pack holds 8/G runs of one size N; each run lives on G CTAs of the
+//    cluster, every CTA holding N/G consecutive rows of u, v, p (plus one ghost row above
+//    and below) in shared memory for all the steps of the launch.  HBM is touched only to
+//    load and store the state once per launch and to stream dv_o (the AB2 history) once
+//    per step.
+//  * Inside a run, CTAs exchange data through distributed shared memory and synchronise
+//    with the hardware cluster barrier (barrier.cluster), which cannot deadlock: all CTAs
+//    of a cluster are co-scheduled and every CTA executes the same barrier sequence.
+//  * Per step: predictor (advection, diffusion, forcing, AB2, pressure gradient) ->
+//    divergence -> r2c FFT along x per row -> all-to-all of column blocks -> complex FFT
+//    along y, divide by the modified wavenumbers, inverse FFT -> all-to-all back -> c2r
+//    along x -> mean removal (FP64) -> correction, p update, max|u|+|v| (for the next dt)
+//    -> ghost rows from the neighbouring CTAs.  Five cluster barriers per step.
+//  * G (rows per CTA = N/G, the tile shape) is picked per N by the autotuner below, among
+//    the G that fit the shared-memory budget.
+//
+// The time step follows FEN's constant-CFL update (navier_stokes.f90:680-696):
+// dt_o = dt; dt = min(CFL delta / maxvel, dt_visc), capped at 1.1 dt_o; A = 1 + dt/(2 dt_o),
+// B = -dt/(2 dt_o).  Density is 1.  The forcing is S_x = amp sin(kf y) at the u points.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/fen_gpu.h"
+#include "fen_fft.cuh"
+
+namespace cg = cooperative_groups;
+using namespace fen;
+
+int fen_internal_fail(int code, const char* msg);
+
+namespace fen {
+namespace ens {
+
+constexpr int kCl = 8;                 // CTAs per cluster
+constexpr size_t kSmemLimit = 232448;  // opt-in dynamic shared memory per CTA (227 KB)
+constexpr size_t kSmemReserve = 1024;  // static shared memory of the kernel + slack
+
+// One grid size N of the ensemble.
+struct ClassDesc {
+  int N, G, M, SR, C, buf;  // rows per CTA M = N/G; spectrum row SR = N/2+1; column block C; buffer size (float2)
+  FFTPlan px, py;           // complex FFT lengths N/2 (x, real packing) and N (y)
+  const float2* twx;        // exp(-2 pi i m/(N/2)), m < N/2
+  const float2* twn;        // exp(-2 pi i k/N), k <= N/2
+  const float2* twy;        // exp(-2 pi i m/N), m < N
+  const float* lamx;        // 2 (cos(2 pi k/N) - 1)/delta^2, k <= N/2
+  const float* lamy;        // same, k < N
+  const float* force;       // amp sin(kf (j + 1/2) delta), j < N (u points)
+  float idx, id2, inv_nn;   // 1/delta, 1/delta^2, 1/N^2
+  double delta;
+};
+
+struct RunScal {
+  double dt, dt_o, t, maxvel, nu, dt_visc, ke, maxdiv;
+  int nan, pad[3];
+};
+
+struct Pack {
+  int cls, nruns, first, pad;  // runs run_list[first .. first + nruns)
+};
+
+struct EnsArgs {
+  const ClassDesc* cls;
+  const Pack* packs;
+  int npacks;
+  const int* run_list;
+  const long long* run_off;  // float offset of each run's state (u, v, p, dvo_x, dvo_y, N^2 each)
+  float* state;
+  RunScal* scal;
+  int* counter;
+  int nsteps;
+  double cfl;
+};
+
+__host__ __device__ inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// Shared-memory footprint of one CTA for grid size N on G CTAs (bytes, dynamic part).
+__host__ __device__ inline size_t smem_bytes(int N, int G, int* buf_out = nullptr) {
+  const int M = N / G, SR = N / 2 + 1, C = (SR + G - 1) / G;
+  const int buf = round_up(M * SR > N * C ? M * SR : N * C, 2);
+  if (buf_out) *buf_out = buf;
+  const size_t fields = (size_t)round_up(3 * (M + 2) * N, 4) * sizeof(float);
+  return fields + (size_t)3 * buf * sizeof(float2) + 8 * sizeof(double);
+}
+
+struct Carve {
+  float *u, *v, *p;
+  float2 *X, *Y, *Z;
+  double* red;
+};
+
+__device__ inline Carve carve(unsigned char* s, const ClassDesc& D) {
+  Carve c;
+  const int rows = (D.M + 2) * D.N;
+  c.u = reinterpret_cast<float*>(s);
+  c.v = c.u + rows;
+  c.p = c.v + rows;
+  float2* b = reinterpret_cast<float2*>(s + (size_t)round_up(3 * rows, 4) * sizeof(float));
+  c.X = b;
+  c.Y = b + D.buf;
+  c.Z = b + 2 * D.buf;
+  c.red = reinterpret_cast<double*>(b + 3 * D.buf);
+  return c;
+}
+
+template <int NT>
+__device__ inline double block_sum(double v, double* scratch) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) scratch[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (l < NT / 32) ? scratch[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  return r;  // valid in thread 0
+}
+
+template <int NT>
+__device__ inline float block_max(float v, float* scratch) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) scratch[w] = v;
+  __syncthreads();
+  float r = -INFINITY;
+  if (w == 0) {
+    r = (l < NT / 32) ? scratch[l] : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_down_sync(0xffffffffu, r, o));
+  }
+  return r;
+}
+
+__device__ inline const double2* tw64(const float2* p) { return reinterpret_cast<const double2*>(p); }
+
+template <int NT>
+__device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, int q, cg::cluster_group& cl,
+                         unsigned char* smem, double* s_sc, float* s_f, double* s_rd, float* s_rf) {
+  const int N = D.N, G = D.G, M = D.M, SR = D.SR, C = D.C;
+  const int slot = q / G, r = q - slot * G;
+  const bool active = slot < P.nruns;
+  if (!active && G == 1) return;  // no partner waits on this CTA
+  const int run = active ? a.run_list[P.first + slot] : 0;
+  const int base = slot * G;
+  const Carve S = carve(smem, D);
+  auto gsync = [&]() {
+    if (G > 1) cl.sync();
+    else __syncthreads();
+  };
+  auto pf = [&](float* ptr, int g) -> float* { return G == 1 ? ptr : cl.map_shared_rank(ptr, base + g); };
+  auto p2 = [&](float2* ptr, int g) -> float2* { return G == 1 ? ptr : cl.map_shared_rank(ptr, base + g); };
+  auto pd = [&](double* ptr, int g) -> double* { return G == 1 ? ptr : cl.map_shared_rank(ptr, base + g); };
+
+  const size_t NN = (size_t)N * N;
+  float* gu = a.state + (active ? a.run_off[run] : 0);
+  float* gv = gu + NN;
+  float* gp = gv + NN;
+  float* gdx = gp + NN;
+  float* gdy = gdx + NN;
+
+  // ---- load the CTA's rows (with one ghost row each side) ----
+  const int rows = (M + 2) * N;
+  for (int t = threadIdx.x; t < rows; t += NT) {
+    const int mm = t / N, i = t - mm * N;
+    int jg = r * M + mm - 1;
+    jg = jg < 0 ? jg + N : (jg >= N ? jg - N : jg);
+    float uu = 0.f, vv = 0.f, pp = 0.f;
+    if (active) {
+      uu = gu[(size_t)jg * N + i];
+      vv = gv[(size_t)jg * N + i];
+      pp = gp[(size_t)jg * N + i];
+    }
+    S.u[t] = uu;
+    S.v[t] = vv;
+    S.p[t] = pp;
+  }
+  if (threadIdx.x == 0) {
+    RunScal rs;
+    if (active) rs = a.scal[run];
+    else { rs.dt = rs.dt_o = 1.0; rs.t = 0.0; rs.maxvel = 1.0; rs.nu = 1.0; rs.dt_visc = 1.0; rs.nan = 0; }
+    s_sc[0] = rs.dt;
+    s_sc[1] = rs.dt_o;
+    s_sc[2] = rs.t;
+    s_sc[3] = rs.maxvel;
+    s_sc[4] = rs.nu;
+    s_sc[5] = rs.dt_visc;
+    s_sc[6] = rs.nan;
+  }
+  __syncthreads();
+  const float mu = (float)s_sc[4];
+  const float idx = D.idx, id2 = D.id2, q4 = 0.25f * D.idx;
+  const int cells = M * N;
+  const int Mh = N / 2, npair = Mh / 2 + 1;
+  float* Xf = reinterpret_cast<float*>(S.X);
+  float* Yf = reinterpret_cast<float*>(S.Y);
+  float* Zf = reinterpret_cast<float*>(S.Z);
+  const int rp = (r + 1) % G, rm = (r - 1 + G) % G;
+  const int c0 = r * C, Cr = max(0, min(C, SR - c0));
+
+  for (int step = 0; step < a.nsteps; ++step) {
+    // ---- update_timestep (constant CFL), FP64 ----
+    if (threadIdx.x == 0) {
+      const double dt_o = s_sc[0], mv = s_sc[3];
+      const double dt_conv = (mv > 0.0) ? a.cfl * D.delta / mv : 1.0;
+      double dt = fmin(dt_conv, s_sc[5]);
+      if (dt > 1.1 * dt_o) dt = 1.1 * dt_o;
+      s_sc[0] = dt;
+      s_sc[1] = dt_o;
+      s_f[0] = (float)dt;
+      s_f[1] = (float)(1.0 + 0.5 * dt / dt_o);
+      s_f[2] = (float)(-0.5 * dt / dt_o);
+      s_f[3] = (float)(1.0 / dt);
+    }
+    __syncthreads();
+    const float dt = s_f[0], A = s_f[1], B = s_f[2], rdt = s_f[3];
+
+    // ---- predictor: u* -> X, v* -> Y (FP32), dv_o streamed from/to HBM ----
+    for (int t = threadIdx.x; t < cells; t += NT) {
+      const int m = t / N, i = t - m * N;
+      const int ip = (i + 1 == N) ? 1 - N : 1;
+      const int im = (i == 0) ? N - 1 : -1;
+      const int c = t + N;
+      const float* U = S.u;
+      const float* V = S.v;
+      const float* Pp = S.p;
+      const float uc = U[c], uip = U[c + ip], uim = U[c + im], ujp = U[c + N], ujm = U[c - N], uimjp = U[c + N + im];
+      const float vc = V[c], vip = V[c + ip], vim = V[c + im], vjp = V[c + N], vjm = V[c - N], vipjm = V[c - N + ip];
+      const int jg = r * M + m;
+      // u: -(d(uu)/dx + d(uv)/dy) + nu lap(u) + S_x      (navier_stokes.f90:297-323, fields.f90:326-329)
+      const float fe = (uip + uc) * (uip + uc), fw = (uc + uim) * (uc + uim);
+      const float cn = (ujp + uc) * (vip + vc), cs = (uc + ujm) * (vipjm + vjm);
+      const float dvx = -((fe - fw) + (cn - cs)) * q4 + mu * (((uip + uim) + (ujp + ujm)) - 4.0f * uc) * id2 + __ldg(D.force + jg);
+      // v: -(d(uv)/dx + d(vv)/dy) + nu lap(v)
+      const float cw = (uimjp + uim) * (vc + vim);
+      const float fn = (vjp + vc) * (vjp + vc), fs = (vc + vjm) * (vc + vjm);
+      const float dvy = -((cn - cw) + (fn - fs)) * q4 + mu * (((vip + vim) + (vjp + vjm)) - 4.0f * vc) * id2;
+      float ox = 0.f, oy = 0.f;
+      if (active) {
+        const size_t gi = (size_t)jg * N + i;
+        ox = gdx[gi];
+        oy = gdy[gi];
+        gdx[gi] = dvx;
+        gdy[gi] = dvy;
+      }
+      Xf[t] = uc + dt * (-(Pp[c + ip] - Pp[c]) * idx + A * dvx + B * ox);
+      Yf[t] = vc + dt * (-(Pp[c + N] - Pp[c]) * idx + A * dvy + B * oy);
+    }
+    gsync();  // B1: v* rows visible to the next CTA
+
+    // ---- divergence -> Z (real rows of stride 2 SR floats); u, v <- u*, v* ----
+    {
+      const float* Yprev = pf(Yf, rm);
+      const float sc = idx * rdt;
+      for (int t = threadIdx.x; t < cells; t += NT) {
+        const int m = t / N, i = t - m * N;
+        const int im = (i == 0) ? N - 1 : -1;
+        const float us = Xf[t], usm = Xf[t + im], vs = Yf[t];
+        const float vsm = (m > 0) ? Yf[t - N] : Yprev[(M - 1) * N + i];
+        Zf[m * 2 * SR + i] = ((us - usm) + (vs - vsm)) * sc;
+        S.u[t + N] = us;
+        S.v[t + N] = vs;
+      }
+    }
+    __syncthreads();
+
+    // ---- r2c along x: complex FFT of length N/2 on the packed rows, then unpacking ----
+    float2* SPEC = smem_fft<-1, float2>(S.Z, S.X, M, SR, 1, D.px, tw64(D.twx));
+    for (int t = threadIdx.x; t < M * npair; t += NT) {
+      const int m = t / npair, k = t - m * npair;
+      float2* row = SPEC + m * SR;
+      if (k == 0) {
+        const float2 x0 = r2c_post(row, 1, Mh, 0, tw64(D.twn));
+        const float2 xm = r2c_post(row, 1, Mh, Mh, tw64(D.twn));
+        row[0] = x0;
+        row[Mh] = xm;
+      } else {
+        const float2 xa = r2c_post(row, 1, Mh, k, tw64(D.twn));
+        const float2 xb = r2c_post(row, 1, Mh, Mh - k, tw64(D.twn));
+        row[k] = xa;
+        row[Mh - k] = xb;
+      }
+    }
+    gsync();  // B2: every row spectrum complete
+
+    // ---- all-to-all: gather the column block [c0, c0+Cr) of every row into T (= Y) ----
+    float2* T = S.Y;
+    float2* F = (SPEC == S.Z) ? S.X : S.Z;
+    for (int t = threadIdx.x; t < N * C; t += NT) {
+      const int y = t / C, cc = t - y * C;
+      float2 val = make_float2(0.f, 0.f);
+      if (cc < Cr) {
+        const int g = y / M, m = y - g * M;
+        val = p2(SPEC, g)[m * SR + c0 + cc];
+      }
+      T[t] = val;
+    }
+    __syncthreads();
+    // ---- y: forward FFT, divide by lam_x + lam_y (zero mode -> 0), inverse FFT ----
+    float2* R1 = smem_fft<-1, float2>(T, F, C, 1, C, D.py, tw64(D.twy));
+    for (int t = threadIdx.x; t < N * C; t += NT) {
+      const int y = t / C, cc = t - y * C;
+      if (cc < Cr) {
+        const int kx = c0 + cc;
+        const float lam = __ldg(D.lamx + kx) + __ldg(D.lamy + y);
+        const float s = (kx == 0 && y == 0) ? 0.f : D.inv_nn / lam;
+        float2 z = R1[t];
+        z.x *= s;
+        z.y *= s;
+        R1[t] = z;
+      }
+    }
+    __syncthreads();
+    float2* R2 = smem_fft<1, float2>(R1, (R1 == T) ? F : T, C, 1, C, D.py, tw64(D.twy));
+    gsync();  // B3: column solves complete; row spectra no longer read
+
+    // ---- all-to-all back: rows of this CTA from every column owner, into SPEC ----
+    for (int t = threadIdx.x; t < M * SR; t += NT) {
+      const int m = t / SR, cc = t - m * SR;
+      const int o = cc / C, cl_ = cc - o * C;
+      SPEC[m * SR + cc] = p2(R2, o)[(r * M + m) * C + cl_];
+    }
+    __syncthreads();
+    // ---- c2r along x: packing then inverse complex FFT of length N/2 ----
+    for (int t = threadIdx.x; t < M * npair; t += NT) {
+      const int m = t / npair, k = t - m * npair;
+      float2* row = SPEC + m * SR;
+      if (k == 0) {
+        row[0] = c2r_pre(row[0], row[Mh], Mh, 0, tw64(D.twn));
+      } else {
+        const float2 xa = row[k], xb = row[Mh - k];
+        const float2 za = c2r_pre(xa, xb, Mh, k, tw64(D.twn));
+        const float2 zb = c2r_pre(xb, xa, Mh, Mh - k, tw64(D.twn));
+        row[k] = za;
+        if (Mh - k != k) row[Mh - k] = zb;
+      }
+    }
+    __syncthreads();
+    float2* W3 = (SPEC != S.X && R2 != S.X) ? S.X : ((SPEC != S.Y && R2 != S.Y) ? S.Y : S.Z);
+    float2* PHI = smem_fft<1, float2>(SPEC, W3, M, SR, 1, D.px, tw64(D.twx));
+    const float* Phf = reinterpret_cast<const float*>(PHI);
+    {  // FP64 sum of phi for the mean removal (poisson.f90:491-503)
+      float part = 0.f;
+      for (int t = threadIdx.x; t < cells; t += NT) {
+        const int m = t / N, i = t - m * N;
+        part += Phf[m * 2 * SR + i];
+      }
+      const double s = block_sum<NT>((double)part, s_rd);
+      if (threadIdx.x == 0) S.red[0] = s;
+    }
+    gsync();  // B4: phi and the partial sums visible
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int g = 0; g < G; ++g) s += pd(S.red, g)[0];
+      s_f[4] = (float)(s / ((double)N * N));
+    }
+    __syncthreads();
+
+    // ---- correction, p update, max(|u| + |v|) ----
+    {
+      const float meanf = s_f[4];
+      const float* Phn = reinterpret_cast<const float*>(p2(PHI, rp));
+      float vmax = 0.f;
+      int bad = 0;
+      for (int t = threadIdx.x; t < cells; t += NT) {
+        const int m = t / N, i = t - m * N;
+        const int ip = (i + 1 == N) ? 1 - N : 1;
+        const int o = m * 2 * SR + i;
+        const float ph = Phf[o], phip = Phf[o + ip];
+        const float phjp = (m + 1 < M) ? Phf[o + 2 * SR] : Phn[i];
+        const int c = t + N;
+        const float un = S.u[c] - dt * (phip - ph) * idx;
+        const float vn = S.v[c] - dt * (phjp - ph) * idx;
+        S.u[c] = un;
+        S.v[c] = vn;
+        S.p[c] = S.p[c] + (ph - meanf);
+        const float vel = fabsf(un) + fabsf(vn);
+        if (vel != vel) bad = 1;
+        vmax = fmaxf(vmax, vel);
+      }
+      const float mx = block_max<NT>(vmax, s_rf);
+      bad = __syncthreads_or(bad);
+      if (threadIdx.x == 0) {
+        S.red[1] = (double)mx;
+        S.red[2] = (double)bad;
+      }
+    }
+    gsync();  // B5: corrected rows, maxima visible
+    if (threadIdx.x == 0) {
+      double mv = 0.0, bad = 0.0;
+      for (int g = 0; g < G; ++g) {
+        const double* rr = pd(S.red, g);
+        mv = fmax(mv, rr[1]);
+        bad = fmax(bad, rr[2]);
+      }
+      s_sc[3] = mv;
+      s_sc[2] += s_sc[0];
+      if (bad != 0.0) s_sc[6] = 1.0;
+    }
+    // ---- ghost rows from the neighbouring CTAs (periodic in y) ----
+    {
+      const float* Um = pf(S.u, rm);
+      const float* Vm = pf(S.v, rm);
+      const float* Pm = pf(S.p, rm);
+      const float* Un = pf(S.u, rp);
+      const float* Vn = pf(S.v, rp);
+      const float* Pn = pf(S.p, rp);
+      for (int t = threadIdx.x; t < 2 * N; t += NT) {
+        if (t < N) {
+          S.u[t] = Um[M * N + t];
+          S.v[t] = Vm[M * N + t];
+          S.p[t] = Pm[M * N + t];
+        } else {
+          const int i = t - N;
+          S.u[(M + 1) * N + i] = Un[N + i];
+          S.v[(M + 1) * N + i] = Vn[N + i];
+          S.p[(M + 1) * N + i] = Pn[N + i];
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- store the state; kinetic energy and max div (FP64 across the run) ----
+  {
+    float kpart = 0.f, dmax = -INFINITY;
+    for (int t = threadIdx.x; t < cells; t += NT) {
+      const int m = t / N, i = t - m * N;
+      const int im = (i == 0) ? N - 1 : -1;
+      const int c = t + N;
+      const float uu = S.u[c], vv = S.v[c];
+      if (active) {
+        const size_t gi = (size_t)(r * M + m) * N + i;
+        gu[gi] = uu;
+        gv[gi] = vv;
+        gp[gi] = S.p[c];
+      }
+      kpart += uu * uu + vv * vv;
+      dmax = fmaxf(dmax, ((uu - S.u[c + im]) + (vv - S.v[c - N])) * idx);
+    }
+    const double ks = block_sum<NT>((double)kpart, s_rd);
+    const float dm = block_max<NT>(dmax, s_rf);
+    if (threadIdx.x == 0) {
+      S.red[3] = ks;
+      S.red[4] = (double)dm;
+    }
+    gsync();
+    if (threadIdx.x == 0 && r == 0 && active) {
+      double k = 0.0, d = -INFINITY;
+      for (int g = 0; g < G; ++g) {
+        const double* rr = pd(S.red, g);
+        k += rr[3];
+        d = fmax(d, rr[4]);
+      }
+      RunScal rs = a.scal[run];
+      rs.dt = s_sc[0];
+      rs.dt_o = s_sc[1];
+      rs.t = s_sc[2];
+      rs.maxvel = s_sc[3];
+      rs.nan = (int)s_sc[6];
+      rs.ke = 0.5 * k / ((double)N * N);
+      rs.maxdiv = d;
+      a.scal[run] = rs;
+    }
+    gsync();  // partners finished reading this CTA's partial sums
+  }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) k_ensemble(EnsArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_pack;
+  __shared__ ClassDesc s_D;
+  __shared__ double s_sc[8];
+  __shared__ float s_f[8];
+  __shared__ double s_rd[32];
+  __shared__ float s_rf[32];
+  cg::cluster_group cl = cg::this_cluster();
+  const int q = (int)cl.block_rank();
+  for (;;) {
+    if (q == 0 && threadIdx.x == 0) s_pack = atomicAdd(a.counter, 1);
+    cl.sync();
+    const int pk = *cl.map_shared_rank(&s_pack, 0);
+    cl.sync();  // every CTA has read the pack index before rank 0 fetches the next one
+    if (pk >= a.npacks) break;
+    const Pack P = a.packs[pk];
+    if (threadIdx.x == 0) s_D = a.cls[P.cls];
+    __syncthreads();
+    run_pack<NT>(a, P, s_D, q, cl, smem, s_sc, s_f, s_rd, s_rf);
+    __syncthreads();
+  }
+}
+
+}  // namespace ens
+}  // namespace fen
+
+using namespace fen::ens;
+
+// ------------------------------------------------------------------------------------------
+// Host side
+// ------------------------------------------------------------------------------------------
+struct fen_ensemble {
+  int nruns = 0;
+  int dev = 0;
+  std::vector<int> n;
+  std::vector<double> nu;
+  double L = 0, cfl = 0, famp = 0;
+  int fk = 0;
+  std::vector<int> cls_n;                // distinct grid sizes, largest first
+  std::vector<int> cls_g;                // CTAs per run for each size
+  std::vector<int> run_cls;              // class of each run
+  std::vector<ClassDesc> cls_host;
+  std::vector<void*> bufs;
+  std::vector<long long> off;
+  float* state = nullptr;
+  long long* d_off = nullptr;
+  RunScal* d_scal = nullptr;
+  std::vector<RunScal> scal;
+  ClassDesc* d_cls = nullptr;
+  Pack* d_packs = nullptr;
+  int* d_runlist = nullptr;
+  int* d_counter = nullptr;
+  int npacks = 0;
+  int threads = 1024;
+  size_t smem = 0;
+  int nclusters = 0;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int exec_steps = -1;
+  long long launches = 0;
+  bool scal_dirty = false;
+};
+
+namespace {
+
+#define EK(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess)                                                                      \
+      return fen_internal_fail(FEN_ERR_CUDA, (std::string(#x) + ": " + cudaGetErrorString(e_)).c_str()); \
+  } while (0)
+
+bool plan_len(int M, FFTPlan& P) {
+  P.M = M;
+  P.nst = 0;
+  int m = M;
+  while (m % 4 == 0) { P.R[P.nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { P.R[P.nst++] = 2; m /= 2; }
+  while (m % 3 == 0) { P.R[P.nst++] = 3; m /= 3; }
+  return m == 1 && P.nst <= kMaxStages;
+}
+
+bool g_feasible(int N, int G) {
+  if (G != 1 && G != 2 && G != 4 && G != 8) return false;
+  if (N % G != 0 || N / G < 2) return false;
+  return smem_bytes(N, G) + kSmemReserve <= kSmemLimit;
+}
+
+template <typename T>
+int dev_upload(fen_ensemble* e, const std::vector<T>& h, const T** out) {
+  void* d = nullptr;
+  EK(cudaMalloc(&d, std::max<size_t>(h.size(), 1) * sizeof(T)));
+  e->bufs.push_back(d);
+  EK(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  *out = (const T*)d;
+  return 0;
+}
+
+int build_class(fen_ensemble* e, int N, ClassDesc& D) {
+  D = ClassDesc{};
+  D.N = N;
+  if (!plan_len(N / 2, D.px) || !plan_len(N, D.py)) return fen_internal_fail(FEN_ERR_ARG, "ensemble grid size must be 2^a 3^b, a >= 2");
+  const double d = e->L / N;
+  D.delta = d;
+  D.idx = (float)(1.0 / d);
+  D.id2 = (float)(1.0 / (d * d));
+  D.inv_nn = (float)(1.0 / ((double)N * N));
+  std::vector<float2> twx(N / 2), twn(N / 2 + 1), twy(N);
+  for (int m = 0; m < N / 2; ++m) { const double t = 2.0 * M_PI * m / (N / 2); twx[m] = make_float2((float)cos(t), (float)-sin(t)); }
+  for (int k = 0; k <= N / 2; ++k) { const double t = 2.0 * M_PI * k / N; twn[k] = make_float2((float)cos(t), (float)-sin(t)); }
+  for (int m = 0; m < N; ++m) { const double t = 2.0 * M_PI * m / N; twy[m] = make_float2((float)cos(t), (float)-sin(t)); }
+  std::vector<float> lx(N / 2 + 1), ly(N), fo(N);
+  for (int k = 0; k <= N / 2; ++k) lx[k] = (float)(2.0 * (cos(2.0 * M_PI * k / N) - 1.0) / (d * d));
+  for (int k = 0; k < N; ++k) ly[k] = (float)(2.0 * (cos(2.0 * M_PI * k / N) - 1.0) / (d * d));
+  for (int j = 0; j < N; ++j) fo[j] = (float)(e->famp * sin(e->fk * (j + 0.5) * d));
+  int r;
+  if ((r = dev_upload(e, twx, &D.twx)) || (r = dev_upload(e, twn, &D.twn)) || (r = dev_upload(e, twy, &D.twy)) ||
+      (r = dev_upload(e, lx, &D.lamx)) || (r = dev_upload(e, ly, &D.lamy)) || (r = dev_upload(e, fo, &D.force)))
+    return r;
+  return 0;
+}
+
+void set_g(ClassDesc& D, int G) {
+  D.G = G;
+  D.M = D.N / G;
+  D.SR = D.N / 2 + 1;
+  D.C = (D.SR + G - 1) / G;
+  int buf = 0;
+  smem_bytes(D.N, G, &buf);
+  D.buf = buf;
+}
+
+const void* kernel_ptr(int threads) {
+  return threads == 512 ? (const void*)k_ensemble<512> : (const void*)k_ensemble<1024>;
+}
+
+// Pack the runs `subset` (all runs when empty) with the current G per class; uploads the
+// class table, the packs and the run list, and sizes the launch.
+int build_packs(fen_ensemble* e, const std::vector<int>& subset) {
+  std::vector<Pack> packs;
+  std::vector<int> list;
+  size_t smem = 0;
+  for (size_t c = 0; c < e->cls_n.size(); ++c) {
+    set_g(e->cls_host[c], e->cls_g[c]);
+    const int G = e->cls_g[c], per = kCl / G;
+    std::vector<int> runs;
+    if (subset.empty()) {
+      for (int q = 0; q < e->nruns; ++q)
+        if (e->run_cls[q] == (int)c) runs.push_back(q);
+    } else {
+      for (int q : subset)
+        if (e->run_cls[q] == (int)c) runs.push_back(q);
+    }
+    if (runs.empty()) continue;
+    smem = std::max(smem, smem_bytes(e->cls_n[c], G));
+    for (size_t s = 0; s < runs.size(); s += per) {
+      Pack p;
+      p.cls = (int)c;
+      p.first = (int)list.size();
+      p.nruns = (int)std::min<size_t>(per, runs.size() - s);
+      p.pad = 0;
+      for (int k = 0; k < p.nruns; ++k) list.push_back(runs[s + k]);
+      packs.push_back(p);
+    }
+  }
+  EK(cudaMemcpy(e->d_cls, e->cls_host.data(), e->cls_host.size() * sizeof(ClassDesc), cudaMemcpyHostToDevice));
+  if (e->d_packs) cudaFree(e->d_packs);
+  if (e->d_runlist) cudaFree(e->d_runlist);
+  e->d_packs = nullptr;
+  e->d_runlist = nullptr;
+  EK(cudaMalloc(&e->d_packs, std::max<size_t>(packs.size(), 1) * sizeof(Pack)));
+  EK(cudaMalloc(&e->d_runlist, std::max<size_t>(list.size(), 1) * sizeof(int)));
+  if (!packs.empty()) EK(cudaMemcpy(e->d_packs, packs.data(), packs.size() * sizeof(Pack), cudaMemcpyHostToDevice));
+  if (!list.empty()) EK(cudaMemcpy(e->d_runlist, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+  e->npacks = (int)packs.size();
+  e->smem = smem;
+  const void* k = kernel_ptr(e->threads);
+  EK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1)));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kCl;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(kCl, 1, 1);
+  cfg.blockDim = dim3(e->threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int nc = 0;
+  EK(cudaOccupancyMaxActiveClusters(&nc, k, &cfg));
+  if (nc < 1) return fen_internal_fail(FEN_ERR_CUDA, "no cluster of 8 CTAs fits this device with the ensemble's shared memory");
+  e->nclusters = nc;
+  if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+  if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
+  e->exec_steps = -1;
+  return 0;
+}
+
+int launch(fen_ensemble* e, int nsteps) {
+  EnsArgs a;
+  a.cls = e->d_cls;
+  a.packs = e->d_packs;
+  a.npacks = e->npacks;
+  a.run_list = e->d_runlist;
+  a.run_off = e->d_off;
+  a.state = e->state;
+  a.scal = e->d_scal;
+  a.counter = e->d_counter;
+  a.nsteps = nsteps;
+  a.cfl = e->cfl;
+  EK(cudaMemsetAsync(e->d_counter, 0, sizeof(int), e->stream));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kCl;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(kCl * std::max(1, std::min(e->nclusters, e->npacks)), 1, 1);
+  cfg.blockDim = dim3(e->threads, 1, 1);
+  cfg.dynamicSmemBytes = e->smem;
+  cfg.stream = e->stream;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (e->threads == 512) EK(cudaLaunchKernelEx(&cfg, k_ensemble<512>, a));
+  else EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024>, a));
+  EK(cudaGetLastError());
+  return 0;
+}
+
+int push_scal(fen_ensemble* e) {
+  if (e->scal_dirty) {
+    EK(cudaMemcpyAsync(e->d_scal, e->scal.data(), e->scal.size() * sizeof(RunScal), cudaMemcpyHostToDevice, e->stream));
+    e->scal_dirty = false;
+  }
+  return 0;
+}
+
+int pull_scal(fen_ensemble* e) {
+  EK(cudaMemcpyAsync(e->scal.data(), e->d_scal, e->scal.size() * sizeof(RunScal), cudaMemcpyDeviceToHost, e->stream));
+  EK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+int advance_graph(fen_ensemble* e, int nsteps, float* ms) {
+  int r;
+  if ((r = push_scal(e))) return r;
+  if (e->exec_steps != nsteps) {
+    if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
+    if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
+    EK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    r = launch(e, nsteps);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+    if (r) { if (g) cudaGraphDestroy(g); return r; }
+    EK(ce);
+    e->graph = g;
+    EK(cudaGraphInstantiate(&e->exec, e->graph, 0));
+    e->exec_steps = nsteps;
+  }
+  cudaEvent_t e0, e1;
+  EK(cudaEventCreate(&e0));
+  EK(cudaEventCreate(&e1));
+  EK(cudaEventRecord(e0, e->stream));
+  EK(cudaGraphLaunch(e->exec, e->stream));
+  EK(cudaEventRecord(e1, e->stream));
+  EK(cudaEventSynchronize(e1));
+  EK(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  e->launches += 1;
+  return pull_scal(e);
+}
+
+std::string device_key(int dev) {
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return "unknown";
+  std::string s = p.name;
+  for (auto& ch : s)
+    if (ch == ' ') ch = '_';
+  return s + "_sm" + std::to_string(p.multiProcessorCount);
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t fen_ensemble_smem_bytes(int n, int groups) {
+  if (n <= 0 || groups <= 0 || n % groups) return 0;
+  return smem_bytes(n, groups) + kSmemReserve;
+}
+
+int fen_ensemble_create(int nruns, const int* n, const double* viscosity, double length, double cfl, double forcing_amplitude,
+                        int forcing_wavenumber, fen_ensemble** out) {
+  if (!out || nruns < 1 || !n || !viscosity || !(length > 0) || !(cfl > 0)) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  *out = nullptr;
+  for (int q = 0; q < nruns; ++q) {
+    FFTPlan P;
+    if (n[q] < 8 || n[q] % 4 != 0 || !plan_len(n[q], P) || !plan_len(n[q] / 2, P))
+      return fen_internal_fail(FEN_ERR_ARG, ("ensemble run " + std::to_string(q) + ": N must be 2^a 3^b, a >= 2, N >= 8").c_str());
+    if (!(viscosity[q] > 0)) return fen_internal_fail(FEN_ERR_ARG, "viscosity must be positive");
+    bool ok = false;
+    for (int G = 1; G <= 8; G *= 2) ok = ok || g_feasible(n[q], G);
+    if (!ok) return fen_internal_fail(FEN_ERR_ARG, ("ensemble run " + std::to_string(q) + ": N = " + std::to_string(n[q]) +
+                                                    " does not fit a cluster's shared memory").c_str());
+  }
+  fen_ensemble* e = new fen_ensemble();
+  e->nruns = nruns;
+  e->n.assign(n, n + nruns);
+  e->nu.assign(viscosity, viscosity + nruns);
+  e->L = length;
+  e->cfl = cfl;
+  e->famp = forcing_amplitude;
+  e->fk = forcing_wavenumber;
+  cudaError_t ce = cudaGetDevice(&e->dev);
+  if (ce != cudaSuccess) { delete e; return fen_internal_fail(FEN_ERR_CUDA, cudaGetErrorString(ce)); }
+  int cc = 0;
+  cudaDeviceGetAttribute(&cc, cudaDevAttrClusterLaunch, e->dev);
+  if (!cc) { delete e; return fen_internal_fail(FEN_ERR_CUDA, "device has no thread-block cluster launch"); }
+  std::vector<int> sizes(e->n);
+  std::sort(sizes.begin(), sizes.end(), std::greater<int>());
+  sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+  e->cls_n = sizes;
+  e->run_cls.resize(nruns);
+  for (int q = 0; q < nruns; ++q) e->run_cls[q] = (int)(std::find(sizes.begin(), sizes.end(), e->n[q]) - sizes.begin());
+  e->cls_host.resize(sizes.size());
+  e->cls_g.resize(sizes.size());
+  int r = 0;
+  for (size_t c = 0; c < sizes.size() && !r; ++c) {
+    r = build_class(e, sizes[c], e->cls_host[c]);
+    int G = 1;  // default tile: the fewest CTAs per run that fit
+    while (!g_feasible(sizes[c], G)) G *= 2;
+    e->cls_g[c] = G;
+  }
+  if (r) { fen_ensemble_destroy(e); return r; }
+  e->off.resize(nruns);
+  long long tot = 0;
+  for (int q = 0; q < nruns; ++q) {
+    e->off[q] = tot;
+    tot += 5LL * e->n[q] * e->n[q];
+  }
+  e->scal.assign(nruns, RunScal{});
+  for (int q = 0; q < nruns; ++q) {
+    const double d = length / e->n[q];
+    e->scal[q].nu = e->nu[q];
+    e->scal[q].dt_visc = 0.125 * d * d / e->nu[q];
+    e->scal[q].dt = e->scal[q].dt_o = std::min(cfl * d, e->scal[q].dt_visc);
+    e->scal[q].maxvel = 0.0;
+  }
+  e->scal_dirty = true;
+  auto fail_cuda = [&](cudaError_t err, const char* what) {
+    fen_ensemble_destroy(e);
+    return fen_internal_fail(FEN_ERR_CUDA, (std::string(what) + ": " + cudaGetErrorString(err)).c_str());
+  };
+  if ((ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail_cuda(ce, "stream");
+  if ((ce = cudaMalloc(&e->state, tot * sizeof(float))) != cudaSuccess) return fail_cuda(ce, "state");
+  if ((ce = cudaMemset(e->state, 0, tot * sizeof(float))) != cudaSuccess) return fail_cuda(ce, "state");
+  if ((ce = cudaMalloc(&e->d_off, nruns * sizeof(long long))) != cudaSuccess) return fail_cuda(ce, "offsets");
+  if ((ce = cudaMemcpy(e->d_off, e->off.data(), nruns * sizeof(long long), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return fail_cuda(ce, "offsets");
+  if ((ce = cudaMalloc(&e->d_scal, nruns * sizeof(RunScal))) != cudaSuccess) return fail_cuda(ce, "scalars");
+  if ((ce = cudaMalloc(&e->d_cls, sizes.size() * sizeof(ClassDesc))) != cudaSuccess) return fail_cuda(ce, "classes");
+  if ((ce = cudaMalloc(&e->d_counter, sizeof(int))) != cudaSuccess) return fail_cuda(ce, "counter");
+  if ((r = build_packs(e, {}))) { fen_ensemble_destroy(e); return r; }
+  *out = e;
+  return 0;
+}
+
+int fen_ensemble_destroy(fen_ensemble* e) {
+  if (!e) return 0;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  if (e->graph) cudaGraphDestroy(e->graph);
+  for (void* b : e->bufs) cudaFree(b);
+  void* ptrs[] = {e->state, e->d_off, e->d_scal, e->d_cls, e->d_packs, e->d_runlist, e->d_counter};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return 0;
+}
+
+int fen_ensemble_upload(fen_ensemble* e, int run, const double* u, const double* v, const double* p) {
+  if (!e || run < 0 || run >= e->nruns || !u || !v) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  const int N = e->n[run];
+  const size_t NN = (size_t)N * N;
+  std::vector<float> h(5 * NN, 0.f);
+  double mv = 0.0;
+  for (size_t k = 0; k < NN; ++k) {
+    h[k] = (float)u[k];
+    h[NN + k] = (float)v[k];
+    h[2 * NN + k] = p ? (float)p[k] : 0.f;
+    const double vel = fabs((double)h[k]) + fabs((double)h[NN + k]);
+    if (vel > mv || vel != vel) mv = vel;
+  }
+  EK(cudaMemcpyAsync(e->state + e->off[run], h.data(), 5 * NN * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+  EK(cudaStreamSynchronize(e->stream));
+  e->scal[run].maxvel = mv;
+  e->scal[run].t = 0.0;
+  e->scal[run].nan = 0;
+  e->scal_dirty = true;
+  return 0;
+}
+
+int fen_ensemble_download(fen_ensemble* e, int run, double* u, double* v, double* p) {
+  if (!e || run < 0 || run >= e->nruns) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  const int N = e->n[run];
+  const size_t NN = (size_t)N * N;
+  std::vector<float> h(3 * NN);
+  EK(cudaMemcpyAsync(h.data(), e->state + e->off[run], 3 * NN * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+  EK(cudaStreamSynchronize(e->stream));
+  for (size_t k = 0; k < NN; ++k) {
+    if (u) u[k] = h[k];
+    if (v) v[k] = h[NN + k];
+    if (p) p[k] = h[2 * NN + k];
+  }
+  return 0;
+}
+
+int fen_ensemble_set_timestep(fen_ensemble* e, double U) {
+  if (!e || !(U > 0)) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  for (int q = 0; q < e->nruns; ++q) {
+    const double d = e->L / e->n[q];
+    e->scal[q].dt = e->scal[q].dt_o = std::min(e->cfl * d / U, e->scal[q].dt_visc);
+  }
+  e->scal_dirty = true;
+  return 0;
+}
+
+int fen_ensemble_advance(fen_ensemble* e, int nsteps, double* ms) {
+  if (!e || nsteps < 1) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  float f = 0.f;
+  int r;
+  if ((r = advance_graph(e, nsteps, &f))) return r;
+  if (ms) *ms = f;
+  for (int q = 0; q < e->nruns; ++q)
+    if (e->scal[q].nan) return fen_internal_fail(FEN_ERR_NAN, ("NaN in the velocity of ensemble run " + std::to_string(q)).c_str());
+  return 0;
+}
+
+int fen_ensemble_status(fen_ensemble* e, int run, double* out) {
+  if (!e || run < 0 || run >= e->nruns || !out) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  const RunScal& s = e->scal[run];
+  out[0] = s.t;
+  out[1] = s.dt;
+  out[2] = s.dt_o;
+  out[3] = s.maxvel;
+  out[4] = s.ke;
+  out[5] = s.maxdiv;
+  out[6] = s.nan;
+  out[7] = s.nu;
+  return 0;
+}
+
+int fen_ensemble_config(fen_ensemble* e, int* threads, int* sizes, int* groups, int* nclasses, int* nclusters) {
+  if (!e) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  if (threads) *threads = e->threads;
+  if (nclasses) *nclasses = (int)e->cls_n.size();
+  if (nclusters) *nclusters = e->nclusters;
+  for (size_t c = 0; c < e->cls_n.size(); ++c) {
+    if (sizes) sizes[c] = e->cls_n[c];
+    if (groups) groups[c] = e->cls_g[c];
+  }
+  return 0;
+}
+
+int fen_ensemble_set_config(fen_ensemble* e, int threads, const int* groups) {
+  if (!e || (threads != 512 && threads != 1024)) return fen_internal_fail(FEN_ERR_ARG, "threads must be 512 or 1024");
+  if (groups)
+    for (size_t c = 0; c < e->cls_n.size(); ++c)
+      if (!g_feasible(e->cls_n[c], groups[c]))
+        return fen_internal_fail(FEN_ERR_ARG, ("N = " + std::to_string(e->cls_n[c]) + " on " + std::to_string(groups[c]) +
+                                               " CTAs does not fit").c_str());
+  e->threads = threads;
+  if (groups)
+    for (size_t c = 0; c < e->cls_n.size(); ++c) e->cls_g[c] = groups[c];
+  return build_packs(e, {});
+}
+
+long long fen_ensemble_launches(fen_ensemble* e) { return e ? e->launches : 0; }
+
+// Autotuner: per grid size, the CTAs per run G (tile = N/G rows) among those that fit; then
+// the CTA size.  Each candidate advances a sample of the ensemble's own runs for `steps`
+// steps (the state is restored afterwards) and the fastest is kept.  Results are cached in
+// `cache_path` (one "device N G" or "device threads T" line each) and reused when present.
+int fen_ensemble_tune(fen_ensemble* e, int steps, const char* cache_path) {
+  if (!e || steps < 1) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  const std::string key = device_key(e->dev);
+  std::map<int, int> cached_g;
+  int cached_t = 0;
+  if (cache_path) {
+    std::ifstream f(cache_path);
+    std::string line;
+    while (std::getline(f, line)) {
+      std::istringstream ss(line);
+      std::string k, what;
+      int a = 0, b = 0;
+      if (!(ss >> k >> what >> a)) continue;
+      if (k != key) continue;
+      if (what == "threads") cached_t = a;
+      else if (what == "N" && (ss >> b)) cached_g[a] = b;
+    }
+  }
+  bool all = cached_t == 512 || cached_t == 1024;
+  for (int N : e->cls_n) all = all && cached_g.count(N) && g_feasible(N, cached_g[N]);
+  int r;
+  if (all) {
+    for (size_t c = 0; c < e->cls_n.size(); ++c) e->cls_g[c] = cached_g[e->cls_n[c]];
+    e->threads = cached_t;
+    return build_packs(e, {});
+  }
+  // back up the state and the scalars
+  const long long tot = e->off.back() + 5LL * e->n.back() * e->n.back();
+  float* backup = nullptr;
+  EK(cudaMalloc(&backup, tot * sizeof(float)));
+  auto restore = [&]() -> int {
+    EK(cudaMemcpyAsync(e->state, backup, tot * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));
+    EK(cudaStreamSynchronize(e->stream));
+    return 0;
+  };
+  EK(cudaMemcpyAsync(backup, e->state, tot * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));
+  if ((r = push_scal(e))) { cudaFree(backup); return r; }
+  std::vector<RunScal> scal0 = e->scal;
+  auto trial = [&](const std::vector<int>& subset, float* ms) -> int {
+    int rr;
+    if ((rr = build_packs(e, subset))) return rr;
+    e->scal = scal0;
+    e->scal_dirty = true;
+    if ((rr = push_scal(e))) return rr;
+    if ((rr = launch(e, 1))) return rr;  // warm-up
+    EK(cudaStreamSynchronize(e->stream));
+    cudaEvent_t a0, a1;
+    EK(cudaEventCreate(&a0));
+    EK(cudaEventCreate(&a1));
+    EK(cudaEventRecord(a0, e->stream));
+    if ((rr = launch(e, steps))) return rr;
+    EK(cudaEventRecord(a1, e->stream));
+    EK(cudaEventSynchronize(a1));
+    EK(cudaEventElapsedTime(ms, a0, a1));
+    cudaEventDestroy(a0);
+    cudaEventDestroy(a1);
+    e->launches += 2;
+    return restore();
+  };
+  e->threads = 1024;
+  const std::vector<int> g0 = e->cls_g;
+  for (size_t c = 0; c < e->cls_n.size() && !r; ++c) {
+    std::vector<int> subset;
+    for (int q = 0; q < e->nruns && (int)subset.size() < 4 * kCl * std::max(1, e->nclusters); ++q)
+      if (e->run_cls[q] == (int)c) subset.push_back(q);
+    float best = 1e30f;
+    int bestG = g0[c];
+    for (int G = 1; G <= kCl && !r; G *= 2) {
+      if (!g_feasible(e->cls_n[c], G)) continue;
+      e->cls_g[c] = G;
+      float ms = 0.f;
+      r = trial(subset, &ms);
+      if (!r && ms < best) { best = ms; bestG = G; }
+    }
+    e->cls_g[c] = bestG;
+  }
+  float best_t = 1e30f;
+  int bt = 1024;
+  for (int T : {1024, 512}) {
+    if (r) break;
+    e->threads = T;
+    float ms = 0.f;
+    r = trial({}, &ms);
+    if (!r && ms < best_t) { best_t = ms; bt = T; }
+  }
+  e->threads = bt;
+  e->scal = scal0;
+  e->scal_dirty = true;
+  cudaFree(backup);
+  if (r) return r;
+  if ((r = build_packs(e, {}))) return r;
+  if (cache_path) {
+    std::ofstream f(cache_path, std::ios::app);
+    for (size_t c = 0; c < e->cls_n.size(); ++c) f << key << " N " << e->cls_n[c] << " " << e->cls_g[c] << "\n";
+    f << key << " threads " << e->threads << "\n";
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -160,6 +160,41 @@ int fen_profile_step(fen_ctx* ctx, int reps, double dt, double* out);
 #define FEN_NOALLOC_MAX_N 1024
 int fen_poisson_pp2d_noalloc(const double* rhs, double* phi, int nx, int ny, double lx, void* stream);
 
+/* ---- Batched ensemble of 2D periodic runs (no counterpart in the reference) ------------
+ * FEN runs one grid per program (solver_mod::advance_solution, solver.f90:333, with the pp
+ * Poisson solver, poisson.f90:416-505).  An ensemble holds `nruns` independent 2D periodic
+ * runs on [0, length]^2, run q on an n[q] x n[q] grid (n = 2^a 3^b, a >= 2) with its own
+ * viscosity, density 1, forcing S_x = forcing_amplitude sin(forcing_wavenumber y) at the
+ * u points, and FEN's constant-CFL time step (CFL = cfl).  Fields are FP32 on the device,
+ * reductions FP64.  One fen_ensemble_advance is ONE persistent kernel launch (captured in a
+ * CUDA graph) that advances every run by nsteps steps.
+ * Host arrays are interiors of n*n doubles, x fastest: u(i,j) at ((i+1) d, (j+1/2) d),
+ * v(i,j) at ((i+1/2) d, (j+1) d), p(i,j) at the cell centres (0-based i, j; d = length/n). */
+typedef struct fen_ensemble fen_ensemble;
+int fen_ensemble_create(int nruns, const int* n, const double* viscosity, double length, double cfl,
+                        double forcing_amplitude, int forcing_wavenumber, fen_ensemble** out);
+int fen_ensemble_destroy(fen_ensemble* ens);
+/* State of one run; p may be NULL (zero).  dv_o restarts at zero, time at zero. */
+int fen_ensemble_upload(fen_ensemble* ens, int run, const double* u, const double* v, const double* p);
+int fen_ensemble_download(fen_ensemble* ens, int run, double* u, double* v, double* p);
+/* set_timestep(U) of every run (navier_stokes.f90:623-665): dt = dt_o = min(cfl d / U, dt_visc). */
+int fen_ensemble_set_timestep(fen_ensemble* ens, double U);
+/* Advance every run by nsteps steps in one launch; *ms = device time (CUDA events). */
+int fen_ensemble_advance(fen_ensemble* ens, int nsteps, double* ms);
+/* out[8] = time, dt, dt_o, maxvel, kinetic energy 1/2 <u^2+v^2>, max div, NaN flag, viscosity. */
+int fen_ensemble_status(fen_ensemble* ens, int run, double* out);
+/* Launch shape: CTA size, the distinct grid sizes (largest first), CTAs per run for each. */
+int fen_ensemble_config(fen_ensemble* ens, int* threads, int* sizes, int* groups, int* nclasses, int* nclusters);
+int fen_ensemble_set_config(fen_ensemble* ens, int threads, const int* groups);
+/* Autotuner: times each feasible CTAs-per-run choice per grid size, then the CTA size, on
+ * the ensemble's own runs (state restored afterwards); caches results in cache_path (may be
+ * NULL) and reuses them when present. */
+int fen_ensemble_tune(fen_ensemble* ens, int steps, const char* cache_path);
+long long fen_ensemble_launches(fen_ensemble* ens);
+/* Dynamic + static shared memory per CTA for an n x n run on `groups` CTAs (0 if invalid);
+ * host-only, no device needed. */
+size_t fen_ensemble_smem_bytes(int n, int groups);
+
 #ifdef __cplusplus
 }
 #endif
