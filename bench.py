@@ -21,7 +21,8 @@ Fortran/MPI/FFTW reference cannot be built on these machines) on rank 0's host c
 At N=1 the line also carries `forms`: the mixed-precision form against the FP64 path on the
 channel workload (throughput of each and the mixed form's relative L2 error after the same
 steps), and the discrete adjoint on 2D decaying turbulence (backward/forward time ratio and
-the gradient's agreement with central differences).  `--no-forms` skips them.
+the gradient's agreement with central differences), and the batched ensemble of 512 2D
+Kolmogorov runs in one persistent launch.  `--no-forms` skips them.
 """
 import argparse
 import json
@@ -301,6 +302,33 @@ def form_adjoint(F, ndir=16, nsteps=500, every=50):
             "workload": "2D decaying turbulence 256^2, nu=2e-3, dt=2e-3, 500 steps, checkpoints every 50, FP64"}
 
 
+def form_ensemble(F, steps=2000, nruns=512, tune_steps=10):
+    """Batched ensemble: 512 independent 2D Kolmogorov runs (N ~ U{64, 96, 128, 192, 256},
+    Re ~ U[50, 500], forcing sin(4y), noise 1e-2, CFL 0.4) advanced `steps` steps in one
+    persistent launch, FP32 with FP64 reductions, tile shapes from the autotuner."""
+    from tests import cases as C
+
+    n, nu, init = C.kolmogorov_ensemble(nruns)
+    e = F.Ensemble(n, nu, length=2 * np.pi, CFL=0.4, forcing=(1.0, 4))
+    for q in range(nruns):
+        e.upload(q, *init(q))
+    e.set_timestep(1.0)
+    t0 = time.perf_counter()
+    cfg = e.tune(steps=tune_steps)
+    tune_s = time.perf_counter() - t0
+    l0 = e.launches()
+    ms = e.advance(steps)
+    launches = e.launches() - l0
+    cells = int(np.sum(n.astype(np.int64) ** 2))
+    st = [e.status(q) for q in range(nruns)]
+    e.destroy()
+    return {"value": round(cells * steps / (ms / 1e3) / 1e6, 3), "unit": "Mcell-steps/s", "ms": round(ms, 3),
+            "runs": nruns, "cells": cells, "steps": steps, "launches": launches, "config": cfg,
+            "tune_s": round(tune_s, 2), "max_maxdiv": max(abs(s["maxdiv"]) for s in st),
+            "any_nan": any(s["nan"] for s in st),
+            "workload": f"{nruns} 2D Kolmogorov runs, N~U{{64..256}}, Re~U[50,500], CFL 0.4, {steps} steps, FP32"}
+
+
 def run_reference(args, name, cfg):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -457,7 +485,8 @@ def main():
             line["cpu_baseline"] = cpu_baseline(cfg_name, cfg)
         if world == 1 and not args.no_forms:
             s.destroy_solver()
-            line["forms"] = {"mixed": form_mixed(F, args.form_steps), "adjoint": form_adjoint(F)}
+            line["forms"] = {"mixed": form_mixed(F, args.form_steps), "adjoint": form_adjoint(F),
+                             "ensemble": form_ensemble(F)}
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()

@@ -53,9 +53,24 @@ constexpr int kCl = 8;                 // CTAs per cluster
 constexpr size_t kSmemLimit = 232448;  // opt-in dynamic shared memory per CTA (227 KB)
 constexpr size_t kSmemReserve = 1024;  // static shared memory of the kernel + slack
 
+// Division by a run-time constant: q = umulhi(n, m) with m = floor(2^32/d) + 1 is exact
+// for n * d < 2^32 (all indices here are below 2^16).
+struct FDiv {
+  unsigned d, m;
+};
+__host__ __device__ inline FDiv make_fdiv(unsigned d) {
+  FDiv f;
+  f.d = d;
+  f.m = (d > 1) ? (unsigned)(0x100000000ull / d) + 1u : 0u;
+  return f;
+}
+__device__ __forceinline__ int fdiv(int n, FDiv f) { return f.d > 1 ? (int)__umulhi((unsigned)n, f.m) : n; }
+
 // One grid size N of the ensemble.
 struct ClassDesc {
   int N, G, M, SR, C, buf;  // rows per CTA M = N/G; spectrum row SR = N/2+1; column block C; buffer size (float2)
+  FDiv fN, fSR, fC, fM, fNP;  // division by N, SR, C, M and the packing pairs N/4 + 1
+  int tabs;                   // 1: tables copied into shared memory (when they fit), 0: read from global
   FFTPlan px, py;           // complex FFT lengths N/2 (x, real packing) and N (y)
   const float2* twx;        // exp(-2 pi i m/(N/2)), m < N/2
   const float2* twn;        // exp(-2 pi i k/N), k <= N/2
@@ -91,24 +106,31 @@ struct EnsArgs {
 
 __host__ __device__ inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
-// Shared-memory footprint of one CTA for grid size N on G CTAs (bytes, dynamic part).
-__host__ __device__ inline size_t smem_bytes(int N, int G, int* buf_out = nullptr) {
+// Shared-memory footprint of one CTA for grid size N on G CTAs (bytes, dynamic part):
+// u, v, p rows with one ghost row each side; three work buffers; the transform twiddles,
+// modified wavenumbers and forcing of this N; eight FP64 reduction slots.
+__host__ __device__ inline int tw_count(int N) { return round_up(N / 2 + (N / 2 + 1) + N, 2); }
+__host__ __device__ inline int tab_count(int N, int G) { return round_up((N / 2 + 1) + N + N / G, 4); }
+__host__ __device__ inline size_t smem_bytes(int N, int G, int* buf_out = nullptr, bool tables = false) {
   const int M = N / G, SR = N / 2 + 1, C = (SR + G - 1) / G;
   const int buf = round_up(M * SR > N * C ? M * SR : N * C, 2);
   if (buf_out) *buf_out = buf;
   const size_t fields = (size_t)round_up(3 * (M + 2) * N, 4) * sizeof(float);
-  return fields + (size_t)3 * buf * sizeof(float2) + 8 * sizeof(double);
+  const size_t tabs = tables ? (size_t)tw_count(N) * sizeof(float2) + (size_t)tab_count(N, G) * sizeof(float) : 0;
+  return fields + (size_t)3 * buf * sizeof(float2) + tabs + 8 * sizeof(double);
 }
 
 struct Carve {
   float *u, *v, *p;
   float2 *X, *Y, *Z;
+  float2 *twx, *twn, *twy;
+  float *lamx, *lamy, *force;
   double* red;
 };
 
 __device__ inline Carve carve(unsigned char* s, const ClassDesc& D) {
   Carve c;
-  const int rows = (D.M + 2) * D.N;
+  const int N = D.N, rows = (D.M + 2) * N;
   c.u = reinterpret_cast<float*>(s);
   c.v = c.u + rows;
   c.p = c.v + rows;
@@ -116,7 +138,23 @@ __device__ inline Carve carve(unsigned char* s, const ClassDesc& D) {
   c.X = b;
   c.Y = b + D.buf;
   c.Z = b + 2 * D.buf;
-  c.red = reinterpret_cast<double*>(b + 3 * D.buf);
+  if (D.tabs) {
+    c.twx = b + 3 * D.buf;
+    c.twn = c.twx + N / 2;
+    c.twy = c.twn + (N / 2 + 1);
+    c.lamx = reinterpret_cast<float*>(c.twx + tw_count(N));
+    c.lamy = c.lamx + (N / 2 + 1);
+    c.force = c.lamy + N;
+    c.red = reinterpret_cast<double*>(c.lamx + tab_count(N, D.G));
+  } else {  // tables stay in global memory (generic pointers; read through L1)
+    c.twx = const_cast<float2*>(D.twx);
+    c.twn = const_cast<float2*>(D.twn);
+    c.twy = const_cast<float2*>(D.twy);
+    c.lamx = const_cast<float*>(D.lamx);
+    c.lamy = const_cast<float*>(D.lamy);
+    c.force = nullptr;  // set per CTA from D.force + r M
+    c.red = reinterpret_cast<double*>(b + 3 * D.buf);
+  }
   return c;
 }
 
@@ -152,6 +190,149 @@ __device__ inline float block_max(float v, float* scratch) {
 
 __device__ inline const double2* tw64(const float2* p) { return reinterpret_cast<const double2*>(p); }
 
+// Twiddle constants of the in-register radix-8/16 DFTs: cos(2 pi m/16), m = 0..15.
+__device__ __forceinline__ float cos16(int m) {
+  switch (m & 15) {
+    case 0: return 1.0f;
+    case 1: case 15: return 0.92387953251128674f;
+    case 2: case 14: return 0.70710678118654752f;
+    case 3: case 13: return 0.38268343236508977f;
+    case 4: case 12: return 0.0f;
+    case 5: case 11: return -0.38268343236508977f;
+    case 6: case 10: return -0.70710678118654752f;
+    default: return -0.92387953251128674f;  // 7, 9
+    case 8: return -1.0f;
+  }
+}
+
+// v * exp(DIR 2 pi i m / R) for a compile-time R | 16 (m known after unrolling).
+template <int DIR, int R>
+__device__ __forceinline__ float2 rot(float2 v, int m) {
+  const int e = (m * (16 / R)) & 15;
+  if (e == 0) return v;
+  if (e == 4) return DIR < 0 ? make_float2(v.y, -v.x) : make_float2(-v.y, v.x);
+  if (e == 8) return make_float2(-v.x, -v.y);
+  if (e == 12) return DIR < 0 ? make_float2(-v.y, v.x) : make_float2(v.y, -v.x);
+  const float c = cos16(e), s = (float)DIR * cos16(e + 12);  // sin(2 pi e/16) = cos(2 pi (e-4)/16)
+  return make_float2(v.x * c - v.y * s, v.x * s + v.y * c);
+}
+
+// In-register DFT of size R in natural order (R = 2, 3, 4, 8, 16); sizes 8 and 16 are
+// A x B compositions: DFT-A over the stride-B subsequences, twiddles w_R^(n2 k1), DFT-B.
+template <int DIR, int R>
+__device__ __forceinline__ void dftr(float2 (&x)[16]);
+template <int DIR, int A, int B>
+__device__ __forceinline__ void dft_comp(float2 (&x)[16]) {
+  float2 y[A * B];
+#pragma unroll
+  for (int n2 = 0; n2 < B; ++n2) {
+    float2 tt[16];
+#pragma unroll
+    for (int n1 = 0; n1 < A; ++n1) tt[n1] = x[B * n1 + n2];
+    dftr<DIR, A>(tt);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) y[n2 * A + k1] = rot<DIR, A * B>(tt[k1], n2 * k1);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < A; ++k1) {
+    float2 tt[16];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) tt[n2] = y[n2 * A + k1];
+    dftr<DIR, B>(tt);
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) x[k1 + A * k2] = tt[k2];
+  }
+}
+template <int DIR, int R>
+__device__ __forceinline__ void dftr(float2 (&x)[16]) {
+  if (R == 2) dft2<DIR>(x[0], x[1]);
+  else if (R == 3) dft3<DIR>(x[0], x[1], x[2]);
+  else if (R == 4) dft4<DIR>(x[0], x[1], x[2], x[3]);
+  else if (R == 8) dft_comp<DIR, 4, 2>(x);
+  else if (R == 16) dft_comp<DIR, 4, 4>(x);
+}
+
+// One radix-R pass of a Stockham FFT over nl lines (element (line l, position p) at
+// buf[l*ls + p*es]); lines fastest over threads, so strided layouts stay bank-conflict free.
+// Ns (product of the earlier radices) is a power of two: radices run 16s, 8, 4, 2, then one 3.
+template <int DIR, int R, int NT>
+__device__ __forceinline__ void fft_pass(const float2* __restrict__ src0, float2* __restrict__ dst0, int work, FDiv fnl,
+                                         int ls, int es, int Ns, int nb, int tstep, const float2* __restrict__ tw) {
+#pragma unroll 1
+  for (int t = threadIdx.x; t < work; t += NT) {
+    const int j = fdiv(t, fnl);
+    const int l = t - j * (int)fnl.d;
+    const int k = j & (Ns - 1);
+    const float2* src = src0 + l * ls;
+    float2* dst = dst0 + l * ls;
+    float2 v[16];
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = src[(j + q * nb) * es];
+    if (Ns > 1) {
+#pragma unroll
+      for (int q = 1; q < R; ++q) {
+        const float2 w = tw[q * k * tstep];
+        v[q] = (DIR < 0) ? cmul(v[q], w) : cmulc(v[q], w);
+      }
+    }
+    dftr<DIR, R>(v);
+    const int o = (j - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; ++q) dst[(o + q * Ns) * es] = v[q];
+  }
+}
+
+// Complex FFT of length P.M on nl lines; returns the buffer holding the result (a or b).
+template <int DIR, int NT>
+__device__ float2* ens_fft(float2* a, float2* b, int nl, FDiv fnl, int ls, int es, const FFTPlan& P, const float2* tw) {
+  const int L = P.M;
+  int Ns = 1;
+  for (int s = 0; s < P.nst; ++s) {
+    const int R = P.R[s];
+    const int nb = L / R, tstep = L / (Ns * R);
+    const int work = nl * nb;
+    switch (R) {
+      case 16: fft_pass<DIR, 16, NT>(a, b, work, fnl, ls, es, Ns, nb, tstep, tw); break;
+      case 8: fft_pass<DIR, 8, NT>(a, b, work, fnl, ls, es, Ns, nb, tstep, tw); break;
+      case 4: fft_pass<DIR, 4, NT>(a, b, work, fnl, ls, es, Ns, nb, tstep, tw); break;
+      case 2: fft_pass<DIR, 2, NT>(a, b, work, fnl, ls, es, Ns, nb, tstep, tw); break;
+      default: fft_pass<DIR, 3, NT>(a, b, work, fnl, ls, es, Ns, nb, tstep, tw); break;
+    }
+    __syncthreads();
+    float2* t = a;
+    a = b;
+    b = t;
+    Ns *= R;
+  }
+  return a;
+}
+
+// Real-FFT packing on a row of shared memory (complex length Mh = N/2, twiddles wN =
+// exp(-2 pi i k/N) in shared memory): the same relations as r2c_post / c2r_pre.
+__device__ __forceinline__ float2 pack_r2c(const float2* Z, int Mh, int k, const float2* wN) {
+  const float2 zk = Z[k == Mh ? 0 : k];
+  const float2 zc = cconj(Z[k == 0 ? 0 : Mh - k]);
+  const float2 E = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+  const float2 Dd = csub(zk, zc);
+  const float2 O = make_float2(0.5f * Dd.y, -0.5f * Dd.x);
+  return cadd(E, cmul(wN[k], O));
+}
+__device__ __forceinline__ float2 pack_c2r(float2 xk, float2 xmk, int k, const float2* wN) {
+  if (k == 0) { xk.y = 0.f; xmk.y = 0.f; }
+  const float2 b = cconj(xmk);
+  const float2 s = cadd(xk, b);
+  const float2 d = cmulc(csub(xk, b), wN[k]);
+  return make_float2(s.x - d.y, s.y + d.x);
+}
+
+// Elements handled per thread per batch: loads of a batch are issued before any use, so
+// their latencies (HBM for dv_o, distributed shared memory for the all-to-alls) overlap.
+template <int NT>
+struct Batch {
+  static constexpr int kCells = (NT >= 1024) ? 9 : 18;
+  static constexpr int kElems = (NT >= 1024) ? 5 : 10;
+};
+
 template <int NT>
 __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, int q, cg::cluster_group& cl,
                          unsigned char* smem, double* s_sc, float* s_f, double* s_rd, float* s_rf) {
@@ -169,6 +350,7 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
   auto pf = [&](float* ptr, int g) -> float* { return G == 1 ? ptr : cl.map_shared_rank(ptr, base + g); };
   auto p2 = [&](float2* ptr, int g) -> float2* { return G == 1 ? ptr : cl.map_shared_rank(ptr, base + g); };
   auto pd = [&](double* ptr, int g) -> double* { return G == 1 ? ptr : cl.map_shared_rank(ptr, base + g); };
+  constexpr int CPT = Batch<NT>::kCells, EPT = Batch<NT>::kElems;
 
   const size_t NN = (size_t)N * N;
   float* gu = a.state + (active ? a.run_off[run] : 0);
@@ -176,11 +358,12 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
   float* gp = gv + NN;
   float* gdx = gp + NN;
   float* gdy = gdx + NN;
+  const FDiv fN = D.fN;
 
   // ---- load the CTA's rows (with one ghost row each side) ----
   const int rows = (M + 2) * N;
   for (int t = threadIdx.x; t < rows; t += NT) {
-    const int mm = t / N, i = t - mm * N;
+    const int mm = fdiv(t, fN), i = t - mm * N;
     int jg = r * M + mm - 1;
     jg = jg < 0 ? jg + N : (jg >= N ? jg - N : jg);
     float uu = 0.f, vv = 0.f, pp = 0.f;
@@ -192,6 +375,18 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
     S.u[t] = uu;
     S.v[t] = vv;
     S.p[t] = pp;
+  }
+  if (D.tabs) {
+    for (int t = threadIdx.x; t < N / 2; t += NT) S.twx[t] = D.twx[t];
+    for (int t = threadIdx.x; t <= N / 2; t += NT) {
+      S.twn[t] = D.twn[t];
+      S.lamx[t] = D.lamx[t];
+    }
+    for (int t = threadIdx.x; t < N; t += NT) {
+      S.twy[t] = D.twy[t];
+      S.lamy[t] = D.lamy[t];
+    }
+    for (int t = threadIdx.x; t < M; t += NT) S.force[t] = D.force[r * M + t];
   }
   if (threadIdx.x == 0) {
     RunScal rs;
@@ -215,6 +410,7 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
   float* Zf = reinterpret_cast<float*>(S.Z);
   const int rp = (r + 1) % G, rm = (r - 1 + G) % G;
   const int c0 = r * C, Cr = max(0, min(C, SR - c0));
+  const float* force = D.tabs ? S.force : D.force + r * M;
 
   for (int step = 0; step < a.nsteps; ++step) {
     // ---- update_timestep (constant CFL), FP64 ----
@@ -225,44 +421,59 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
       if (dt > 1.1 * dt_o) dt = 1.1 * dt_o;
       s_sc[0] = dt;
       s_sc[1] = dt_o;
+      const float rf = (float)dt / (float)dt_o;  // the FP32 stencils take A, B and 1/dt in FP32
       s_f[0] = (float)dt;
-      s_f[1] = (float)(1.0 + 0.5 * dt / dt_o);
-      s_f[2] = (float)(-0.5 * dt / dt_o);
-      s_f[3] = (float)(1.0 / dt);
+      s_f[1] = 1.0f + 0.5f * rf;
+      s_f[2] = -0.5f * rf;
+      s_f[3] = 1.0f / (float)dt;
     }
     __syncthreads();
     const float dt = s_f[0], A = s_f[1], B = s_f[2], rdt = s_f[3];
 
     // ---- predictor: u* -> X, v* -> Y (FP32), dv_o streamed from/to HBM ----
-    for (int t = threadIdx.x; t < cells; t += NT) {
-      const int m = t / N, i = t - m * N;
-      const int ip = (i + 1 == N) ? 1 - N : 1;
-      const int im = (i == 0) ? N - 1 : -1;
-      const int c = t + N;
-      const float* U = S.u;
-      const float* V = S.v;
-      const float* Pp = S.p;
-      const float uc = U[c], uip = U[c + ip], uim = U[c + im], ujp = U[c + N], ujm = U[c - N], uimjp = U[c + N + im];
-      const float vc = V[c], vip = V[c + ip], vim = V[c + im], vjp = V[c + N], vjm = V[c - N], vipjm = V[c - N + ip];
-      const int jg = r * M + m;
-      // u: -(d(uu)/dx + d(uv)/dy) + nu lap(u) + S_x      (navier_stokes.f90:297-323, fields.f90:326-329)
-      const float fe = (uip + uc) * (uip + uc), fw = (uc + uim) * (uc + uim);
-      const float cn = (ujp + uc) * (vip + vc), cs = (uc + ujm) * (vipjm + vjm);
-      const float dvx = -((fe - fw) + (cn - cs)) * q4 + mu * (((uip + uim) + (ujp + ujm)) - 4.0f * uc) * id2 + __ldg(D.force + jg);
-      // v: -(d(uv)/dx + d(vv)/dy) + nu lap(v)
-      const float cw = (uimjp + uim) * (vc + vim);
-      const float fn = (vjp + vc) * (vjp + vc), fs = (vc + vjm) * (vc + vjm);
-      const float dvy = -((cn - cw) + (fn - fs)) * q4 + mu * (((vip + vim) + (vjp + vjm)) - 4.0f * vc) * id2;
-      float ox = 0.f, oy = 0.f;
-      if (active) {
-        const size_t gi = (size_t)jg * N + i;
-        ox = gdx[gi];
-        oy = gdy[gi];
-        gdx[gi] = dvx;
-        gdy[gi] = dvy;
+    for (int b0 = 0; b0 < cells; b0 += CPT * NT) {
+      float ox[CPT], oy[CPT];
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        ox[k] = 0.f;
+        oy[k] = 0.f;
+        if (active && t < cells) {
+          const size_t gi = (size_t)r * M * N + t;
+          ox[k] = gdx[gi];
+          oy[k] = gdy[gi];
+        }
       }
-      Xf[t] = uc + dt * (-(Pp[c + ip] - Pp[c]) * idx + A * dvx + B * ox);
-      Yf[t] = vc + dt * (-(Pp[c + N] - Pp[c]) * idx + A * dvy + B * oy);
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < cells) {
+          const int m = fdiv(t, fN), i = t - m * N;
+          const int ip = (i + 1 == N) ? 1 - N : 1;
+          const int im = (i == 0) ? N - 1 : -1;
+          const int c = t + N;
+          const float* U = S.u;
+          const float* V = S.v;
+          const float* Pp = S.p;
+          const float uc = U[c], uip = U[c + ip], uim = U[c + im], ujp = U[c + N], ujm = U[c - N], uimjp = U[c + N + im];
+          const float vc = V[c], vip = V[c + ip], vim = V[c + im], vjp = V[c + N], vjm = V[c - N], vipjm = V[c - N + ip];
+          // u: -(d(uu)/dx + d(uv)/dy) + nu lap(u) + S_x      (navier_stokes.f90:297-323, fields.f90:326-329)
+          const float fe = (uip + uc) * (uip + uc), fw = (uc + uim) * (uc + uim);
+          const float cn = (ujp + uc) * (vip + vc), cs = (uc + ujm) * (vipjm + vjm);
+          const float dvx = -((fe - fw) + (cn - cs)) * q4 + mu * (((uip + uim) + (ujp + ujm)) - 4.0f * uc) * id2 + force[m];
+          // v: -(d(uv)/dx + d(vv)/dy) + nu lap(v)
+          const float cw = (uimjp + uim) * (vc + vim);
+          const float fn = (vjp + vc) * (vjp + vc), fs = (vc + vjm) * (vc + vjm);
+          const float dvy = -((cn - cw) + (fn - fs)) * q4 + mu * (((vip + vim) + (vjp + vjm)) - 4.0f * vc) * id2;
+          if (active) {
+            const size_t gi = (size_t)r * M * N + t;
+            gdx[gi] = dvx;
+            gdy[gi] = dvy;
+          }
+          Xf[t] = uc + dt * (-(Pp[c + ip] - Pp[c]) * idx + A * dvx + B * ox[k]);
+          Yf[t] = vc + dt * (-(Pp[c + N] - Pp[c]) * idx + A * dvy + B * oy[k]);
+        }
+      }
     }
     gsync();  // B1: v* rows visible to the next CTA
 
@@ -271,7 +482,7 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
       const float* Yprev = pf(Yf, rm);
       const float sc = idx * rdt;
       for (int t = threadIdx.x; t < cells; t += NT) {
-        const int m = t / N, i = t - m * N;
+        const int m = fdiv(t, fN), i = t - m * N;
         const int im = (i == 0) ? N - 1 : -1;
         const float us = Xf[t], usm = Xf[t + im], vs = Yf[t];
         const float vsm = (m > 0) ? Yf[t - N] : Yprev[(M - 1) * N + i];
@@ -283,18 +494,18 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
     __syncthreads();
 
     // ---- r2c along x: complex FFT of length N/2 on the packed rows, then unpacking ----
-    float2* SPEC = smem_fft<-1, float2>(S.Z, S.X, M, SR, 1, D.px, tw64(D.twx));
+    float2* SPEC = ens_fft<-1, NT>(S.Z, S.X, M, D.fM, SR, 1, D.px, S.twx);
     for (int t = threadIdx.x; t < M * npair; t += NT) {
-      const int m = t / npair, k = t - m * npair;
+      const int m = fdiv(t, D.fNP), k = t - m * npair;
       float2* row = SPEC + m * SR;
       if (k == 0) {
-        const float2 x0 = r2c_post(row, 1, Mh, 0, tw64(D.twn));
-        const float2 xm = r2c_post(row, 1, Mh, Mh, tw64(D.twn));
+        const float2 x0 = pack_r2c(row, Mh, 0, S.twn);
+        const float2 xm = pack_r2c(row, Mh, Mh, S.twn);
         row[0] = x0;
         row[Mh] = xm;
       } else {
-        const float2 xa = r2c_post(row, 1, Mh, k, tw64(D.twn));
-        const float2 xb = r2c_post(row, 1, Mh, Mh - k, tw64(D.twn));
+        const float2 xa = pack_r2c(row, Mh, k, S.twn);
+        const float2 xb = pack_r2c(row, Mh, Mh - k, S.twn);
         row[k] = xa;
         row[Mh - k] = xb;
       }
@@ -304,23 +515,34 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
     // ---- all-to-all: gather the column block [c0, c0+Cr) of every row into T (= Y) ----
     float2* T = S.Y;
     float2* F = (SPEC == S.Z) ? S.X : S.Z;
-    for (int t = threadIdx.x; t < N * C; t += NT) {
-      const int y = t / C, cc = t - y * C;
-      float2 val = make_float2(0.f, 0.f);
-      if (cc < Cr) {
-        const int g = y / M, m = y - g * M;
-        val = p2(SPEC, g)[m * SR + c0 + cc];
+    for (int b0 = 0; b0 < N * C; b0 += EPT * NT) {
+      float2 val[EPT];
+#pragma unroll
+      for (int k = 0; k < EPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        val[k] = make_float2(0.f, 0.f);
+        if (t < N * C) {
+          const int y = fdiv(t, D.fC), cc = t - y * C;
+          if (cc < Cr) {
+            const int g = fdiv(y, D.fM), m = y - g * M;
+            val[k] = p2(SPEC, g)[m * SR + c0 + cc];
+          }
+        }
       }
-      T[t] = val;
+#pragma unroll
+      for (int k = 0; k < EPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < N * C) T[t] = val[k];
+      }
     }
     __syncthreads();
     // ---- y: forward FFT, divide by lam_x + lam_y (zero mode -> 0), inverse FFT ----
-    float2* R1 = smem_fft<-1, float2>(T, F, C, 1, C, D.py, tw64(D.twy));
+    float2* R1 = ens_fft<-1, NT>(T, F, C, D.fC, 1, C, D.py, S.twy);
     for (int t = threadIdx.x; t < N * C; t += NT) {
-      const int y = t / C, cc = t - y * C;
+      const int y = fdiv(t, D.fC), cc = t - y * C;
       if (cc < Cr) {
         const int kx = c0 + cc;
-        const float lam = __ldg(D.lamx + kx) + __ldg(D.lamy + y);
+        const float lam = S.lamx[kx] + S.lamy[y];
         const float s = (kx == 0 && y == 0) ? 0.f : D.inv_nn / lam;
         float2 z = R1[t];
         z.x *= s;
@@ -329,48 +551,60 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
       }
     }
     __syncthreads();
-    float2* R2 = smem_fft<1, float2>(R1, (R1 == T) ? F : T, C, 1, C, D.py, tw64(D.twy));
+    float2* R2 = ens_fft<1, NT>(R1, (R1 == T) ? F : T, C, D.fC, 1, C, D.py, S.twy);
     gsync();  // B3: column solves complete; row spectra no longer read
 
     // ---- all-to-all back: rows of this CTA from every column owner, into SPEC ----
-    for (int t = threadIdx.x; t < M * SR; t += NT) {
-      const int m = t / SR, cc = t - m * SR;
-      const int o = cc / C, cl_ = cc - o * C;
-      SPEC[m * SR + cc] = p2(R2, o)[(r * M + m) * C + cl_];
+    for (int b0 = 0; b0 < M * SR; b0 += EPT * NT) {
+      float2 val[EPT];
+#pragma unroll
+      for (int k = 0; k < EPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < M * SR) {
+          const int m = fdiv(t, D.fSR), cc = t - m * SR;
+          const int o = fdiv(cc, D.fC), cl_ = cc - o * C;
+          val[k] = p2(R2, o)[(r * M + m) * C + cl_];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < EPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < M * SR) SPEC[t] = val[k];
+      }
     }
     __syncthreads();
     // ---- c2r along x: packing then inverse complex FFT of length N/2 ----
     for (int t = threadIdx.x; t < M * npair; t += NT) {
-      const int m = t / npair, k = t - m * npair;
+      const int m = fdiv(t, D.fNP), k = t - m * npair;
       float2* row = SPEC + m * SR;
       if (k == 0) {
-        row[0] = c2r_pre(row[0], row[Mh], Mh, 0, tw64(D.twn));
+        row[0] = pack_c2r(row[0], row[Mh], 0, S.twn);
       } else {
         const float2 xa = row[k], xb = row[Mh - k];
-        const float2 za = c2r_pre(xa, xb, Mh, k, tw64(D.twn));
-        const float2 zb = c2r_pre(xb, xa, Mh, Mh - k, tw64(D.twn));
+        const float2 za = pack_c2r(xa, xb, k, S.twn);
+        const float2 zb = pack_c2r(xb, xa, Mh - k, S.twn);
         row[k] = za;
         if (Mh - k != k) row[Mh - k] = zb;
       }
     }
     __syncthreads();
     float2* W3 = (SPEC != S.X && R2 != S.X) ? S.X : ((SPEC != S.Y && R2 != S.Y) ? S.Y : S.Z);
-    float2* PHI = smem_fft<1, float2>(SPEC, W3, M, SR, 1, D.px, tw64(D.twx));
+    float2* PHI = ens_fft<1, NT>(SPEC, W3, M, D.fM, SR, 1, D.px, S.twx);
     const float* Phf = reinterpret_cast<const float*>(PHI);
     {  // FP64 sum of phi for the mean removal (poisson.f90:491-503)
       float part = 0.f;
       for (int t = threadIdx.x; t < cells; t += NT) {
-        const int m = t / N, i = t - m * N;
+        const int m = fdiv(t, fN), i = t - m * N;
         part += Phf[m * 2 * SR + i];
       }
       const double s = block_sum<NT>((double)part, s_rd);
       if (threadIdx.x == 0) S.red[0] = s;
     }
     gsync();  // B4: phi and the partial sums visible
-    if (threadIdx.x == 0) {
-      double s = 0.0;
-      for (int g = 0; g < G; ++g) s += pd(S.red, g)[0];
-      s_f[4] = (float)(s / ((double)N * N));
+    if (threadIdx.x < 32) {  // lanes read the G partial sums; fixed-order butterfly sum
+      double s = (threadIdx.x < G) ? pd(S.red, threadIdx.x)[0] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (threadIdx.x == 0) s_f[4] = (float)(s / ((double)N * N));
     }
     __syncthreads();
 
@@ -381,7 +615,7 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
       float vmax = 0.f;
       int bad = 0;
       for (int t = threadIdx.x; t < cells; t += NT) {
-        const int m = t / N, i = t - m * N;
+        const int m = fdiv(t, fN), i = t - m * N;
         const int ip = (i + 1 == N) ? 1 - N : 1;
         const int o = m * 2 * SR + i;
         const float ph = Phf[o], phip = Phf[o + ip];
@@ -404,16 +638,22 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
       }
     }
     gsync();  // B5: corrected rows, maxima visible
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
       double mv = 0.0, bad = 0.0;
-      for (int g = 0; g < G; ++g) {
-        const double* rr = pd(S.red, g);
-        mv = fmax(mv, rr[1]);
-        bad = fmax(bad, rr[2]);
+      if (threadIdx.x < G) {
+        const double* rr = pd(S.red, threadIdx.x);
+        mv = rr[1];
+        bad = rr[2];
       }
-      s_sc[3] = mv;
-      s_sc[2] += s_sc[0];
-      if (bad != 0.0) s_sc[6] = 1.0;
+      for (int o = 16; o > 0; o >>= 1) {
+        mv = fmax(mv, __shfl_xor_sync(0xffffffffu, mv, o));
+        bad = fmax(bad, __shfl_xor_sync(0xffffffffu, bad, o));
+      }
+      if (threadIdx.x == 0) {
+        s_sc[3] = mv;
+        s_sc[2] += s_sc[0];
+        if (bad != 0.0) s_sc[6] = 1.0;
+      }
     }
     // ---- ghost rows from the neighbouring CTAs (periodic in y) ----
     {
@@ -423,17 +663,15 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
       const float* Un = pf(S.u, rp);
       const float* Vn = pf(S.v, rp);
       const float* Pn = pf(S.p, rp);
-      for (int t = threadIdx.x; t < 2 * N; t += NT) {
-        if (t < N) {
-          S.u[t] = Um[M * N + t];
-          S.v[t] = Vm[M * N + t];
-          S.p[t] = Pm[M * N + t];
-        } else {
-          const int i = t - N;
-          S.u[(M + 1) * N + i] = Un[N + i];
-          S.v[(M + 1) * N + i] = Vn[N + i];
-          S.p[(M + 1) * N + i] = Pn[N + i];
-        }
+      for (int t = threadIdx.x; t < N; t += NT) {
+        const float a0 = Um[M * N + t], a1 = Vm[M * N + t], a2 = Pm[M * N + t];
+        const float b0 = Un[N + t], b1 = Vn[N + t], b2 = Pn[N + t];
+        S.u[t] = a0;
+        S.v[t] = a1;
+        S.p[t] = a2;
+        S.u[(M + 1) * N + t] = b0;
+        S.v[(M + 1) * N + t] = b1;
+        S.p[(M + 1) * N + t] = b2;
       }
     }
     __syncthreads();
@@ -443,12 +681,12 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
   {
     float kpart = 0.f, dmax = -INFINITY;
     for (int t = threadIdx.x; t < cells; t += NT) {
-      const int m = t / N, i = t - m * N;
+      const int m = fdiv(t, fN), i = t - m * N;
       const int im = (i == 0) ? N - 1 : -1;
       const int c = t + N;
       const float uu = S.u[c], vv = S.v[c];
       if (active) {
-        const size_t gi = (size_t)(r * M + m) * N + i;
+        const size_t gi = (size_t)r * M * N + t;
         gu[gi] = uu;
         gv[gi] = vv;
         gp[gi] = S.p[c];
@@ -559,13 +797,16 @@ namespace {
       return fen_internal_fail(FEN_ERR_CUDA, (std::string(#x) + ": " + cudaGetErrorString(e_)).c_str()); \
   } while (0)
 
+// Radix schedule of the in-register passes: 16s first, then one 8, 4 or 2, then a 3.
 bool plan_len(int M, FFTPlan& P) {
   P.M = M;
   P.nst = 0;
   int m = M;
-  while (m % 4 == 0) { P.R[P.nst++] = 4; m /= 4; }
-  while (m % 2 == 0) { P.R[P.nst++] = 2; m /= 2; }
-  while (m % 3 == 0) { P.R[P.nst++] = 3; m /= 3; }
+  while (m % 16 == 0) { P.R[P.nst++] = 16; m /= 16; }
+  if (m % 8 == 0) { P.R[P.nst++] = 8; m /= 8; }
+  if (m % 4 == 0) { P.R[P.nst++] = 4; m /= 4; }
+  if (m % 2 == 0) { P.R[P.nst++] = 2; m /= 2; }
+  if (m % 3 == 0) { P.R[P.nst++] = 3; m /= 3; }
   return m == 1 && P.nst <= kMaxStages;
 }
 
@@ -617,6 +858,12 @@ void set_g(ClassDesc& D, int G) {
   int buf = 0;
   smem_bytes(D.N, G, &buf);
   D.buf = buf;
+  D.fN = make_fdiv(D.N);
+  D.fSR = make_fdiv(D.SR);
+  D.fC = make_fdiv(D.C);
+  D.fM = make_fdiv(D.M);
+  D.fNP = make_fdiv(D.N / 4 + 1);
+  D.tabs = smem_bytes(D.N, G, nullptr, true) + kSmemReserve <= kSmemLimit;
 }
 
 const void* kernel_ptr(int threads) {
@@ -641,7 +888,7 @@ int build_packs(fen_ensemble* e, const std::vector<int>& subset) {
         if (e->run_cls[q] == (int)c) runs.push_back(q);
     }
     if (runs.empty()) continue;
-    smem = std::max(smem, smem_bytes(e->cls_n[c], G));
+    smem = std::max(smem, smem_bytes(e->cls_n[c], G, nullptr, e->cls_host[c].tabs != 0));
     for (size_t s = 0; s < runs.size(); s += per) {
       Pack p;
       p.cls = (int)c;
@@ -785,8 +1032,9 @@ int fen_ensemble_create(int nruns, const int* n, const double* viscosity, double
   *out = nullptr;
   for (int q = 0; q < nruns; ++q) {
     FFTPlan P;
-    if (n[q] < 8 || n[q] % 4 != 0 || !plan_len(n[q], P) || !plan_len(n[q] / 2, P))
-      return fen_internal_fail(FEN_ERR_ARG, ("ensemble run " + std::to_string(q) + ": N must be 2^a 3^b, a >= 2, N >= 8").c_str());
+    if (n[q] < 8 || n[q] % 4 != 0 || n[q] % 9 == 0 || !plan_len(n[q], P) || !plan_len(n[q] / 2, P))
+      return fen_internal_fail(FEN_ERR_ARG,
+                               ("ensemble run " + std::to_string(q) + ": N must be 2^a 3^b with a >= 2, b <= 1, N >= 8").c_str());
     if (!(viscosity[q] > 0)) return fen_internal_fail(FEN_ERR_ARG, "viscosity must be positive");
     bool ok = false;
     for (int G = 1; G <= 8; G *= 2) ok = ok || g_feasible(n[q], G);

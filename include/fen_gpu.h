@@ -163,7 +163,7 @@ int fen_poisson_pp2d_noalloc(const double* rhs, double* phi, int nx, int ny, dou
 /* ---- Batched ensemble of 2D periodic runs (no counterpart in the reference) ------------
  * FEN runs one grid per program (solver_mod::advance_solution, solver.f90:333, with the pp
  * Poisson solver, poisson.f90:416-505).  An ensemble holds `nruns` independent 2D periodic
- * runs on [0, length]^2, run q on an n[q] x n[q] grid (n = 2^a 3^b, a >= 2) with its own
+ * runs on [0, length]^2, run q on an n[q] x n[q] grid (n = 2^a 3^b, a >= 2, b <= 1) with its own
  * viscosity, density 1, forcing S_x = forcing_amplitude sin(forcing_wavenumber y) at the
  * u points, and FEN's constant-CFL time step (CFL = cfl).  Fields are FP32 on the device,
  * reductions FP64.  One fen_ensemble_advance is ONE persistent kernel launch (captured in a

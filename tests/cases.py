@@ -151,3 +151,19 @@ def project_pp_2d(u, v, d):
     ph = np.where(lam == 0.0, 0.0, dh / np.where(lam == 0.0, 1.0, lam))
     phi = np.fft.ifft2(ph).real
     return u - (np.roll(phi, -1, axis=1) - phi) / d, v - (np.roll(phi, -1, axis=0) - phi) / d
+
+
+def kolmogorov_ensemble(nruns=512, seed=5, sizes=(64, 96, 128, 192, 256), re_range=(50.0, 500.0), amp=1e-2):
+    """Seeded ensemble of 2D Kolmogorov runs: N ~ U{sizes}, Re ~ U[re_range], nu = 1/Re
+    (PCG64(seed)); the initial velocity of run q is uniform noise in [-amp, amp] from
+    PCG64(seed + q).  Returns (n, nu, init) with init(q) -> (u, v) interiors (N, N)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = rng.choice(np.asarray(sizes), size=nruns)
+    re = rng.uniform(re_range[0], re_range[1], size=nruns)
+
+    def init(q):
+        r = np.random.Generator(np.random.PCG64(seed + q))
+        N = int(n[q])
+        return amp * r.uniform(-1, 1, (N, N)), amp * r.uniform(-1, 1, (N, N))
+
+    return n.astype(np.int32), 1.0 / re, init
