@@ -109,6 +109,9 @@ struct fen_ctx {
   int refine = 0;
   float* d32[3] = {nullptr, nullptr, nullptr};
   float* dvo32[3] = {nullptr, nullptr, nullptr};
+  float* d32l[3] = {nullptr, nullptr, nullptr};    // increment lo (pairs with d32)
+  float* dvo32l[3] = {nullptr, nullptr, nullptr};  // dv_o lo (pairs with dvo32)
+  double* tmp64 = nullptr;                         // FP64 staging of dv_o pairs
   float* S32[3] = {nullptr, nullptr, nullptr};
   int has_S = 0;
   // poisson
@@ -582,6 +585,7 @@ int launch_stage_t(fen_ctx* c, const Stage& s, int first_from_field, const void*
     if (c->mixed) {
       ld = LD_DIVMIX;
       a.fu = (const T*)c->d32[0]; a.fv = (const T*)c->d32[1]; a.fw = (const T*)c->d32[2];
+      a.ful = c->d32l[0]; a.fvl = c->d32l[1]; a.fwl = c->d32l[2];
       a.pu = DFField{c->u32, c->u32l}; a.pv = DFField{c->v32, c->v32l}; a.pw = DFField{c->w32, c->w32l};
     } else {
       a.fu = (const T*)c->us; a.fv = (const T*)c->vs; a.fw = (const T*)c->ws;
@@ -708,24 +712,36 @@ int launch_predictor(fen_ctx* c, const StepScalars* sc) {
     pa.u = DFField{c->u32, c->u32l}; pa.v = DFField{c->v32, c->v32l};
     pa.w = DFField{c->w32, c->w32l}; pa.p = DFField{c->p32, c->p32l};
     pa.du = c->d32[0]; pa.dv = c->d32[1]; pa.dw = c->d32[2];
+    pa.dul = c->d32l[0]; pa.dvl = c->d32l[1]; pa.dwl = c->d32l[2];
     pa.dox = c->dvo32[0]; pa.doy = c->dvo32[1]; pa.doz = c->dvo32[2];
+    pa.doxl = c->dvo32l[0]; pa.doyl = c->dvo32l[1]; pa.dozl = c->dvo32l[2];
     pa.Sx = c->S32[0]; pa.Sy = c->S32[1]; pa.Sz = c->S32[2];
+    const double rhof = rhof_of(c);
+    double id[3], id2[3];
     for (int q = 0; q < 3; ++q) {
-      pa.id[q] = 1.0 / c->d[q];
-      pa.id2[q] = 1.0 / (c->d[q] * c->d[q]);
+      id[q] = 1.0 / c->d[q];
+      id2[q] = 1.0 / (c->d[q] * c->d[q]);
     }
-    pa.mu = c->prm.viscosity;
-    pa.rhof = rhof_of(c);
-    pa.rhof_one = (pa.rhof == 1.0);
-    for (int q = 0; q < 3; ++q) pa.g[q] = c->prm.g[q];
+    if (c->iso)
+      for (int q = 1; q < 3; ++q) { id[q] = id[0]; id2[q] = id2[0]; }
+    F2* qs[3] = {&pa.qx, &pa.qy, &pa.qz};
+    F2* ms[3] = {&pa.mx, &pa.my, &pa.mz};
+    F2* gs[3] = {&pa.gx, &pa.gy, &pa.gz};
+    for (int q = 0; q < 3; ++q) {
+      *qs[q] = split_d(0.25 * id[q]);
+      *ms[q] = split_d(c->prm.viscosity * id2[q] / rhof);
+      *gs[q] = split_d(id[q] / rhof);
+      pa.g[q] = split_d(c->prm.g[q]);
+    }
+    pa.irho = split_d(1.0 / rhof);
     pa.iso = c->iso;
     pa.has_S = c->has_S;
     if (c->dim == 3) k_predictor_df<3><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
     else k_predictor_df<2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
   } else {
     PredArgs<double> pa = pred_args<double>(c);
-    if (c->dim == 3) k_predictor<double, 3><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
-    else k_predictor<double, 2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+    if (c->dim == 3) k_predictor<3><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+    else k_predictor<2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
   }
   c->launches++;
   CK(cudaGetLastError());
@@ -826,8 +842,10 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
   mark();  // 1: predictor
   if (c->mixed) {
     float* f[3] = {c->d32[0], c->d32[1], c->d32[2]};
+    float* fl[3] = {c->d32l[0], c->d32l[1], c->d32l[2]};
     int ids[3] = {FEN_U, FEN_V, FEN_W};
     if ((r = ghost<float>(c, c->dim, f, ids, true))) return r;
+    if ((r = ghost<float>(c, c->dim, fl, ids, true))) return r;
   } else {
     double* f[3] = {c->us, c->vs, c->ws};
     int ids[3] = {FEN_U, FEN_V, FEN_W};
@@ -854,6 +872,7 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
       memset(&ra, 0, sizeof(ra));
       ra.u = DFField{c->u32, c->u32l}; ra.v = DFField{c->v32, c->v32l}; ra.w = DFField{c->w32, c->w32l};
       ra.du = c->d32[0]; ra.dv = c->d32[1]; ra.dw = c->d32[2];
+      ra.dul = c->d32l[0]; ra.dvl = c->d32l[1]; ra.dwl = c->d32l[2];
       ra.phi = c->phi32;
       ra.r = c->res32;
       for (int q = 0; q < 3; ++q) {
@@ -874,6 +893,7 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
     CorrDFArgs ca;
     memset(&ca, 0, sizeof(ca));
     ca.du = c->d32[0]; ca.dv = c->d32[1]; ca.dw = c->d32[2]; ca.phi = c->phi32;
+    ca.dul = c->d32l[0]; ca.dvl = c->d32l[1]; ca.dwl = c->d32l[2];
     ca.dphi = c->refine ? c->dphi32 : nullptr;
     ca.u = DFFieldW{c->u32, c->u32l}; ca.v = DFFieldW{c->v32, c->v32l};
     ca.w = DFFieldW{c->w32, c->w32l}; ca.p = DFFieldW{c->p32, c->p32l};
@@ -1018,8 +1038,9 @@ int fen_ctx_destroy(fen_ctx* c) {
   for (double* b : bufs) if (b) cudaFree(b);
   float* fb[] = {c->u32, c->v32, c->w32, c->p32, c->u32l, c->v32l, c->w32l, c->p32l, c->phi32, c->d32[0],
                  c->d32[1], c->d32[2], c->dvo32[0], c->dvo32[1], c->dvo32[2], c->S32[0], c->S32[1], c->S32[2],
-                 c->dphi32, c->res32};
+                 c->dphi32, c->res32, c->d32l[0], c->d32l[1], c->d32l[2], c->dvo32l[0], c->dvo32l[1], c->dvo32l[2]};
   for (float* b : fb) if (b) cudaFree(b);
+  if (c->tmp64) cudaFree(c->tmp64);
   for (int f = 0; f < 5; ++f) for (int q = 0; q < 6; ++q) if (c->bcval[f][q]) cudaFree(c->bcval[f][q]);
   if (c->specC) cudaFree(c->specC);
   if (c->specR) cudaFree(c->specR);
@@ -1102,9 +1123,11 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
     if ((r = alloc(f, L.total))) { fen_ctx_destroy(c); return r; }
   if (c->mixed) {
     float** fl[] = {&c->u32, &c->v32, &c->w32, &c->p32, &c->u32l, &c->v32l, &c->w32l, &c->p32l, &c->phi32,
-                    &c->d32[0], &c->d32[1], &c->d32[2], &c->dvo32[0], &c->dvo32[1], &c->dvo32[2]};
+                    &c->d32[0], &c->d32[1], &c->d32[2], &c->dvo32[0], &c->dvo32[1], &c->dvo32[2],
+                    &c->d32l[0], &c->d32l[1], &c->d32l[2], &c->dvo32l[0], &c->dvo32l[1], &c->dvo32l[2]};
     for (float** f : fl)
       if ((r = alloc(f, L.total))) { fen_ctx_destroy(c); return r; }
+    if ((r = alloc(&c->tmp64, L.total))) { fen_ctx_destroy(c); return r; }
     if (c->refine && ((r = alloc(&c->dphi32, L.total)) || (r = alloc(&c->res32, L.total)))) { fen_ctx_destroy(c); return r; }
   } else {
     double** fl[] = {&c->phi, &c->us, &c->vs, &c->ws, &c->dvo[0], &c->dvo[1], &c->dvo[2]};
@@ -1140,8 +1163,17 @@ int fen_upload(fen_ctx* c, int f, const double* host) {
     drop_graph(c);
     return c->mixed ? relayout<float>(c, c->S32[f - FEN_S_X], hrw, 0) : relayout<double>(c, c->S[f - FEN_S_X], hrw, 0);
   }
-  if (f >= FEN_DVO_X && f <= FEN_DVO_Z)
-    return c->mixed ? relayout<float>(c, c->dvo32[f - FEN_DVO_X], hrw, 0) : relayout<double>(c, c->dvo[f - FEN_DVO_X], hrw, 0);
+  if (f >= FEN_DVO_X && f <= FEN_DVO_Z) {
+    if (!c->mixed) return relayout<double>(c, c->dvo[f - FEN_DVO_X], hrw, 0);
+    // dv_o is a pair in the mixed form: FP64 staging, then split
+    if ((r = relayout<double>(c, c->tmp64, hrw, 0))) return r;
+    const int grid = std::min(cdiv(c->L.total, 256), 152 * 16);
+    k_split<<<grid, 256, 0, c->stream>>>(c->L.total, c->tmp64, c->dvo32[f - FEN_DVO_X], c->dvo32l[f - FEN_DVO_X]);
+    c->launches++;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+  }
   if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, hrw, 0) : relayout<double>(c, c->phi, hrw, 0);
   double* d = (f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p;
   if ((r = relayout<double>(c, d, hrw, 0))) return r;
@@ -1162,8 +1194,14 @@ int fen_download(fen_ctx* c, int f, double* host) {
     }
     return c->mixed ? relayout<float>(c, c->S32[f - FEN_S_X], host, 1) : relayout<double>(c, c->S[f - FEN_S_X], host, 1);
   }
-  if (f >= FEN_DVO_X && f <= FEN_DVO_Z)
-    return c->mixed ? relayout<float>(c, c->dvo32[f - FEN_DVO_X], host, 1) : relayout<double>(c, c->dvo[f - FEN_DVO_X], host, 1);
+  if (f >= FEN_DVO_X && f <= FEN_DVO_Z) {
+    if (!c->mixed) return relayout<double>(c, c->dvo[f - FEN_DVO_X], host, 1);
+    const int grid = std::min(cdiv(c->L.total, 256), 152 * 16);
+    k_join<<<grid, 256, 0, c->stream>>>(c->L.total, c->dvo32[f - FEN_DVO_X], c->dvo32l[f - FEN_DVO_X], c->tmp64);
+    c->launches++;
+    CK(cudaGetLastError());
+    return relayout<double>(c, c->tmp64, host, 1);
+  }
   if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, host, 1) : relayout<double>(c, c->phi, host, 1);
   double* d = (f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p;
   int r;
@@ -1336,12 +1374,15 @@ int fen_explicit_terms(fen_ctx* c, double* out) {
   const size_t es = c->mixed ? sizeof(float) : sizeof(double);
   std::vector<void*> save(3, nullptr);
   for (int q = 0; q < c->dim; ++q) {
-    CK(cudaMalloc(&save[q], tot * es));
+    CK(cudaMalloc(&save[q], 2 * tot * es));
     void* src = c->mixed ? (void*)c->dvo32[q] : (void*)c->dvo[q];
     CK(cudaMemcpyAsync(save[q], src, tot * es, cudaMemcpyDeviceToDevice, c->stream));
+    if (c->mixed)
+      CK(cudaMemcpyAsync((char*)save[q] + tot * es, c->dvo32l[q], tot * es, cudaMemcpyDeviceToDevice, c->stream));
   }
   StepScalars s = *c->sc_host;
   s.A = 1.0; s.B = 0.0; s.dt = 1.0;
+  s.Ap[0] = 1.0f; s.Ap[1] = 0.0f; s.Bp[0] = 0.0f; s.Bp[1] = 0.0f; s.dtp[0] = 1.0f; s.dtp[1] = 0.0f;
   StepScalars* dsc;
   CK(cudaMalloc((void**)&dsc, sizeof(StepScalars)));
   CK(cudaMemcpyAsync(dsc, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream));
@@ -1359,6 +1400,8 @@ int fen_explicit_terms(fen_ctx* c, double* out) {
           out[(size_t)q * ncell + t++] = h[(size_t)i + (size_t)nxg * ((size_t)j + (size_t)nyg * k)];
     void* dst = c->mixed ? (void*)c->dvo32[q] : (void*)c->dvo[q];
     CK(cudaMemcpyAsync(dst, save[q], tot * es, cudaMemcpyDeviceToDevice, c->stream));
+    if (c->mixed)
+      CK(cudaMemcpyAsync(c->dvo32l[q], (char*)save[q] + tot * es, tot * es, cudaMemcpyDeviceToDevice, c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
   for (int q = 0; q < c->dim; ++q) cudaFree(save[q]);

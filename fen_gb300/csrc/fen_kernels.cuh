@@ -26,112 +26,116 @@ struct PredArgs {
   int iso, has_S, rhof_one, use_dev_dt;
 };
 
-// DELTA = true (mixed form) writes the increment dt*rhs instead of v + dt*rhs.
-template <typename T, int DIM, bool DELTA = false>
-__global__ void __launch_bounds__(256) k_predictor(Layout L, const StepScalars* __restrict__ sc, PredArgs<T> a) {
-  const long long ncell = (long long)L.n0 * L.n1 * L.n2;
-  const T A = (T)sc->A, B = (T)sc->B;
-  const T dt = (T)(a.use_dev_dt ? sc->dt : a.dt_host);
-  const T idx = (T)a.id[0], idy = (T)a.id[1], idz = (T)a.id[2];
-  const T id2x = (T)a.id2[0], id2y = (T)a.id2[1], id2z = (T)a.id2[2];
-  const T mu = (T)a.mu, rhof = (T)a.rhof;
+// FP64 predictor: divergence-form advection (navier_stokes.f90:297-353), diffusion with
+// constant mu (:384-404, fields.f90:326-337), body force (:245-255), pressure gradient
+// (fields.f90:55-58) and the AB2 update with dv_o <- dv (:140-213); one thread per cell.
+// FP64 issue is the bound on GB300, so the arithmetic is arranged to issue few FP64
+// instructions: the edge products that two momentum equations of the same cell share
+// (u v at (i+1/2, j+1/2), u w at (i+1/2, k+1/2), v w at (j+1/2, k+1/2)) are formed once,
+// the factor 1/4 of every product is folded into the differencing scale, each Laplacian is
+// the neighbour sum minus 2*DIM times the centre, and sums use fused multiply-adds.  The
+// result differs from FEN's operation order by rounding only.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_predictor(Layout L, const StepScalars* __restrict__ sc, PredArgs<double> a) {
+  const unsigned n0 = L.n0, n1 = L.n1;
+  const unsigned ncell = n0 * n1 * (unsigned)L.n2;
+  const double A = sc->A, B = sc->B;
+  const double dt = a.use_dev_dt ? sc->dt : a.dt_host;
+  const double idx = a.id[0], idy = a.iso ? a.id[0] : a.id[1], idz = a.iso ? a.id[0] : a.id[2];
+  const double qx = 0.25 * idx, qy = 0.25 * idy, qz = 0.25 * idz;
+  const double irho = a.rhof_one ? 1.0 : 1.0 / a.rhof;
+  // diffusion coefficients mu/rhof/delta^2 per axis (rhof = 1 keeps mu*id2 exactly)
+  const double mx = a.rhof_one ? a.mu * a.id2[0] : a.mu * a.id2[0] / a.rhof;
+  const double my = a.iso ? mx : (a.rhof_one ? a.mu * a.id2[1] : a.mu * a.id2[1] / a.rhof);
+  const double mz = a.iso ? mx : (a.rhof_one ? a.mu * a.id2[2] : a.mu * a.id2[2] / a.rhof);
+  const double gx = idx * irho, gy = idy * irho, gz = idz * irho;
+  const double g0 = a.g[0], g1 = a.g[1], g2 = a.g[2];
   const long long sy = L.sx, sz = L.sp;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long r = t / L.n0;
-    const int j = 1 + (int)(r % L.n1);
-    const int k = 1 + (int)(r / L.n1);
+  const double* __restrict__ U = a.u;
+  const double* __restrict__ V = a.v;
+  const double* __restrict__ W = a.w;
+  const double* __restrict__ P = a.p;
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < ncell; t += gridDim.x * blockDim.x) {
+    const unsigned r = t / n0;
+    const int i = 1 + (int)(t - r * n0);
+    const int j = 1 + (int)(r % n1);
+    const int k = 1 + (int)(r / n1);
     const long long c = L.idx(i, j, kst<DIM>(k));
-    const T* __restrict__ U = a.u;
-    const T* __restrict__ V = a.v;
-    const T* __restrict__ W = a.w;
-    const T uc = U[c], vc = V[c];
-    const T uip = U[c + 1], uim = U[c - 1], ujp = U[c + sy], ujm = U[c - sy];
-    const T vip = V[c + 1], vim = V[c - 1], vjp = V[c + sy], vjm = V[c - sy];
-    // u advection
-    const T q = (T)0.25;
-    T uuip = q * ((uip + uc) * (uip + uc));
-    T uuim = q * ((uim + uc) * (uim + uc));
-    T uvjp = (ujp + uc) * (vip + vc) * q;
-    T uvjm = (uc + ujm) * (V[c + 1 - sy] + vjm) * q;
-    T dvx = -((uuip - uuim) * idx) - (uvjp - uvjm) * idy;
-    // v advection
-    T vuip = (vip + vc) * (ujp + uc) * q;
-    T vuim = (vc + vim) * (U[c - 1 + sy] + uim) * q;
-    T vvjp = q * ((vjp + vc) * (vjp + vc));
-    T vvjm = q * ((vjm + vc) * (vjm + vc));
-    T dvy = -((vuip - vuim) * idx) - (vvjp - vvjm) * idy;
-    T dvz = 0, wc = 0, wkp = 0, wkm = 0;
-    T ukp = 0, ukm = 0, vkp = 0, vkm = 0;
+    const double uc = U[c], uip = U[c + 1], uim = U[c - 1], ujp = U[c + sy], ujm = U[c - sy];
+    const double vc = V[c], vip = V[c + 1], vim = V[c - 1], vjp = V[c + sy], vjm = V[c - sy];
+    const double su_p = uip + uc, su_m = uc + uim, sv_p = vjp + vc, sv_m = vc + vjm;
+    const double uv_pp = (ujp + uc) * (vip + vc);               // (i+1/2, j+1/2)
+    const double uv_pm = (uc + ujm) * (V[c + 1 - sy] + vjm);    // (i+1/2, j-1/2)
+    const double uv_mp = (vc + vim) * (U[c - 1 + sy] + uim);    // (i-1/2, j+1/2)
+    double ax = (su_p * su_p - su_m * su_m) * qx;
+    ax = fma(uv_pp - uv_pm, qy, ax);
+    double ay = (uv_pp - uv_mp) * qx;
+    ay = fma(sv_p * sv_p - sv_m * sv_m, qy, ay);
+    double lu = (uip + uim) + (ujp + ujm), lv = (vip + vim) + (vjp + vjm);
+    double dvz = 0.0, wc = 0.0;
+    double lux = 0.0, lvx = 0.0;
     if (DIM == 3) {
       wc = W[c];
-      const T wip = W[c + 1], wim = W[c - 1], wjp = W[c + sy], wjm = W[c - sy];
-      wkp = W[c + sz]; wkm = W[c - sz];
-      ukp = U[c + sz]; ukm = U[c - sz]; vkp = V[c + sz]; vkm = V[c - sz];
-      T uwkp = (ukp + uc) * (wip + wc) * q;
-      T uwkm = (uc + ukm) * (W[c + 1 - sz] + wkm) * q;
-      dvx = dvx - (uwkp - uwkm) * idz;
-      T vwkp = (vkp + vc) * (wjp + wc) * q;
-      T vwkm = (vc + vkm) * (W[c + sy - sz] + wkm) * q;
-      dvy = dvy - (vwkp - vwkm) * idz;
-      T wuip = (wc + wip) * (uc + ukp) * q;
-      T wuim = (wc + wim) * (uim + U[c - 1 + sz]) * q;
-      T wvjp = (wc + wjp) * (vc + vkp) * q;
-      T wvjm = (wc + wjm) * (vjm + V[c - sy + sz]) * q;
-      T wwkp = (wc + wkp) * (wc + wkp) * q;
-      T wwkm = (wc + wkm) * (wc + wkm) * q;
-      dvz = -((wuip - wuim) * idx) - (wvjp - wvjm) * idy - (wwkp - wwkm) * idz;
-      // w laplacian: the three directions summed before scaling (fields.f90:335-337)
-      const T two = T(2) * wc;
-      T lw;
-      if (a.iso) lw = ((wip - two + wim) + (wjp - two + wjm) + (wkp - two + wkm)) * id2x;
-      else lw = (wip - two + wim) * id2x + (wjp - two + wjm) * id2y + (wkp - two + wkm) * id2z;
-      dvz = dvz + (a.rhof_one ? mu * lw : mu * lw / rhof);
-    }
-    // u, v laplacian (fields.f90:326-334)
-    {
-      const T two = T(2) * uc;
-      T l;
+      const double wip = W[c + 1], wim = W[c - 1], wjp = W[c + sy], wjm = W[c - sy], wkp = W[c + sz], wkm = W[c - sz];
+      const double ukp = U[c + sz], ukm = U[c - sz], vkp = V[c + sz], vkm = V[c - sz];
+      const double uw_pp = (ukp + uc) * (wip + wc);              // (i+1/2, k+1/2)
+      const double uw_pm = (uc + ukm) * (W[c + 1 - sz] + wkm);   // (i+1/2, k-1/2)
+      const double uw_mp = (wc + wim) * (uim + U[c - 1 + sz]);   // (i-1/2, k+1/2)
+      const double vw_pp = (vkp + vc) * (wjp + wc);              // (j+1/2, k+1/2)
+      const double vw_pm = (vc + vkm) * (W[c + sy - sz] + wkm);  // (j+1/2, k-1/2)
+      const double vw_mp = (wc + wjm) * (vjm + V[c - sy + sz]);  // (j-1/2, k+1/2)
+      const double sw_p = wc + wkp, sw_m = wc + wkm;
+      ax = fma(uw_pp - uw_pm, qz, ax);
+      ay = fma(vw_pp - vw_pm, qz, ay);
+      double az = (uw_pp - uw_mp) * qx;
+      az = fma(vw_pp - vw_mp, qy, az);
+      az = fma(sw_p * sw_p - sw_m * sw_m, qz, az);
+      double lw;
       if (a.iso) {
-        l = ((uip - two + uim) + (ujp - two + ujm)) * id2x;
-        if (DIM == 3) l = l + (ukp - two + ukm) * id2x;
+        lw = fma(-6.0, wc, ((wip + wim) + (wjp + wjm)) + (wkp + wkm));
+        dvz = fma(mx, lw, -az);
       } else {
-        l = (uip - two + uim) * id2x + (ujp - two + ujm) * id2y;
-        if (DIM == 3) l = l + (ukp - two + ukm) * id2z;
+        dvz = fma(mx, fma(-2.0, wc, wip + wim), -az);
+        dvz = fma(my, fma(-2.0, wc, wjp + wjm), dvz);
+        dvz = fma(mz, fma(-2.0, wc, wkp + wkm), dvz);
       }
-      dvx = dvx + (a.rhof_one ? mu * l : mu * l / rhof);
+      lu = lu + (ukp + ukm);
+      lv = lv + (vkp + vkm);
+      lux = ukp + ukm;
+      lvx = vkp + vkm;
     }
-    {
-      const T two = T(2) * vc;
-      T l;
-      if (a.iso) {
-        l = ((vip - two + vim) + (vjp - two + vjm)) * id2x;
-        if (DIM == 3) l = l + (vkp - two + vkm) * id2x;
-      } else {
-        l = (vip - two + vim) * id2x + (vjp - two + vjm) * id2y;
-        if (DIM == 3) l = l + (vkp - two + vkm) * id2z;
+    double dvx, dvy;
+    if (a.iso) {
+      dvx = fma(mx, fma(-2.0 * DIM, uc, lu), -ax);
+      dvy = fma(mx, fma(-2.0 * DIM, vc, lv), -ay);
+    } else {
+      dvx = fma(mx, fma(-2.0, uc, uip + uim), -ax);
+      dvx = fma(my, fma(-2.0, uc, ujp + ujm), dvx);
+      dvy = fma(mx, fma(-2.0, vc, vip + vim), -ay);
+      dvy = fma(my, fma(-2.0, vc, vjp + vjm), dvy);
+      if (DIM == 3) {
+        dvx = fma(mz, fma(-2.0, uc, lux), dvx);
+        dvy = fma(mz, fma(-2.0, vc, lvx), dvy);
       }
-      dvy = dvy + (a.rhof_one ? mu * l : mu * l / rhof);
     }
     if (a.has_S) {
-      dvx = dvx + (a.rhof_one ? a.Sx[c] : a.Sx[c] / rhof);
-      dvy = dvy + (a.rhof_one ? a.Sy[c] : a.Sy[c] / rhof);
-      if (DIM == 3) dvz = dvz + (a.rhof_one ? a.Sz[c] : a.Sz[c] / rhof);
+      dvx = fma(a.Sx[c], irho, dvx);
+      dvy = fma(a.Sy[c], irho, dvy);
+      if (DIM == 3) dvz = fma(a.Sz[c], irho, dvz);
     }
-    // pressure gradient (fields.f90:55-58) and the AB2 update (navier_stokes.f90:169-198)
-    const T pc = a.p[c];
-    const T gpx = (a.p[c + 1] - pc) * (a.iso ? idx : idx);
-    const T gpy = (a.p[c + sy] - pc) * (a.iso ? idx : idy);
-    T rx = (a.rhof_one ? -gpx : -gpx / rhof) + A * dvx + B * a.dox[c] + (T)a.g[0];
-    T ry = (a.rhof_one ? -gpy : -gpy / rhof) + A * dvy + B * a.doy[c] + (T)a.g[1];
-    a.us[c] = DELTA ? dt * rx : uc + dt * rx;
-    a.vs[c] = DELTA ? dt * ry : vc + dt * ry;
+    const double pc = P[c];
+    double rx = fma(-gx, P[c + 1] - pc, g0);
+    double ry = fma(-gy, P[c + sy] - pc, g1);
+    rx = fma(A, dvx, fma(B, a.dox[c], rx));
+    ry = fma(A, dvy, fma(B, a.doy[c], ry));
+    a.us[c] = fma(dt, rx, uc);
+    a.vs[c] = fma(dt, ry, vc);
     a.dox[c] = dvx;
     a.doy[c] = dvy;
     if (DIM == 3) {
-      const T gpz = (a.p[c + sz] - pc) * (a.iso ? idx : idz);
-      T rz = (a.rhof_one ? -gpz : -gpz / rhof) + A * dvz + B * a.doz[c] + (T)a.g[2];
-      a.ws[c] = DELTA ? dt * rz : wc + dt * rz;
+      double rz = fma(-gz, P[c + sz] - pc, g2);
+      rz = fma(A, dvz, fma(B, a.doz[c], rz));
+      a.ws[c] = fma(dt, rz, wc);
       a.doz[c] = dvz;
     }
   }
@@ -159,7 +163,8 @@ struct LineArgs {
   long long out_line, out_pos, out_outer;
   // fields (LD_FIELD / LD_DIV / ST_FIELD)
   Layout L;
-  const T *fu, *fv, *fw;  // predicted velocity for LD_DIV (the FP32 increment for LD_DIVMIX)
+  const T *fu, *fv, *fw;  // predicted velocity for LD_DIV (the increment's hi part for LD_DIVMIX)
+  const float *ful, *fvl, *fwl;  // LD_DIVMIX: the increment's lo part
   DFField pu, pv, pw;     // pair velocity of the mixed form (LD_DIVMIX)
   F2 idp[3];              // 1/delta per axis as float pairs (LD_DIVMIX)
   const T* fsrc;          // LD_FIELD source
@@ -237,6 +242,7 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
           else if (LD == LD_DIV) x = div_at<T, DIM>(a, i + 1, j, k) * (T)a.sc->rho_over_dt;
           else {
             const F2 dd = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
+                                      a.ful, a.fvl, a.fwl,
                                       a.idp, i + 1, j, k);
             x = (T)(dd.hi + dd.lo) * (T)a.sc->rho_over_dt;
           }
@@ -417,35 +423,58 @@ struct ThomasArgs {
   int form3;
 };
 
+// Elimination arithmetic: r - a d as one fused multiply-add, then the row factor.
 template <typename V> struct ThomasOps;
 template <> struct ThomasOps<double> {
-  static __device__ __forceinline__ double sub_amul(double r, double a, double d) { return __dsub_rn(r, __dmul_rn(a, d)); }
+  static __device__ __forceinline__ double sub_amul(double r, double a, double d) { return fma(-a, d, r); }
   static __device__ __forceinline__ double mul(double r, double f) { return __dmul_rn(r, f); }
   static __device__ __forceinline__ double div(double r, double f) { return __ddiv_rn(r, f); }
   static __device__ __forceinline__ double zero() { return 0.0; }
 };
 template <> struct ThomasOps<double2> {
   static __device__ __forceinline__ double2 sub_amul(double2 r, double a, double2 d) {
-    return make_double2(__dsub_rn(r.x, __dmul_rn(a, d.x)), __dsub_rn(r.y, __dmul_rn(a, d.y)));
+    return make_double2(fma(-a, d.x, r.x), fma(-a, d.y, r.y));
   }
   static __device__ __forceinline__ double2 mul(double2 r, double f) { return make_double2(__dmul_rn(r.x, f), __dmul_rn(r.y, f)); }
   static __device__ __forceinline__ double2 div(double2 r, double f) { return make_double2(__ddiv_rn(r.x, f), __ddiv_rn(r.y, f)); }
   static __device__ __forceinline__ double2 zero() { return make_double2(0.0, 0.0); }
 };
 
+// FP32 <-> FP64 conversions on the integer pipe.  GB300 issues FP64 at 1/64 of the FP32
+// rate and its conversion instructions share that pipe, so the mixed form's tridiagonal
+// solve (FP32 storage, FP64 elimination) widens and narrows by rewriting the IEEE fields:
+// exact widening, round-to-nearest-even narrowing.  Zero, subnormal, infinite and NaN
+// values (and results outside the normal FP32 range) take the hardware conversion.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ex = u & 0x7F800000u;
+  if (ex == 0u || ex == 0x7F800000u) return (double)f;
+  const unsigned hi = (u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + 0x38000000u);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned e = (hi >> 20) & 0x7FFu;
+  if (e < 897u || e > 1150u) return (float)d;  // FP32 exponent 1..254 only
+  unsigned f = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+  const unsigned rem = lo & 0x1FFFFFFFu;
+  if (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) f += 1u;  // carries into the exponent
+  return __uint_as_float(f);
+}
+
 // VS is the storage type (float/float2 in the mixed form), VC the FP64 compute type.
 template <typename VS, typename VC>
 __device__ __forceinline__ VC tconv(VS v);
 template <> __device__ __forceinline__ double tconv<double, double>(double v) { return v; }
 template <> __device__ __forceinline__ double2 tconv<double2, double2>(double2 v) { return v; }
-template <> __device__ __forceinline__ double tconv<float, double>(float v) { return (double)v; }
-template <> __device__ __forceinline__ double2 tconv<float2, double2>(float2 v) { return make_double2(v.x, v.y); }
+template <> __device__ __forceinline__ double tconv<float, double>(float v) { return widen(v); }
+template <> __device__ __forceinline__ double2 tconv<float2, double2>(float2 v) { return make_double2(widen(v.x), widen(v.y)); }
 template <typename VC, typename VS>
 __device__ __forceinline__ VS tback(VC v);
 template <> __device__ __forceinline__ double tback<double, double>(double v) { return v; }
 template <> __device__ __forceinline__ double2 tback<double2, double2>(double2 v) { return v; }
-template <> __device__ __forceinline__ float tback<double, float>(double v) { return (float)v; }
-template <> __device__ __forceinline__ float2 tback<double2, float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
+template <> __device__ __forceinline__ float tback<double, float>(double v) { return narrow(v); }
+template <> __device__ __forceinline__ float2 tback<double2, float2>(double2 v) { return make_float2(narrow(v.x), narrow(v.y)); }
 
 template <typename VS, typename VC>
 __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
@@ -695,6 +724,12 @@ static __global__ void k_prologue(StepScalars* sc, int constant_cfl, double cfl,
   sc->B = -0.5 * dt / sc->dt_o;
   sc->rho_over_dt = density / dt;
   sc->dt_over_rhof = dt / rhof;
+  const double v[4] = {dt, sc->A, sc->B, sc->rho_over_dt};
+  float* dst[4] = {sc->dtp, sc->Ap, sc->Bp, sc->rdtp};
+  for (int q = 0; q < 4; ++q) {
+    dst[q][0] = (float)v[q];
+    dst[q][1] = (float)(v[q] - (double)dst[q][0]);
+  }
 }
 
 // Tabulated scale/lam of the all-periodic spectral divide with the SOLVE kernel's formula

@@ -51,123 +51,6 @@ __device__ __forceinline__ float dfd(const DFField& A, long long ca, long long c
   return (A.hi[ca] - A.hi[cb]) + (A.lo[ca] - A.lo[cb]);
 }
 
-// ------------------------------------------------------------------------------------
-// Predictor (mixed): writes the increment dt * rhs (FP32) and dv_o (FP32).
-// ------------------------------------------------------------------------------------
-struct PredDFArgs {
-  DFField u, v, w, p;
-  float *du, *dv, *dw;
-  float *dox, *doy, *doz;
-  const float *Sx, *Sy, *Sz;
-  double id[3], id2[3];
-  double mu, rhof, g[3];
-  int iso, has_S, rhof_one;
-};
-
-template <int DIM>
-__global__ void __launch_bounds__(256) k_predictor_df(Layout L, const StepScalars* __restrict__ sc, PredDFArgs a) {
-  const long long ncell = (long long)L.n0 * L.n1 * L.n2;
-  const float A = (float)sc->A, B = (float)sc->B, dt = (float)sc->dt;
-  const float idx = (float)a.id[0], idy = (float)a.id[1], idz = (float)a.id[2];
-  const float id2x = (float)a.id2[0], id2y = (float)a.id2[1], id2z = (float)a.id2[2];
-  const float mu = (float)a.mu, rhof = (float)a.rhof;
-  const float qx = 0.25f * idx, qy = 0.25f * idy, qz = 0.25f * idz;
-  const long long sy = L.sx, sz = L.sp;
-  const DFField U = a.u, V = a.v, W = a.w, P = a.p;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long r = t / L.n0;
-    const int j = 1 + (int)(r % L.n1);
-    const int k = 1 + (int)(r / L.n1);
-    const long long c = L.idx(i, j, kst<DIM>(k));
-    const long long ip = c + 1, im = c - 1, jp = c + sy, jm = c - sy;
-    // ---- u: -(d(uu)/dx + d(uv)/dy [+ d(uw)/dz]) in difference form
-    const float u_c = U.hi[c], u_ip = U.hi[ip], u_im = U.hi[im], u_jp = U.hi[jp], u_jm = U.hi[jm];
-    const float v_c = V.hi[c], v_ip = V.hi[ip], v_im = V.hi[im], v_jp = V.hi[jp], v_jm = V.hi[jm];
-    float dvx = -(dfd(U, ip, im) * (u_ip + 2.0f * u_c + u_im)) * qx;
-    {
-      const float a1 = u_jp + u_c, b2 = V.hi[ip - sy] + v_jm;
-      const float db = dfd(V, ip, ip - sy) + dfd(V, c, jm);
-      dvx = dvx - (a1 * db + dfd(U, jp, jm) * b2) * qy;
-    }
-    // ---- v
-    float dvy;
-    {
-      const float a1 = v_ip + v_c, b2 = U.hi[im + sy] + u_im;
-      const float db = dfd(U, jp, im + sy) + dfd(U, c, im);
-      dvy = -((a1 * db + dfd(V, ip, im) * b2) * qx);
-    }
-    dvy = dvy - (dfd(V, jp, jm) * (v_jp + 2.0f * v_c + v_jm)) * qy;
-    float dvz = 0.0f;
-    float lux_z = 0.0f, lvy_z = 0.0f;
-    if (DIM == 3) {
-      const long long kp = c + sz, km = c - sz;
-      const float w_c = W.hi[c], w_ip = W.hi[ip], w_im = W.hi[im], w_jp = W.hi[jp], w_jm = W.hi[jm];
-      const float w_kp = W.hi[kp], w_km = W.hi[km];
-      const float u_kp = U.hi[kp], v_kp = V.hi[kp];
-      {  // d(uw)/dz for u
-        const float a1 = u_kp + u_c, b2 = W.hi[ip - sz] + W.hi[km];
-        const float db = dfd(W, ip, ip - sz) + dfd(W, c, km);
-        dvx = dvx - (a1 * db + dfd(U, kp, km) * b2) * qz;
-      }
-      {  // d(vw)/dz for v
-        const float a1 = v_kp + v_c, b2 = W.hi[jp - sz] + W.hi[km];
-        const float db = dfd(W, jp, jp - sz) + dfd(W, c, km);
-        dvy = dvy - (a1 * db + dfd(V, kp, km) * b2) * qz;
-      }
-      {  // w terms: d(wu)/dx, d(wv)/dy, d(ww)/dz
-        const float a1x = w_c + w_ip, b2x = u_im + U.hi[im + sz];
-        const float dbx = dfd(U, c, im) + dfd(U, kp, im + sz);
-        const float a1y = w_c + w_jp, b2y = v_jm + V.hi[jm + sz];
-        const float dby = dfd(V, c, jm) + dfd(V, kp, jm + sz);
-        dvz = -((a1x * dbx + dfd(W, ip, im) * b2x) * qx) - (a1y * dby + dfd(W, jp, jm) * b2y) * qy -
-              (dfd(W, kp, km) * (w_kp + 2.0f * w_c + w_km)) * qz;
-        // w laplacian (fields.f90:335-337)
-        const float lx = dfd(W, ip, c) - dfd(W, c, im);
-        const float ly = dfd(W, jp, c) - dfd(W, c, jm);
-        const float lz = dfd(W, kp, c) - dfd(W, c, km);
-        const float lw = a.iso ? ((lx + ly) + lz) * id2x : lx * id2x + ly * id2y + lz * id2z;
-        dvz = dvz + (a.rhof_one ? mu * lw : mu * lw / rhof);
-      }
-      lux_z = dfd(U, kp, c) - dfd(U, c, km);
-      lvy_z = dfd(V, kp, c) - dfd(V, c, km);
-    }
-    {
-      const float lx = dfd(U, ip, c) - dfd(U, c, im);
-      const float ly = dfd(U, jp, c) - dfd(U, c, jm);
-      float l = a.iso ? (lx + ly) * id2x : lx * id2x + ly * id2y;
-      if (DIM == 3) l = l + lux_z * (a.iso ? id2x : id2z);
-      dvx = dvx + (a.rhof_one ? mu * l : mu * l / rhof);
-    }
-    {
-      const float lx = dfd(V, ip, c) - dfd(V, c, im);
-      const float ly = dfd(V, jp, c) - dfd(V, c, jm);
-      float l = a.iso ? (lx + ly) * id2x : lx * id2x + ly * id2y;
-      if (DIM == 3) l = l + lvy_z * (a.iso ? id2x : id2z);
-      dvy = dvy + (a.rhof_one ? mu * l : mu * l / rhof);
-    }
-    if (a.has_S) {
-      dvx = dvx + (a.rhof_one ? a.Sx[c] : a.Sx[c] / rhof);
-      dvy = dvy + (a.rhof_one ? a.Sy[c] : a.Sy[c] / rhof);
-      if (DIM == 3) dvz = dvz + (a.rhof_one ? a.Sz[c] : a.Sz[c] / rhof);
-    }
-    const float gpx = dfd(P, ip, c) * idx;
-    const float gpy = dfd(P, jp, c) * idy;
-    const float rx = (a.rhof_one ? -gpx : -gpx / rhof) + A * dvx + B * a.dox[c] + (float)a.g[0];
-    const float ry = (a.rhof_one ? -gpy : -gpy / rhof) + A * dvy + B * a.doy[c] + (float)a.g[1];
-    a.du[c] = dt * rx;
-    a.dv[c] = dt * ry;
-    a.dox[c] = dvx;
-    a.doy[c] = dvy;
-    if (DIM == 3) {
-      const float gpz = dfd(P, c + sz, c) * idz;
-      const float rz = (a.rhof_one ? -gpz : -gpz / rhof) + A * dvz + B * a.doz[c] + (float)a.g[2];
-      a.dw[c] = dt * rz;
-      a.doz[c] = dvz;
-    }
-  }
-}
-
 // A double as a pair of floats.
 struct F2 {
   float hi, lo;
@@ -197,23 +80,178 @@ __device__ __forceinline__ F2 add_pair(F2 a, F2 b) {
   return r;
 }
 
-// One axis term of div(v*) as a pair: ((vA - vB) + (dA - dB)) * id, the leading difference
-// error-free.
-__device__ __forceinline__ F2 div_term(const DFField& V, const float* d, long long ca, long long cb, F2 id) {
+// ------------------------------------------------------------------------------------
+// Double-float arithmetic on (hi, lo) pairs of FP32 words (about 48 significant bits).
+// Sums use Knuth's two-sum, products the FMA-exact leading product; results are
+// renormalised so that |lo| <= ulp(hi)/2.  Only FP32 instructions are issued.
+// ------------------------------------------------------------------------------------
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF dfv(const DFField& A, long long c) { return DF{A.hi[c], A.lo[c]}; }
+__device__ __forceinline__ DF dadd(DF a, DF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  e = e + (a.l + b.l);
+  const float h = s + e;
+  return DF{h, e - (h - s)};
+}
+__device__ __forceinline__ DF dsub(DF a, DF b) { return dadd(a, DF{-b.h, -b.l}); }
+__device__ __forceinline__ DF dmul(DF a, DF b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  const float h = p + e;
+  return DF{h, e - (h - p)};
+}
+__device__ __forceinline__ DF dsq(DF a) {
+  const float p = a.h * a.h;
+  float e = fmaf(a.h, a.h, -p);
+  e = fmaf(2.0f * a.h, a.l, e);
+  const float h = p + e;
+  return DF{h, e - (h - p)};
+}
+// Second difference a(+) - 2 a(0) + a(-) of a pair field.
+__device__ __forceinline__ DF d2(DF p, DF c, DF m) {
+  float s1, e1, s2, e2;
+  two_sum(p.h, m.h, s1, e1);
+  two_sum(s1, -2.0f * c.h, s2, e2);
+  float e = (e1 + e2) + ((p.l + m.l) - 2.0f * c.l);
+  const float h = s2 + e;
+  return DF{h, e - (h - s2)};
+}
+
+// ------------------------------------------------------------------------------------
+// Predictor (mixed): the increment dt * rhs and dv_o, both as pairs.  Every term of
+// navier_stokes.f90:140-404 (advection in divergence form, diffusion, body force, pressure
+// gradient, AB2) is evaluated in double-float arithmetic, so the increments keep the
+// state's pair accuracy: FP32 rounding of the increments (about 0.5 |v| per step at
+// CFL 0.5) would otherwise random-walk into the solution.
+// ------------------------------------------------------------------------------------
+struct PredDFArgs {
+  DFField u, v, w, p;
+  float *du, *dv, *dw;        // increment hi
+  float *dul, *dvl, *dwl;     // increment lo
+  float *dox, *doy, *doz;     // dv_o hi
+  float *doxl, *doyl, *dozl;  // dv_o lo
+  const float *Sx, *Sy, *Sz;
+  F2 qx, qy, qz;              // 1/(4 delta) per axis
+  F2 mx, my, mz;              // mu/(rhof delta^2) per axis
+  F2 gx, gy, gz;              // 1/(rhof delta) per axis (pressure gradient)
+  F2 irho;                    // 1/rhof
+  F2 g[3];                    // body acceleration
+  int iso, has_S;
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_predictor_df(Layout L, const StepScalars* __restrict__ sc, PredDFArgs a) {
+  const unsigned n0 = L.n0, n1 = L.n1;
+  const unsigned ncell = n0 * n1 * (unsigned)L.n2;
+  const DF A = DF{sc->Ap[0], sc->Ap[1]}, B = DF{sc->Bp[0], sc->Bp[1]}, DT = DF{sc->dtp[0], sc->dtp[1]};
+  const DF qx = DF{a.qx.hi, a.qx.lo}, qy = DF{a.qy.hi, a.qy.lo}, qz = DF{a.qz.hi, a.qz.lo};
+  const DF mx = DF{a.mx.hi, a.mx.lo}, my = DF{a.my.hi, a.my.lo}, mz = DF{a.mz.hi, a.mz.lo};
+  const long long sy = L.sx, sz = L.sp;
+  const DFField U = a.u, V = a.v, W = a.w, P = a.p;
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < ncell; t += gridDim.x * blockDim.x) {
+    const unsigned r = t / n0;
+    const int i = 1 + (int)(t - r * n0);
+    const int j = 1 + (int)(r % n1);
+    const int k = 1 + (int)(r / n1);
+    const long long c = L.idx(i, j, kst<DIM>(k));
+    const DF uc = dfv(U, c), uip = dfv(U, c + 1), uim = dfv(U, c - 1), ujp = dfv(U, c + sy), ujm = dfv(U, c - sy);
+    const DF vc = dfv(V, c), vip = dfv(V, c + 1), vim = dfv(V, c - 1), vjp = dfv(V, c + sy), vjm = dfv(V, c - sy);
+    // advection: products at faces and edges (1/4 folded into q); the (i+1/2, j+1/2) edge
+    // product is shared by the u and v equations
+    const DF uv_pp = dmul(dadd(ujp, uc), dadd(vip, vc));
+    const DF uv_pm = dmul(dadd(uc, ujm), dadd(dfv(V, c + 1 - sy), vjm));
+    const DF uv_mp = dmul(dadd(vc, vim), dadd(dfv(U, c - 1 + sy), uim));
+    DF ax = dmul(dsub(dsq(dadd(uip, uc)), dsq(dadd(uc, uim))), qx);
+    ax = dadd(ax, dmul(dsub(uv_pp, uv_pm), qy));
+    DF ay = dmul(dsub(uv_pp, uv_mp), qx);
+    ay = dadd(ay, dmul(dsub(dsq(dadd(vjp, vc)), dsq(dadd(vc, vjm))), qy));
+    DF lu = dmul(d2(uip, uc, uim), mx), lv = dmul(d2(vip, vc, vim), mx);
+    lu = dadd(lu, dmul(d2(ujp, uc, ujm), my));
+    lv = dadd(lv, dmul(d2(vjp, vc, vjm), my));
+    DF dz = DF{0.f, 0.f}, wc = DF{0.f, 0.f};
+    if (DIM == 3) {
+      wc = dfv(W, c);
+      const DF wip = dfv(W, c + 1), wim = dfv(W, c - 1), wjp = dfv(W, c + sy), wjm = dfv(W, c - sy);
+      const DF wkp = dfv(W, c + sz), wkm = dfv(W, c - sz);
+      const DF ukp = dfv(U, c + sz), ukm = dfv(U, c - sz), vkp = dfv(V, c + sz), vkm = dfv(V, c - sz);
+      const DF uw_pp = dmul(dadd(ukp, uc), dadd(wip, wc));
+      const DF uw_pm = dmul(dadd(uc, ukm), dadd(dfv(W, c + 1 - sz), wkm));
+      const DF uw_mp = dmul(dadd(wc, wim), dadd(uim, dfv(U, c - 1 + sz)));
+      const DF vw_pp = dmul(dadd(vkp, vc), dadd(wjp, wc));
+      const DF vw_pm = dmul(dadd(vc, vkm), dadd(dfv(W, c + sy - sz), wkm));
+      const DF vw_mp = dmul(dadd(wc, wjm), dadd(vjm, dfv(V, c - sy + sz)));
+      ax = dadd(ax, dmul(dsub(uw_pp, uw_pm), qz));
+      ay = dadd(ay, dmul(dsub(vw_pp, vw_pm), qz));
+      DF az = dmul(dsub(uw_pp, uw_mp), qx);
+      az = dadd(az, dmul(dsub(vw_pp, vw_mp), qy));
+      az = dadd(az, dmul(dsub(dsq(dadd(wc, wkp)), dsq(dadd(wc, wkm))), qz));
+      lu = dadd(lu, dmul(d2(ukp, uc, ukm), mz));
+      lv = dadd(lv, dmul(d2(vkp, vc, vkm), mz));
+      DF lw = dmul(d2(wip, wc, wim), mx);
+      lw = dadd(lw, dmul(d2(wjp, wc, wjm), my));
+      lw = dadd(lw, dmul(d2(wkp, wc, wkm), mz));
+      dz = dsub(lw, az);
+    }
+    DF dx = dsub(lu, ax), dy = dsub(lv, ay);
+    if (a.has_S) {
+      const DF ir = DF{a.irho.hi, a.irho.lo};
+      dx = dadd(dx, dmul(DF{a.Sx[c], 0.f}, ir));
+      dy = dadd(dy, dmul(DF{a.Sy[c], 0.f}, ir));
+      if (DIM == 3) dz = dadd(dz, dmul(DF{a.Sz[c], 0.f}, ir));
+    }
+    // AB2 with the pressure gradient (fields.f90:55-58, navier_stokes.f90:169-198)
+    const DF pc = dfv(P, c);
+    DF rx = dsub(DF{a.g[0].hi, a.g[0].lo}, dmul(dsub(dfv(P, c + 1), pc), DF{a.gx.hi, a.gx.lo}));
+    DF ry = dsub(DF{a.g[1].hi, a.g[1].lo}, dmul(dsub(dfv(P, c + sy), pc), DF{a.gy.hi, a.gy.lo}));
+    rx = dadd(rx, dadd(dmul(A, dx), dmul(B, DF{a.dox[c], a.doxl[c]})));
+    ry = dadd(ry, dadd(dmul(A, dy), dmul(B, DF{a.doy[c], a.doyl[c]})));
+    const DF ix = dmul(DT, rx), iy = dmul(DT, ry);
+    a.du[c] = ix.h; a.dul[c] = ix.l;
+    a.dv[c] = iy.h; a.dvl[c] = iy.l;
+    a.dox[c] = dx.h; a.doxl[c] = dx.l;
+    a.doy[c] = dy.h; a.doyl[c] = dy.l;
+    if (DIM == 3) {
+      DF rz = dsub(DF{a.g[2].hi, a.g[2].lo}, dmul(dsub(dfv(P, c + sz), pc), DF{a.gz.hi, a.gz.lo}));
+      rz = dadd(rz, dadd(dmul(A, dz), dmul(B, DF{a.doz[c], a.dozl[c]})));
+      const DF iz = dmul(DT, rz);
+      a.dw[c] = iz.h; a.dwl[c] = iz.l;
+      a.doz[c] = dz.h; a.dozl[c] = dz.l;
+    }
+  }
+}
+
+// One axis term of div(v*) as a pair: ((vA - vB) + (dA - dB)) * id with v* = v + d, both
+// differences taken error-free on the pairs (d may be null: div(v)).
+__device__ __forceinline__ F2 div_term(const DFField& V, const float* d, const float* dl, long long ca, long long cb,
+                                       F2 id) {
   float s, e;
   two_sum(V.hi[ca], -V.hi[cb], s, e);
-  e = e + ((V.lo[ca] - V.lo[cb]) + (d ? d[ca] - d[cb] : 0.0f));
+  e = e + (V.lo[ca] - V.lo[cb]);
+  if (d) {
+    float s2, e2;
+    two_sum(d[ca], -d[cb], s2, e2);
+    if (dl) e2 = e2 + (dl[ca] - dl[cb]);
+    float s3, e3;
+    two_sum(s, s2, s3, e3);
+    s = s3;
+    e = e3 + (e + e2);
+  }
   return mul_pair(s, e, id);
 }
 
-// div(v*) at (i, j, k) as a pair, v* = v + dt*rhs (d* = the FP32 increment, or null for div(v)).
+// div(v*) at (i, j, k) as a pair, v* = v + (increment hi + lo) (null increments: div(v)).
 template <int DIM>
 __device__ __forceinline__ F2 div_df(const Layout& L, const DFField& U, const DFField& V, const DFField& W,
-                                     const float* du, const float* dv, const float* dw, const F2* id, int i, int j,
-                                     int k) {
+                                     const float* du, const float* dv, const float* dw, const float* dul,
+                                     const float* dvl, const float* dwl, const F2* id, int i, int j, int k) {
   const long long c = L.idx(i, j, kst<DIM>(k));
-  F2 r = add_pair(div_term(U, du, c, c - 1, id[0]), div_term(V, dv, c, c - L.sx, id[1]));
-  if (DIM == 3) r = add_pair(r, div_term(W, dw, c, c - L.sp, id[2]));
+  F2 r = add_pair(div_term(U, du, dul, c, c - 1, id[0]), div_term(V, dv, dvl, c, c - L.sx, id[1]));
+  if (DIM == 3) r = add_pair(r, div_term(W, dw, dwl, c, c - L.sp, id[2]));
   return r;
 }
 
@@ -222,6 +260,7 @@ __device__ __forceinline__ F2 div_df(const Layout& L, const DFField& U, const DF
 // ------------------------------------------------------------------------------------
 struct CorrDFArgs {
   const float *du, *dv, *dw, *phi;
+  const float *dul, *dvl, *dwl;
   const float* dphi;  // refinement correction of phi (or null)
   DFFieldW u, v, w, p;
   double id[3];
@@ -248,19 +287,22 @@ __global__ void __launch_bounds__(256) k_correct_df(Layout L, const StepScalars*
     // grad(phi + dphi) by differences of each part
     const float gx = (a.phi[c + 1] - ph) + (q ? q[c + 1] - qh : 0.0f);
     const float gy = (a.phi[c + L.sx] - ph) + (q ? q[c + L.sx] - qh : 0.0f);
-    float hi, lo;
-    hi = a.u.hi[c]; lo = a.u.lo[c];
-    df_add(hi, lo, a.du[c] - gx * idx * f);
-    a.u.hi[c] = hi; a.u.lo[c] = lo;
-    hi = a.v.hi[c]; lo = a.v.lo[c];
-    df_add(hi, lo, a.dv[c] - gy * idy * f);
-    a.v.hi[c] = hi; a.v.lo[c] = lo;
-    if (DIM == 3) {
-      const float gz = (a.phi[c + L.sp] - ph) + (q ? q[c + L.sp] - qh : 0.0f);
-      hi = a.w.hi[c]; lo = a.w.lo[c];
-      df_add(hi, lo, a.dw[c] - gz * idz * f);
-      a.w.hi[c] = hi; a.w.lo[c] = lo;
+    // v += (increment pair) - dt grad(phi)/rhof, summed as pairs
+    {
+      DF x = dadd(DF{a.u.hi[c], a.u.lo[c]}, DF{a.du[c], a.dul[c]});
+      x = dadd(x, DF{-gx * idx * f, 0.f});
+      a.u.hi[c] = x.h; a.u.lo[c] = x.l;
+      DF y = dadd(DF{a.v.hi[c], a.v.lo[c]}, DF{a.dv[c], a.dvl[c]});
+      y = dadd(y, DF{-gy * idy * f, 0.f});
+      a.v.hi[c] = y.h; a.v.lo[c] = y.l;
+      if (DIM == 3) {
+        const float gz = (a.phi[c + L.sp] - ph) + (q ? q[c + L.sp] - qh : 0.0f);
+        DF z = dadd(DF{a.w.hi[c], a.w.lo[c]}, DF{a.dw[c], a.dwl[c]});
+        z = dadd(z, DF{-gz * idz * f, 0.f});
+        a.w.hi[c] = z.h; a.w.lo[c] = z.l;
+      }
     }
+    float hi, lo;
     hi = a.p.hi[c]; lo = a.p.lo[c];
     df_add(hi, lo, ph);
     if (q) df_add(hi, lo, qh);
@@ -295,7 +337,7 @@ __global__ void __launch_bounds__(256) k_checks_df(Layout L, CheckDFArgs a) {
     float vel = fabsf(a.u.hi[c]) + fabsf(a.v.hi[c]);
     float d = 0.0f;
     if (a.want_div) {
-      const F2 dd = div_df<DIM>(L, a.u, a.v, a.w, nullptr, nullptr, nullptr, a.idp, i, j, k);
+      const F2 dd = div_df<DIM>(L, a.u, a.v, a.w, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, a.idp, i, j, k);
       d = dd.hi + dd.lo;
     }
     if (DIM == 3) vel = vel + fabsf(a.w.hi[c]);
@@ -330,6 +372,7 @@ __global__ void __launch_bounds__(256) k_checks_df(Layout L, CheckDFArgs a) {
 struct ResidualArgs {
   DFField u, v, w;
   const float *du, *dv, *dw;
+  const float *dul, *dvl, *dwl;
   const float* phi;
   float* r;
   F2 idp[3];
@@ -355,7 +398,7 @@ __global__ void __launch_bounds__(256) k_residual_df(Layout L, const StepScalars
     const int j = 1 + (int)(rr % L.n1);
     const int k = 1 + (int)(rr / L.n1);
     const long long c = L.idx(i, j, kst<DIM>(k));
-    const F2 dv = div_df<DIM>(L, a.u, a.v, a.w, a.du, a.dv, a.dw, a.idp, i, j, k);
+    const F2 dv = div_df<DIM>(L, a.u, a.v, a.w, a.du, a.dv, a.dw, a.dul, a.dvl, a.dwl, a.idp, i, j, k);
     const F2 b = mul_pair(dv.hi, dv.lo, rod);
     F2 lap = add_pair(lap_term(a.phi, c, 1, a.id2p[0]), lap_term(a.phi, c, L.sx, a.id2p[1]));
     if (DIM == 3) lap = add_pair(lap, lap_term(a.phi, c, L.sp, a.id2p[2]));
