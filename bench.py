@@ -206,12 +206,12 @@ def cpu_baseline(name, cfg, max_seconds=20.0):
             "sample": f"{steps} steps of {name} at {n[0]}x{n[1]}x{n[2]} ({el:.1f} s), CPU restatement (not FFTW)"}
 
 
-def form_mixed(F, steps):
+def form_mixed(F, steps, scale=1):
     """Channel flow (512x256x384, Re_tau = 180, CFL = 0.5): the mixed form against the FP64
     path over the same `steps` steps from the same initial field.  Returns both throughputs
     and the mixed form's relative L2 error per field (p mean-free)."""
     cfg = CONFIGS["channel"]
-    n, L = cfg["n"], cfg["L"]
+    n, L = tuple(x // scale for x in cfg["n"]), cfg["L"]
     cells = n[0] * n[1] * n[2]
     out, ref = {}, {}
     for prec, name in ((F.FP64, "fp64"), (F.MIXED, "mixed")):
@@ -239,7 +239,7 @@ def form_mixed(F, steps):
         del s
     out["speedup"] = round(out["mixed"] / out["fp64"], 3)
     out["unit"] = "Mcell-steps/s"
-    out["workload"] = f"channel 512x256x384, {steps} steps from Poiseuille + 5% noise, CFL 0.5"
+    out["workload"] = f"channel {n[0]}x{n[1]}x{n[2]}, {steps} steps from Poiseuille + 5% noise, CFL 0.5"
     return out
 
 
@@ -302,13 +302,13 @@ def form_adjoint(F, ndir=16, nsteps=500, every=50):
             "workload": "2D decaying turbulence 256^2, nu=2e-3, dt=2e-3, 500 steps, checkpoints every 50, FP64"}
 
 
-def form_ensemble(F, steps=2000, nruns=512, tune_steps=10):
+def form_ensemble(F, steps=2000, nruns=512, tune_steps=10, sizes=(64, 96, 128, 192, 256)):
     """Batched ensemble: 512 independent 2D Kolmogorov runs (N ~ U{64, 96, 128, 192, 256},
     Re ~ U[50, 500], forcing sin(4y), noise 1e-2, CFL 0.4) advanced `steps` steps in one
     persistent launch, FP32 with FP64 reductions, tile shapes from the autotuner."""
     from tests import cases as C
 
-    n, nu, init = C.kolmogorov_ensemble(nruns)
+    n, nu, init = C.kolmogorov_ensemble(nruns, sizes=tuple(sizes))
     e = F.Ensemble(n, nu, length=2 * np.pi, CFL=0.4, forcing=(1.0, 4))
     for q in range(nruns):
         e.upload(q, *init(q))
@@ -366,6 +366,12 @@ def main():
     ap.add_argument("--grid", type=int, default=0, help="cubic/square override of the grid (profiling runs)")
     ap.add_argument("--no-forms", action="store_true", help="skip the mixed-precision and adjoint measurements")
     ap.add_argument("--form-steps", type=int, default=500, help="channel steps of the mixed-vs-FP64 comparison")
+    ap.add_argument("--form", default="", choices=["", "mixed", "adjoint", "ensemble"],
+                    help="run one form alone and print its JSON (profiling; --grid divides the channel, "
+                         "--ensemble-runs/--ensemble-sizes/--ensemble-steps size the ensemble)")
+    ap.add_argument("--ensemble-runs", type=int, default=512)
+    ap.add_argument("--ensemble-steps", type=int, default=2000)
+    ap.add_argument("--ensemble-sizes", default="64,96,128,192,256")
     args = ap.parse_args()
     cfg_name = args.config
     cfg = dict(CONFIGS[cfg_name])
@@ -374,6 +380,18 @@ def main():
         cfg["n"] = (g0, g0, g0 if cfg["dim"] == 3 else 1) if cfg_name != "channel" else (2 * g0, g0, (3 * g0) // 2)
         cfg["desc"] = cfg["desc"] + f" (grid override {cfg['n']})"
     rank, world, local = env_rank()
+    if args.form and args.impl == "ours":
+        import fen_gb300 as F
+
+        if args.form == "mixed":
+            res = form_mixed(F, args.form_steps, scale=max(1, args.grid and 256 // args.grid or 1))
+        elif args.form == "adjoint":
+            res = form_adjoint(F)
+        else:
+            res = form_ensemble(F, steps=args.ensemble_steps, nruns=args.ensemble_runs,
+                                sizes=[int(x) for x in args.ensemble_sizes.split(",")])
+        print(json.dumps({"form": args.form, **res}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, cfg_name, cfg)
         return
