@@ -70,7 +70,9 @@ _EXPORTS = [
     "fen_adjoint_forward", "fen_adjoint_backward", "fen_ensemble_create", "fen_ensemble_destroy",
     "fen_ensemble_upload", "fen_ensemble_download", "fen_ensemble_set_timestep", "fen_ensemble_advance",
     "fen_ensemble_status", "fen_ensemble_config", "fen_ensemble_set_config", "fen_ensemble_tune",
-    "fen_ensemble_launches", "fen_ensemble_smem_bytes",
+    "fen_ensemble_launches", "fen_ensemble_smem_bytes", "fen_ensemble_adjoint_setup", "fen_ensemble_adjoint_forward",
+    "fen_ensemble_adjoint_seed", "fen_ensemble_adjoint_backward", "fen_ensemble_adjoint_gradient",
+    "fen_ensemble_adjoint_dts",
 ]
 
 
@@ -127,6 +129,12 @@ def load_library(path=None):
     L.fen_ensemble_launches.restype = ctypes.c_longlong
     L.fen_ensemble_smem_bytes.argtypes = [ctypes.c_int, ctypes.c_int]
     L.fen_ensemble_smem_bytes.restype = ctypes.c_size_t
+    L.fen_ensemble_adjoint_setup.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.fen_ensemble_adjoint_forward.argtypes = [vp, dp]
+    L.fen_ensemble_adjoint_seed.argtypes = [vp, ctypes.c_int, dp, dp]
+    L.fen_ensemble_adjoint_backward.argtypes = [vp, dp]
+    L.fen_ensemble_adjoint_gradient.argtypes = [vp, ctypes.c_int, dp, dp]
+    L.fen_ensemble_adjoint_dts.argtypes = [vp, ctypes.c_int, dp, dp]
     if path == LIB_PATH:
         _lib = L
     return L
@@ -436,6 +444,38 @@ class Ensemble:
 
     def launches(self):
         return int(self._L.fen_ensemble_launches(self._h))
+
+    # -- forward/adjoint pair ----------------------------------------------------------------
+    def adjoint_setup(self, nsteps, every):
+        self.adj_nsteps = int(nsteps)
+        self._check(self._L.fen_ensemble_adjoint_setup(self._h, int(nsteps), int(every)))
+
+    def adjoint_forward(self):
+        """Advance every run adj_nsteps steps in one launch, keeping checkpoints; returns ms."""
+        ms = ctypes.c_double()
+        self._check(self._L.fen_ensemble_adjoint_forward(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def adjoint_seed(self, run, lam_u, lam_v):
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (lam_u, lam_v)]
+        self._check(self._L.fen_ensemble_adjoint_seed(self._h, int(run), _dp(a[0]), _dp(a[1])))
+
+    def adjoint_backward(self):
+        """Backward sweep of every run in one launch; returns ms."""
+        ms = ctypes.c_double()
+        self._check(self._L.fen_ensemble_adjoint_backward(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def adjoint_gradient(self, run):
+        N = int(self.n[run])
+        gu, gv = np.zeros((N, N)), np.zeros((N, N))
+        self._check(self._L.fen_ensemble_adjoint_gradient(self._h, int(run), _dp(gu), _dp(gv)))
+        return gu, gv
+
+    def adjoint_dts(self, run):
+        dt, dto = np.zeros(self.adj_nsteps), np.zeros(self.adj_nsteps)
+        self._check(self._L.fen_ensemble_adjoint_dts(self._h, int(run), _dp(dt), _dp(dto)))
+        return dt, dto
 
 
 def ensemble_smem_bytes(n, groups, lib=None):

@@ -102,6 +102,26 @@ struct EnsArgs {
   int* counter;
   int nsteps;
   double cfl;
+  // forward/adjoint pair (mode 1: forward with checkpoints, mode 2: backward sweep)
+  int mode;                  // 0 advance, 1 forward with checkpoints, 2 backward
+  int every, nseg;           // checkpoint interval, segments
+  float* abuf;               // per-run adjoint storage, see AdjLayout
+  const long long* aoff;     // float offset of each run's block in abuf
+  double* rec;               // per run: nsteps x (dt, dt_o)
+};
+
+// Per-run adjoint storage (floats, N2 = N*N): checkpoints nseg x (u, v, p, dvo_x, dvo_y),
+// the step inputs of one segment every x (u, v), a dv_o scratch for the recomputation
+// (u, v), and the adjoint state (u^, v^, p^, dv_o^x, dv_o^y).
+struct AdjLayout {
+  long long ck, seg, dvo, adj;
+  __host__ __device__ AdjLayout(long long N2, int nseg, int every) {
+    ck = 0;
+    seg = ck + (long long)nseg * 5 * N2;
+    dvo = seg + (long long)every * 2 * N2;
+    adj = dvo + 2 * N2;
+  }
+  __host__ __device__ static long long size(long long N2, int nseg, int every) { return AdjLayout(N2, nseg, every).adj + 5 * N2; }
 };
 
 __host__ __device__ inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
@@ -333,92 +353,233 @@ struct Batch {
   static constexpr int kElems = (NT >= 1024) ? 5 : 10;
 };
 
+// One pack seen from one CTA: the run this CTA belongs to, its rows, the shared-memory
+// carve, and the steps (forward, Poisson solve, adjoint) on the G CTAs of the run.
 template <int NT>
-__device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, int q, cg::cluster_group& cl,
-                         unsigned char* smem, double* s_sc, float* s_f, double* s_rd, float* s_rf) {
-  const int N = D.N, G = D.G, M = D.M, SR = D.SR, C = D.C;
-  const int slot = q / G, r = q - slot * G;
-  const bool active = slot < P.nruns;
-  if (!active && G == 1) return;  // no partner waits on this CTA
-  const int run = active ? a.run_list[P.first + slot] : 0;
-  const int base = slot * G;
-  const Carve S = carve(smem, D);
-  auto gsync = [&]() {
+struct Pk {
+  const EnsArgs& a;
+  const ClassDesc& D;
+  cg::cluster_group& cl;
+  Carve S;
+  double* s_sc;  // dt, dt_o, t, maxvel, nu, dt_visc, nan
+  float* s_f;    // dt, A, B, 1/dt, mean
+  double* s_rd;
+  float* s_rf;
+  int N, G, M, SR, C, slot, r, base, run, cells, Mh, npair, rp, rm, c0, Cr;
+  bool active;
+  float idx, id2, q4, mu;
+  const float* force;
+  FDiv fN;
+  float *gu, *gv, *gp, *gdx, *gdy;  // run state in HBM (dv_o may point at the recompute scratch)
+  float* ablk;                      // run's adjoint block (mode 1, 2)
+  double* rec;                      // run's (dt, dt_o) record
+  float *Xf, *Yf, *Zf;
+
+  __device__ Pk(const EnsArgs& a_, const Pack& P, const ClassDesc& D_, int q, cg::cluster_group& cl_, unsigned char* smem,
+                double* s_sc_, float* s_f_, double* s_rd_, float* s_rf_)
+      : a(a_), D(D_), cl(cl_), S(carve(smem, D_)), s_sc(s_sc_), s_f(s_f_), s_rd(s_rd_), s_rf(s_rf_) {
+    N = D.N; G = D.G; M = D.M; SR = D.SR; C = D.C;
+    slot = q / G;
+    r = q - slot * G;
+    active = slot < P.nruns;
+    run = active ? a.run_list[P.first + slot] : 0;
+    base = slot * G;
+    cells = M * N;
+    Mh = N / 2;
+    npair = Mh / 2 + 1;
+    rp = (r + 1) % G;
+    rm = (r - 1 + G) % G;
+    c0 = r * C;
+    Cr = max(0, min(C, SR - c0));
+    idx = D.idx; id2 = D.id2; q4 = 0.25f * D.idx;
+    fN = D.fN;
+    const size_t NN = (size_t)N * N;
+    gu = a.state + (active ? a.run_off[run] : 0);
+    gv = gu + NN; gp = gv + NN; gdx = gp + NN; gdy = gdx + NN;
+    ablk = (a.mode && active) ? a.abuf + a.aoff[run] : nullptr;
+    rec = (a.mode && active) ? a.rec + (size_t)run * a.nsteps * 2 : nullptr;
+    Xf = reinterpret_cast<float*>(S.X); Yf = reinterpret_cast<float*>(S.Y); Zf = reinterpret_cast<float*>(S.Z);
+    force = nullptr;
+    mu = 0.f;
+  }
+  __device__ void gsync() {
     if (G > 1) cl.sync();
     else __syncthreads();
-  };
-  auto pf = [&](float* ptr, int g) -> float* { return G == 1 ? ptr : cl.map_shared_rank(ptr, base + g); };
-  auto p2 = [&](float2* ptr, int g) -> float2* { return G == 1 ? ptr : cl.map_shared_rank(ptr, base + g); };
-  auto pd = [&](double* ptr, int g) -> double* { return G == 1 ? ptr : cl.map_shared_rank(ptr, base + g); };
-  constexpr int CPT = Batch<NT>::kCells, EPT = Batch<NT>::kElems;
-
-  const size_t NN = (size_t)N * N;
-  float* gu = a.state + (active ? a.run_off[run] : 0);
-  float* gv = gu + NN;
-  float* gp = gv + NN;
-  float* gdx = gp + NN;
-  float* gdy = gdx + NN;
-  const FDiv fN = D.fN;
-
-  // ---- load the CTA's rows (with one ghost row each side) ----
-  const int rows = (M + 2) * N;
-  for (int t = threadIdx.x; t < rows; t += NT) {
-    const int mm = fdiv(t, fN), i = t - mm * N;
-    int jg = r * M + mm - 1;
-    jg = jg < 0 ? jg + N : (jg >= N ? jg - N : jg);
-    float uu = 0.f, vv = 0.f, pp = 0.f;
-    if (active) {
-      uu = gu[(size_t)jg * N + i];
-      vv = gv[(size_t)jg * N + i];
-      pp = gp[(size_t)jg * N + i];
-    }
-    S.u[t] = uu;
-    S.v[t] = vv;
-    S.p[t] = pp;
   }
-  if (D.tabs) {
-    for (int t = threadIdx.x; t < N / 2; t += NT) S.twx[t] = D.twx[t];
-    for (int t = threadIdx.x; t <= N / 2; t += NT) {
-      S.twn[t] = D.twn[t];
-      S.lamx[t] = D.lamx[t];
-    }
-    for (int t = threadIdx.x; t < N; t += NT) {
-      S.twy[t] = D.twy[t];
-      S.lamy[t] = D.lamy[t];
-    }
-    for (int t = threadIdx.x; t < M; t += NT) S.force[t] = D.force[r * M + t];
-  }
-  if (threadIdx.x == 0) {
-    RunScal rs;
-    if (active) rs = a.scal[run];
-    else { rs.dt = rs.dt_o = 1.0; rs.t = 0.0; rs.maxvel = 1.0; rs.nu = 1.0; rs.dt_visc = 1.0; rs.nan = 0; }
-    s_sc[0] = rs.dt;
-    s_sc[1] = rs.dt_o;
-    s_sc[2] = rs.t;
-    s_sc[3] = rs.maxvel;
-    s_sc[4] = rs.nu;
-    s_sc[5] = rs.dt_visc;
-    s_sc[6] = rs.nan;
-  }
-  __syncthreads();
-  const float mu = (float)s_sc[4];
-  const float idx = D.idx, id2 = D.id2, q4 = 0.25f * D.idx;
-  const int cells = M * N;
-  const int Mh = N / 2, npair = Mh / 2 + 1;
-  float* Xf = reinterpret_cast<float*>(S.X);
-  float* Yf = reinterpret_cast<float*>(S.Y);
-  float* Zf = reinterpret_cast<float*>(S.Z);
-  const int rp = (r + 1) % G, rm = (r - 1 + G) % G;
-  const int c0 = r * C, Cr = max(0, min(C, SR - c0));
-  const float* force = D.tabs ? S.force : D.force + r * M;
+  template <typename T>
+  __device__ T* peer(T* p, int g) { return G == 1 ? p : cl.map_shared_rank(p, base + g); }
+  __device__ int wrapj(int jg) const { return jg < 0 ? jg + N : (jg >= N ? jg - N : jg); }
 
-  for (int step = 0; step < a.nsteps; ++step) {
-    // ---- update_timestep (constant CFL), FP64 ----
+  // rows r*M-1 .. r*M+M of a global N x N array into shared rows 0 .. M+1
+  __device__ void load_rows(const float* g, float* s) {
+    const int rows = (M + 2) * N;
+    for (int t = threadIdx.x; t < rows; t += NT) {
+      const int mm = fdiv(t, fN), i = t - mm * N;
+      s[t] = active ? g[(size_t)wrapj(r * M + mm - 1) * N + i] : 0.f;
+    }
+  }
+  __device__ void store_rows(const float* s, float* g) {
+    if (!active) return;
+    for (int t = threadIdx.x; t < cells; t += NT) g[(size_t)r * M * N + t] = s[t + N];
+  }
+  // global -> global copy of this CTA's rows
+  __device__ void copy_rows(const float* src, float* dst) {
+    if (!active) return;
+    for (int t = threadIdx.x; t < cells; t += NT) dst[(size_t)r * M * N + t] = src[(size_t)r * M * N + t];
+  }
+  // ghost rows 0 and M+1 of up to three row arrays from the neighbouring CTAs (after a
+  // cluster barrier that made the neighbours' interior rows final)
+  __device__ void ghosts(float* f0, float* f1, float* f2) {
+    float* fs[3] = {f0, f1, f2};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      if (!fs[q]) continue;
+      const float* Fm = peer(fs[q], rm);
+      const float* Fn = peer(fs[q], rp);
+      for (int t = threadIdx.x; t < N; t += NT) {
+        const float x0 = Fm[M * N + t], x1 = Fn[N + t];
+        fs[q][t] = x0;
+        fs[q][(M + 1) * N + t] = x1;
+      }
+    }
+  }
+
+  // ---- the Poisson solve: rhs in Z (real rows of stride 2 SR); returns phi's buffer and
+  // leaves the FP64 mean of phi in s_f[4] (poisson.f90:416-505 with the mean removal) ----
+  __device__ float2* poisson() {
+    constexpr int EPT = Batch<NT>::kElems;
+    float2* SPEC = ens_fft<-1, NT>(S.Z, S.X, M, D.fM, SR, 1, D.px, S.twx);
+    for (int t = threadIdx.x; t < M * npair; t += NT) {
+      const int m = fdiv(t, D.fNP), k = t - m * npair;
+      float2* row = SPEC + m * SR;
+      if (k == 0) {
+        const float2 x0 = pack_r2c(row, Mh, 0, S.twn);
+        const float2 xm = pack_r2c(row, Mh, Mh, S.twn);
+        row[0] = x0;
+        row[Mh] = xm;
+      } else {
+        const float2 xa = pack_r2c(row, Mh, k, S.twn);
+        const float2 xb = pack_r2c(row, Mh, Mh - k, S.twn);
+        row[k] = xa;
+        row[Mh - k] = xb;
+      }
+    }
+    gsync();  // every row spectrum complete
+    // all-to-all: the column block [c0, c0+Cr) of every row into T (= Y)
+    float2* T = S.Y;
+    float2* F = (SPEC == S.Z) ? S.X : S.Z;
+    for (int b0 = 0; b0 < N * C; b0 += EPT * NT) {
+      float2 val[EPT];
+#pragma unroll
+      for (int k = 0; k < EPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        val[k] = make_float2(0.f, 0.f);
+        if (t < N * C) {
+          const int y = fdiv(t, D.fC), cc = t - y * C;
+          if (cc < Cr) {
+            const int g = fdiv(y, D.fM), m = y - g * M;
+            val[k] = peer(SPEC, g)[m * SR + c0 + cc];
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < EPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < N * C) T[t] = val[k];
+      }
+    }
+    __syncthreads();
+    float2* R1 = ens_fft<-1, NT>(T, F, C, D.fC, 1, C, D.py, S.twy);
+    for (int t = threadIdx.x; t < N * C; t += NT) {
+      const int y = fdiv(t, D.fC), cc = t - y * C;
+      if (cc < Cr) {
+        const int kx = c0 + cc;
+        const float lam = S.lamx[kx] + S.lamy[y];
+        const float s = (kx == 0 && y == 0) ? 0.f : D.inv_nn / lam;
+        float2 z = R1[t];
+        z.x *= s;
+        z.y *= s;
+        R1[t] = z;
+      }
+    }
+    __syncthreads();
+    float2* R2 = ens_fft<1, NT>(R1, (R1 == T) ? F : T, C, D.fC, 1, C, D.py, S.twy);
+    gsync();  // column solves complete; row spectra no longer read
+    for (int b0 = 0; b0 < M * SR; b0 += EPT * NT) {
+      float2 val[EPT];
+#pragma unroll
+      for (int k = 0; k < EPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < M * SR) {
+          const int m = fdiv(t, D.fSR), cc = t - m * SR;
+          const int o = fdiv(cc, D.fC), cl_ = cc - o * C;
+          val[k] = peer(R2, o)[(r * M + m) * C + cl_];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < EPT; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < M * SR) SPEC[t] = val[k];
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < M * npair; t += NT) {
+      const int m = fdiv(t, D.fNP), k = t - m * npair;
+      float2* row = SPEC + m * SR;
+      if (k == 0) {
+        row[0] = pack_c2r(row[0], row[Mh], 0, S.twn);
+      } else {
+        const float2 xa = row[k], xb = row[Mh - k];
+        const float2 za = pack_c2r(xa, xb, k, S.twn);
+        const float2 zb = pack_c2r(xb, xa, Mh - k, S.twn);
+        row[k] = za;
+        if (Mh - k != k) row[Mh - k] = zb;
+      }
+    }
+    __syncthreads();
+    float2* W3 = (SPEC != S.X && R2 != S.X) ? S.X : ((SPEC != S.Y && R2 != S.Y) ? S.Y : S.Z);
+    float2* PHI = ens_fft<1, NT>(SPEC, W3, M, D.fM, SR, 1, D.px, S.twx);
+    const float* Phf = reinterpret_cast<const float*>(PHI);
+    {  // FP64 sum of phi for the mean removal
+      float part = 0.f;
+      for (int t = threadIdx.x; t < cells; t += NT) {
+        const int m = fdiv(t, fN), i = t - m * N;
+        part += Phf[m * 2 * SR + i];
+      }
+      const double s = block_sum<NT>((double)part, s_rd);
+      if (threadIdx.x == 0) S.red[0] = s;
+    }
+    gsync();  // phi and the partial sums visible
+    if (threadIdx.x < 32) {  // lanes read the G partial sums; fixed-order butterfly sum
+      double s = (threadIdx.x < G) ? peer(S.red, threadIdx.x)[0] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (threadIdx.x == 0) s_f[4] = (float)(s / ((double)N * N));
+    }
+    __syncthreads();
+    return PHI;
+  }
+
+  // ---- one forward step (navier_stokes.f90:50-136, constant CFL) ----
+  // rec_step >= 0 replays the recorded (dt, dt_o) of that step instead of the CFL update;
+  // rec_out >= 0 records this step's (dt, dt_o).
+  __device__ void fwd_step(int rec_step, int rec_out) {
+    constexpr int CPT = Batch<NT>::kCells;
     if (threadIdx.x == 0) {
-      const double dt_o = s_sc[0], mv = s_sc[3];
-      const double dt_conv = (mv > 0.0) ? a.cfl * D.delta / mv : 1.0;
-      double dt = fmin(dt_conv, s_sc[5]);
-      if (dt > 1.1 * dt_o) dt = 1.1 * dt_o;
+      double dt, dt_o;
+      if (rec_step >= 0 && rec) {
+        dt = rec[2 * rec_step];
+        dt_o = rec[2 * rec_step + 1];
+      } else {
+        dt_o = s_sc[0];
+        const double mv = s_sc[3];
+        const double dt_conv = (mv > 0.0) ? a.cfl * D.delta / mv : 1.0;
+        dt = fmin(dt_conv, s_sc[5]);
+        if (dt > 1.1 * dt_o) dt = 1.1 * dt_o;
+      }
+      if (rec_out >= 0 && rec && r == 0) {
+        rec[2 * rec_out] = dt;
+        rec[2 * rec_out + 1] = dt_o;
+      }
       s_sc[0] = dt;
       s_sc[1] = dt_o;
       const float rf = (float)dt / (float)dt_o;  // the FP32 stencils take A, B and 1/dt in FP32
@@ -430,7 +591,7 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
     __syncthreads();
     const float dt = s_f[0], A = s_f[1], B = s_f[2], rdt = s_f[3];
 
-    // ---- predictor: u* -> X, v* -> Y (FP32), dv_o streamed from/to HBM ----
+    // predictor: u* -> X, v* -> Y (FP32), dv_o streamed from/to HBM
     for (int b0 = 0; b0 < cells; b0 += CPT * NT) {
       float ox[CPT], oy[CPT];
 #pragma unroll
@@ -475,11 +636,11 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
         }
       }
     }
-    gsync();  // B1: v* rows visible to the next CTA
+    gsync();  // v* rows visible to the next CTA
 
-    // ---- divergence -> Z (real rows of stride 2 SR floats); u, v <- u*, v* ----
+    // divergence * rho/dt -> Z; u, v <- u*, v*
     {
-      const float* Yprev = pf(Yf, rm);
+      const float* Yprev = peer(Yf, rm);
       const float sc = idx * rdt;
       for (int t = threadIdx.x; t < cells; t += NT) {
         const int m = fdiv(t, fN), i = t - m * N;
@@ -492,126 +653,13 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
       }
     }
     __syncthreads();
-
-    // ---- r2c along x: complex FFT of length N/2 on the packed rows, then unpacking ----
-    float2* SPEC = ens_fft<-1, NT>(S.Z, S.X, M, D.fM, SR, 1, D.px, S.twx);
-    for (int t = threadIdx.x; t < M * npair; t += NT) {
-      const int m = fdiv(t, D.fNP), k = t - m * npair;
-      float2* row = SPEC + m * SR;
-      if (k == 0) {
-        const float2 x0 = pack_r2c(row, Mh, 0, S.twn);
-        const float2 xm = pack_r2c(row, Mh, Mh, S.twn);
-        row[0] = x0;
-        row[Mh] = xm;
-      } else {
-        const float2 xa = pack_r2c(row, Mh, k, S.twn);
-        const float2 xb = pack_r2c(row, Mh, Mh - k, S.twn);
-        row[k] = xa;
-        row[Mh - k] = xb;
-      }
-    }
-    gsync();  // B2: every row spectrum complete
-
-    // ---- all-to-all: gather the column block [c0, c0+Cr) of every row into T (= Y) ----
-    float2* T = S.Y;
-    float2* F = (SPEC == S.Z) ? S.X : S.Z;
-    for (int b0 = 0; b0 < N * C; b0 += EPT * NT) {
-      float2 val[EPT];
-#pragma unroll
-      for (int k = 0; k < EPT; ++k) {
-        const int t = b0 + threadIdx.x + k * NT;
-        val[k] = make_float2(0.f, 0.f);
-        if (t < N * C) {
-          const int y = fdiv(t, D.fC), cc = t - y * C;
-          if (cc < Cr) {
-            const int g = fdiv(y, D.fM), m = y - g * M;
-            val[k] = p2(SPEC, g)[m * SR + c0 + cc];
-          }
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < EPT; ++k) {
-        const int t = b0 + threadIdx.x + k * NT;
-        if (t < N * C) T[t] = val[k];
-      }
-    }
-    __syncthreads();
-    // ---- y: forward FFT, divide by lam_x + lam_y (zero mode -> 0), inverse FFT ----
-    float2* R1 = ens_fft<-1, NT>(T, F, C, D.fC, 1, C, D.py, S.twy);
-    for (int t = threadIdx.x; t < N * C; t += NT) {
-      const int y = fdiv(t, D.fC), cc = t - y * C;
-      if (cc < Cr) {
-        const int kx = c0 + cc;
-        const float lam = S.lamx[kx] + S.lamy[y];
-        const float s = (kx == 0 && y == 0) ? 0.f : D.inv_nn / lam;
-        float2 z = R1[t];
-        z.x *= s;
-        z.y *= s;
-        R1[t] = z;
-      }
-    }
-    __syncthreads();
-    float2* R2 = ens_fft<1, NT>(R1, (R1 == T) ? F : T, C, D.fC, 1, C, D.py, S.twy);
-    gsync();  // B3: column solves complete; row spectra no longer read
-
-    // ---- all-to-all back: rows of this CTA from every column owner, into SPEC ----
-    for (int b0 = 0; b0 < M * SR; b0 += EPT * NT) {
-      float2 val[EPT];
-#pragma unroll
-      for (int k = 0; k < EPT; ++k) {
-        const int t = b0 + threadIdx.x + k * NT;
-        if (t < M * SR) {
-          const int m = fdiv(t, D.fSR), cc = t - m * SR;
-          const int o = fdiv(cc, D.fC), cl_ = cc - o * C;
-          val[k] = p2(R2, o)[(r * M + m) * C + cl_];
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < EPT; ++k) {
-        const int t = b0 + threadIdx.x + k * NT;
-        if (t < M * SR) SPEC[t] = val[k];
-      }
-    }
-    __syncthreads();
-    // ---- c2r along x: packing then inverse complex FFT of length N/2 ----
-    for (int t = threadIdx.x; t < M * npair; t += NT) {
-      const int m = fdiv(t, D.fNP), k = t - m * npair;
-      float2* row = SPEC + m * SR;
-      if (k == 0) {
-        row[0] = pack_c2r(row[0], row[Mh], 0, S.twn);
-      } else {
-        const float2 xa = row[k], xb = row[Mh - k];
-        const float2 za = pack_c2r(xa, xb, k, S.twn);
-        const float2 zb = pack_c2r(xb, xa, Mh - k, S.twn);
-        row[k] = za;
-        if (Mh - k != k) row[Mh - k] = zb;
-      }
-    }
-    __syncthreads();
-    float2* W3 = (SPEC != S.X && R2 != S.X) ? S.X : ((SPEC != S.Y && R2 != S.Y) ? S.Y : S.Z);
-    float2* PHI = ens_fft<1, NT>(SPEC, W3, M, D.fM, SR, 1, D.px, S.twx);
+    float2* PHI = poisson();
     const float* Phf = reinterpret_cast<const float*>(PHI);
-    {  // FP64 sum of phi for the mean removal (poisson.f90:491-503)
-      float part = 0.f;
-      for (int t = threadIdx.x; t < cells; t += NT) {
-        const int m = fdiv(t, fN), i = t - m * N;
-        part += Phf[m * 2 * SR + i];
-      }
-      const double s = block_sum<NT>((double)part, s_rd);
-      if (threadIdx.x == 0) S.red[0] = s;
-    }
-    gsync();  // B4: phi and the partial sums visible
-    if (threadIdx.x < 32) {  // lanes read the G partial sums; fixed-order butterfly sum
-      double s = (threadIdx.x < G) ? pd(S.red, threadIdx.x)[0] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (threadIdx.x == 0) s_f[4] = (float)(s / ((double)N * N));
-    }
-    __syncthreads();
 
-    // ---- correction, p update, max(|u| + |v|) ----
+    // correction, p update, max(|u| + |v|)
     {
       const float meanf = s_f[4];
-      const float* Phn = reinterpret_cast<const float*>(p2(PHI, rp));
+      const float* Phn = reinterpret_cast<const float*>(peer(PHI, rp));
       float vmax = 0.f;
       int bad = 0;
       for (int t = threadIdx.x; t < cells; t += NT) {
@@ -637,59 +685,236 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
         S.red[2] = (double)bad;
       }
     }
-    gsync();  // B5: corrected rows, maxima visible
+    gsync();  // corrected rows, maxima visible
     if (threadIdx.x < 32) {
-      double mv = 0.0, bad = 0.0;
+      double mv = 0.0, bd = 0.0;
       if (threadIdx.x < G) {
-        const double* rr = pd(S.red, threadIdx.x);
+        const double* rr = peer(S.red, threadIdx.x);
         mv = rr[1];
-        bad = rr[2];
+        bd = rr[2];
       }
       for (int o = 16; o > 0; o >>= 1) {
         mv = fmax(mv, __shfl_xor_sync(0xffffffffu, mv, o));
-        bad = fmax(bad, __shfl_xor_sync(0xffffffffu, bad, o));
+        bd = fmax(bd, __shfl_xor_sync(0xffffffffu, bd, o));
       }
       if (threadIdx.x == 0) {
         s_sc[3] = mv;
         s_sc[2] += s_sc[0];
-        if (bad != 0.0) s_sc[6] = 1.0;
+        if (bd != 0.0) s_sc[6] = 1.0;
       }
     }
-    // ---- ghost rows from the neighbouring CTAs (periodic in y) ----
-    {
-      const float* Um = pf(S.u, rm);
-      const float* Vm = pf(S.v, rm);
-      const float* Pm = pf(S.p, rm);
-      const float* Un = pf(S.u, rp);
-      const float* Vn = pf(S.v, rp);
-      const float* Pn = pf(S.p, rp);
-      for (int t = threadIdx.x; t < N; t += NT) {
-        const float a0 = Um[M * N + t], a1 = Vm[M * N + t], a2 = Pm[M * N + t];
-        const float b0 = Un[N + t], b1 = Vn[N + t], b2 = Pn[N + t];
-        S.u[t] = a0;
-        S.v[t] = a1;
-        S.p[t] = a2;
-        S.u[(M + 1) * N + t] = b0;
-        S.v[(M + 1) * N + t] = b1;
-        S.p[(M + 1) * N + t] = b2;
-      }
-    }
+    ghosts(S.u, S.v, S.p);
     __syncthreads();
   }
 
-  // ---- store the state; kinetic energy and max div (FP64 across the run) ----
-  {
-    float kpart = 0.f, dmax = -INFINITY;
+  // ---- one adjoint step (the transpose of fwd_step for fixed dt; see fen_adjoint.cuh) ----
+  // Adjoint state: u^, v^ (rows with ghosts) in S.u, S.v, p^ in S.p, dv_o^ in HBM (ax, ay);
+  // the forward step's input velocity (u, v) in HBM (fu, fv, full N x N arrays).
+  __device__ void adj_step(const float* fu, const float* fv, double dtd, double dt_od, float* ax, float* ay) {
+    const float dt = (float)dtd;
+    const float rf = (float)dtd / (float)dt_od;
+    const float A = 1.0f + 0.5f * rf, B = -0.5f * rf, rdt = 1.0f / dt;
+    // phi^ = p^ + dt D(v^)  -> Z
     for (int t = threadIdx.x; t < cells; t += NT) {
       const int m = fdiv(t, fN), i = t - m * N;
       const int im = (i == 0) ? N - 1 : -1;
       const int c = t + N;
-      const float uu = S.u[c], vv = S.v[c];
+      Zf[m * 2 * SR + i] = S.p[c] + dt * (((S.u[c] - S.u[c + im]) + (S.v[c] - S.v[c - N])) * idx);
+    }
+    __syncthreads();
+    // b^ = P phi^ (symmetric); v*^ = v^ - (rho/dt) G b^  (in place)
+    float2* PHI = poisson();
+    {
+      const float* Phf = reinterpret_cast<const float*>(PHI);
+      const float* Phn = reinterpret_cast<const float*>(peer(PHI, rp));
+      for (int t = threadIdx.x; t < cells; t += NT) {
+        const int m = fdiv(t, fN), i = t - m * N;
+        const int ip = (i + 1 == N) ? 1 - N : 1;
+        const int o = m * 2 * SR + i;
+        const float b = Phf[o], bip = Phf[o + ip];
+        const float bjp = (m + 1 < M) ? Phf[o + 2 * SR] : Phn[i];
+        const int c = t + N;
+        S.u[c] = S.u[c] - rdt * (bip - b) * idx;
+        S.v[c] = S.v[c] - rdt * (bjp - b) * idx;
+      }
+    }
+    gsync();
+    ghosts(S.u, S.v, nullptr);
+    __syncthreads();
+    // p^ += dt D(v*^); dv^ = dv_o^ + dt A v*^ -> X, Y (rows with ghosts); dv_o^ = dt B v*^
+    for (int t = threadIdx.x; t < cells; t += NT) {
+      const int m = fdiv(t, fN), i = t - m * N;
+      const int im = (i == 0) ? N - 1 : -1;
+      const int c = t + N;
+      const float us = S.u[c], vs = S.v[c];
+      S.p[c] = S.p[c] + dt * (((us - S.u[c + im]) + (vs - S.v[c - N])) * idx);
+      float ox = 0.f, oy = 0.f;
       if (active) {
         const size_t gi = (size_t)r * M * N + t;
-        gu[gi] = uu;
-        gv[gi] = vv;
-        gp[gi] = S.p[c];
+        ox = ax[gi];
+        oy = ay[gi];
+        ax[gi] = dt * B * us;
+        ay[gi] = dt * B * vs;
+      }
+      Xf[c] = ox + dt * A * us;
+      Yf[c] = oy + dt * A * vs;
+    }
+    gsync();
+    ghosts(Xf, Yf, nullptr);
+    __syncthreads();
+    // v^ = v*^ + N'(v)^T dv^ + mu L dv^   (navier_stokes.f90:297-323 transposed)
+    const float mur = mu;
+    for (int t = threadIdx.x; t < cells; t += NT) {
+      const int m = fdiv(t, fN), i = t - m * N;
+      const int ip = (i + 1 == N) ? 1 - N : 1;
+      const int im = (i == 0) ? N - 1 : -1;
+      const int c = t + N;
+      const float* hu = Xf;
+      const float* hv = Yf;
+      // forward input velocity around (i, j) from HBM (periodic in both directions)
+      const int jg = r * M + m;
+      const size_t row = (size_t)jg * N, rowp = (size_t)wrapj(jg + 1) * N, rowm = (size_t)wrapj(jg - 1) * N;
+      const int i_p = i + ip, i_m = i + im;
+      float u0 = 0.f, uip = 0.f, uim = 0.f, ujp = 0.f, uimjp = 0.f, v0 = 0.f, vip = 0.f, vjp = 0.f, vjm = 0.f, vipjm = 0.f;
+      if (active) {
+        u0 = fu[row + i]; uip = fu[row + i_p]; uim = fu[row + i_m]; ujp = fu[rowp + i]; uimjp = fu[rowp + i_m];
+        v0 = fv[row + i]; vip = fv[row + i_p]; vjp = fv[rowp + i]; vjm = fv[rowm + i]; vipjm = fv[rowm + i_p];
+      }
+      const float Fu_p = (hu[c + ip] - hu[c]) * idx, Fu_m = (hu[c] - hu[c + im]) * idx;
+      const float Fv_p = (hv[c + N] - hv[c]) * idx, Fv_m = (hv[c] - hv[c - N]) * idx;
+      const float C_ij = (hu[c + N] - hu[c]) * idx + (hv[c + ip] - hv[c]) * idx;
+      const float C_ijm = (hu[c] - hu[c - N]) * idx + (hv[c + ip - N] - hv[c - N]) * idx;
+      const float C_imj = (hu[c + im + N] - hu[c + im]) * idx + (hv[c] - hv[c + im]) * idx;
+      const float gu_ = Fu_p * 0.5f * (uip + u0) + Fu_m * 0.5f * (u0 + uim) + C_ij * 0.25f * (vip + v0) +
+                        C_ijm * 0.25f * (vipjm + vjm);
+      const float gv_ = Fv_p * 0.5f * (vjp + v0) + Fv_m * 0.5f * (v0 + vjm) + C_ij * 0.25f * (ujp + u0) +
+                        C_imj * 0.25f * (uimjp + uim);
+      const float lu = ((hu[c + ip] + hu[c + im]) + (hu[c + N] + hu[c - N]) - 4.0f * hu[c]) * id2;
+      const float lv = ((hv[c + ip] + hv[c + im]) + (hv[c + N] + hv[c - N]) - 4.0f * hv[c]) * id2;
+      S.u[c] = S.u[c] + gu_ + mur * lu;
+      S.v[c] = S.v[c] + gv_ + mur * lv;
+    }
+    gsync();
+    ghosts(S.u, S.v, nullptr);
+    __syncthreads();
+  }
+};
+
+template <int NT>
+__device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, int q, cg::cluster_group& cl,
+                         unsigned char* smem, double* s_sc, float* s_f, double* s_rd, float* s_rf) {
+  Pk<NT> k(a, P, D, q, cl, smem, s_sc, s_f, s_rd, s_rf);
+  if (!k.active && k.G == 1) return;  // no partner waits on this CTA
+  const int N = k.N, M = k.M, r = k.r;
+  const Carve& S = k.S;
+  const long long N2 = (long long)N * N;
+  // tables of this grid size
+  if (D.tabs) {
+    for (int t = threadIdx.x; t < N / 2; t += NT) S.twx[t] = D.twx[t];
+    for (int t = threadIdx.x; t <= N / 2; t += NT) {
+      S.twn[t] = D.twn[t];
+      S.lamx[t] = D.lamx[t];
+    }
+    for (int t = threadIdx.x; t < N; t += NT) {
+      S.twy[t] = D.twy[t];
+      S.lamy[t] = D.lamy[t];
+    }
+    for (int t = threadIdx.x; t < M; t += NT) S.force[t] = D.force[r * M + t];
+  }
+  k.force = D.tabs ? S.force : D.force + r * M;
+  if (threadIdx.x == 0) {
+    RunScal rs;
+    if (k.active) rs = a.scal[k.run];
+    else { rs.dt = rs.dt_o = 1.0; rs.t = 0.0; rs.maxvel = 1.0; rs.nu = 1.0; rs.dt_visc = 1.0; rs.nan = 0; }
+    s_sc[0] = rs.dt;
+    s_sc[1] = rs.dt_o;
+    s_sc[2] = rs.t;
+    s_sc[3] = rs.maxvel;
+    s_sc[4] = rs.nu;
+    s_sc[5] = rs.dt_visc;
+    s_sc[6] = rs.nan;
+  }
+  __syncthreads();
+  k.mu = (float)s_sc[4];
+
+  if (a.mode == 2) {
+    // ---- backward sweep: per segment, recompute from the checkpoint, then adjoint steps ----
+    const AdjLayout AL(N2, a.nseg, a.every);
+    float* ab = k.ablk;
+    float* dscr = ab ? ab + AL.dvo : nullptr;
+    float* adj = ab ? ab + AL.adj : nullptr;
+    for (int seg = a.nseg - 1; seg >= 0; --seg) {
+      const int s0 = seg * a.every, s1 = min(a.nsteps, s0 + a.every);
+      float* ck = ab ? ab + AL.ck + (long long)seg * 5 * N2 : nullptr;
+      k.gsync();  // partners are done with this CTA's rows of the previous segment
+      k.load_rows(ck, S.u);
+      k.load_rows(ck ? ck + N2 : nullptr, S.v);
+      k.load_rows(ck ? ck + 2 * N2 : nullptr, S.p);
+      if (ab) {
+        k.copy_rows(ck + 3 * N2, dscr);
+        k.copy_rows(ck + 4 * N2, dscr + N2);
+      }
+      k.gdx = dscr;
+      k.gdy = dscr ? dscr + N2 : nullptr;
+      __syncthreads();
+      for (int s = s0; s < s1; ++s) {
+        float* in = ab ? ab + AL.seg + (long long)(s - s0) * 2 * N2 : nullptr;
+        if (in) {
+          k.store_rows(S.u, in);
+          k.store_rows(S.v, in + N2);
+        }
+        k.fwd_step(s, -1);
+      }
+      k.gsync();  // step inputs of the segment written by every CTA of the run
+      k.load_rows(adj, S.u);
+      k.load_rows(adj ? adj + N2 : nullptr, S.v);
+      k.load_rows(adj ? adj + 2 * N2 : nullptr, S.p);
+      __syncthreads();
+      for (int s = s1 - 1; s >= s0; --s) {
+        const float* in = ab ? ab + AL.seg + (long long)(s - s0) * 2 * N2 : nullptr;
+        const double dts = k.rec ? k.rec[2 * s] : 1.0, dto = k.rec ? k.rec[2 * s + 1] : 1.0;
+        k.adj_step(in, in ? in + N2 : nullptr, dts, dto, adj ? adj + 3 * N2 : nullptr, adj ? adj + 4 * N2 : nullptr);
+      }
+      k.store_rows(S.u, adj);
+      k.store_rows(S.v, adj ? adj + N2 : nullptr);
+      k.store_rows(S.p, adj ? adj + 2 * N2 : nullptr);
+    }
+    k.gsync();
+    return;
+  }
+
+  // ---- advance (mode 0) or forward with checkpoints (mode 1) ----
+  k.load_rows(k.gu, S.u);
+  k.load_rows(k.gv, S.v);
+  k.load_rows(k.gp, S.p);
+  __syncthreads();
+  const AdjLayout AL(N2, a.nseg, a.every);
+  for (int step = 0; step < a.nsteps; ++step) {
+    if (a.mode == 1 && step % a.every == 0 && k.ablk) {
+      float* ck = k.ablk + AL.ck + (long long)(step / a.every) * 5 * N2;
+      k.store_rows(S.u, ck);
+      k.store_rows(S.v, ck + N2);
+      k.store_rows(S.p, ck + 2 * N2);
+      k.copy_rows(k.gdx, ck + 3 * N2);
+      k.copy_rows(k.gdy, ck + 4 * N2);
+    }
+    k.fwd_step(-1, a.mode == 1 ? step : -1);
+  }
+
+  // ---- store the state; kinetic energy and max div (FP64 across the run) ----
+  {
+    const float idx = k.idx;
+    float kpart = 0.f, dmax = -INFINITY;
+    for (int t = threadIdx.x; t < k.cells; t += NT) {
+      const int m = fdiv(t, k.fN), i = t - m * N;
+      const int im = (i == 0) ? N - 1 : -1;
+      const int c = t + N;
+      const float uu = S.u[c], vv = S.v[c];
+      if (k.active) {
+        const size_t gi = (size_t)r * M * N + t;
+        k.gu[gi] = uu;
+        k.gv[gi] = vv;
+        k.gp[gi] = S.p[c];
       }
       kpart += uu * uu + vv * vv;
       dmax = fmaxf(dmax, ((uu - S.u[c + im]) + (vv - S.v[c - N])) * idx);
@@ -700,25 +925,25 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
       S.red[3] = ks;
       S.red[4] = (double)dm;
     }
-    gsync();
-    if (threadIdx.x == 0 && r == 0 && active) {
-      double k = 0.0, d = -INFINITY;
-      for (int g = 0; g < G; ++g) {
-        const double* rr = pd(S.red, g);
-        k += rr[3];
+    k.gsync();
+    if (threadIdx.x == 0 && r == 0 && k.active) {
+      double kk = 0.0, d = -INFINITY;
+      for (int g = 0; g < k.G; ++g) {
+        const double* rr = k.peer(S.red, g);
+        kk += rr[3];
         d = fmax(d, rr[4]);
       }
-      RunScal rs = a.scal[run];
+      RunScal rs = a.scal[k.run];
       rs.dt = s_sc[0];
       rs.dt_o = s_sc[1];
       rs.t = s_sc[2];
       rs.maxvel = s_sc[3];
       rs.nan = (int)s_sc[6];
-      rs.ke = 0.5 * k / ((double)N * N);
+      rs.ke = 0.5 * kk / ((double)N * N);
       rs.maxdiv = d;
-      a.scal[run] = rs;
+      a.scal[k.run] = rs;
     }
-    gsync();  // partners finished reading this CTA's partial sums
+    k.gsync();  // partners finished reading this CTA's partial sums
   }
 }
 
@@ -786,6 +1011,13 @@ struct fen_ensemble {
   int exec_steps = -1;
   long long launches = 0;
   bool scal_dirty = false;
+  // forward/adjoint pair
+  int adj_nsteps = 0, adj_every = 0, adj_nseg = 0;
+  bool adj_ready = false;
+  float* abuf = nullptr;
+  long long* d_aoff = nullptr;
+  std::vector<long long> aoff;
+  double* rec = nullptr;
 };
 
 namespace {
@@ -933,8 +1165,9 @@ int build_packs(fen_ensemble* e, const std::vector<int>& subset) {
   return 0;
 }
 
-int launch(fen_ensemble* e, int nsteps) {
+int launch(fen_ensemble* e, int nsteps, int mode = 0) {
   EnsArgs a;
+  memset(&a, 0, sizeof(a));
   a.cls = e->d_cls;
   a.packs = e->d_packs;
   a.npacks = e->npacks;
@@ -945,6 +1178,12 @@ int launch(fen_ensemble* e, int nsteps) {
   a.counter = e->d_counter;
   a.nsteps = nsteps;
   a.cfl = e->cfl;
+  a.mode = mode;
+  a.every = mode ? e->adj_every : 1;
+  a.nseg = mode ? e->adj_nseg : 1;
+  a.abuf = e->abuf;
+  a.aoff = e->d_aoff;
+  a.rec = e->rec;
   EK(cudaMemsetAsync(e->d_counter, 0, sizeof(int), e->stream));
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
@@ -1109,7 +1348,7 @@ int fen_ensemble_destroy(fen_ensemble* e) {
   if (e->exec) cudaGraphExecDestroy(e->exec);
   if (e->graph) cudaGraphDestroy(e->graph);
   for (void* b : e->bufs) cudaFree(b);
-  void* ptrs[] = {e->state, e->d_off, e->d_scal, e->d_cls, e->d_packs, e->d_runlist, e->d_counter};
+  void* ptrs[] = {e->state, e->d_off, e->d_scal, e->d_cls, e->d_packs, e->d_runlist, e->d_counter, e->abuf, e->d_aoff, e->rec};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (e->stream) cudaStreamDestroy(e->stream);
@@ -1215,6 +1454,126 @@ int fen_ensemble_set_config(fen_ensemble* e, int threads, const int* groups) {
 }
 
 long long fen_ensemble_launches(fen_ensemble* e) { return e ? e->launches : 0; }
+
+}  // extern "C"
+
+// ---- forward/adjoint pair -----------------------------------------------------------------
+namespace {
+int timed_launch(fen_ensemble* e, int nsteps, int mode, float* ms) {
+  int r;
+  if ((r = push_scal(e))) return r;
+  cudaEvent_t e0, e1;
+  EK(cudaEventCreate(&e0));
+  EK(cudaEventCreate(&e1));
+  EK(cudaEventRecord(e0, e->stream));
+  if ((r = launch(e, nsteps, mode))) return r;
+  EK(cudaEventRecord(e1, e->stream));
+  EK(cudaEventSynchronize(e1));
+  EK(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  e->launches += 1;
+  return pull_scal(e);
+}
+}  // namespace
+
+extern "C" {
+
+int fen_ensemble_adjoint_setup(fen_ensemble* e, int nsteps, int every) {
+  if (!e || nsteps < 1 || every < 1) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  every = std::min(every, nsteps);
+  const int nseg = (nsteps + every - 1) / every;
+  if (e->abuf) cudaFree(e->abuf);
+  if (e->d_aoff) cudaFree(e->d_aoff);
+  if (e->rec) cudaFree(e->rec);
+  e->abuf = nullptr;
+  e->d_aoff = nullptr;
+  e->rec = nullptr;
+  e->aoff.resize(e->nruns);
+  long long tot = 0;
+  for (int q = 0; q < e->nruns; ++q) {
+    e->aoff[q] = tot;
+    tot += AdjLayout::size((long long)e->n[q] * e->n[q], nseg, every);
+    tot = (tot + 63) / 64 * 64;
+  }
+  cudaError_t ce;
+  if ((ce = cudaMalloc(&e->abuf, tot * sizeof(float))) != cudaSuccess)
+    return fen_internal_fail(FEN_ERR_NOMEM, (std::string("adjoint storage: ") + cudaGetErrorString(ce)).c_str());
+  EK(cudaMemset(e->abuf, 0, tot * sizeof(float)));
+  EK(cudaMalloc(&e->d_aoff, e->nruns * sizeof(long long)));
+  EK(cudaMemcpy(e->d_aoff, e->aoff.data(), e->nruns * sizeof(long long), cudaMemcpyHostToDevice));
+  EK(cudaMalloc(&e->rec, (size_t)e->nruns * nsteps * 2 * sizeof(double)));
+  e->adj_nsteps = nsteps;
+  e->adj_every = every;
+  e->adj_nseg = nseg;
+  e->adj_ready = false;
+  return 0;
+}
+
+int fen_ensemble_adjoint_forward(fen_ensemble* e, double* ms) {
+  if (!e || !e->abuf) return fen_internal_fail(FEN_ERR_STATE, "fen_ensemble_adjoint_setup first");
+  float f = 0.f;
+  int r;
+  if ((r = timed_launch(e, e->adj_nsteps, 1, &f))) return r;
+  if (ms) *ms = f;
+  e->adj_ready = true;
+  for (int q = 0; q < e->nruns; ++q)
+    if (e->scal[q].nan) return fen_internal_fail(FEN_ERR_NAN, ("NaN in the velocity of ensemble run " + std::to_string(q)).c_str());
+  return 0;
+}
+
+int fen_ensemble_adjoint_seed(fen_ensemble* e, int run, const double* lam_u, const double* lam_v) {
+  if (!e || run < 0 || run >= e->nruns || !lam_u || !lam_v) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  if (!e->abuf) return fen_internal_fail(FEN_ERR_STATE, "fen_ensemble_adjoint_setup first");
+  const long long N2 = (long long)e->n[run] * e->n[run];
+  const AdjLayout AL(N2, e->adj_nseg, e->adj_every);
+  std::vector<float> h(5 * N2, 0.f);
+  for (long long k = 0; k < N2; ++k) {
+    h[k] = (float)lam_u[k];
+    h[N2 + k] = (float)lam_v[k];
+  }
+  EK(cudaMemcpy(e->abuf + e->aoff[run] + AL.adj, h.data(), 5 * N2 * sizeof(float), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int fen_ensemble_adjoint_backward(fen_ensemble* e, double* ms) {
+  if (!e || !e->adj_ready) return fen_internal_fail(FEN_ERR_STATE, "fen_ensemble_adjoint_forward first");
+  float f = 0.f;
+  int r;
+  if ((r = timed_launch(e, e->adj_nsteps, 2, &f))) return r;
+  if (ms) *ms = f;
+  return 0;
+}
+
+int fen_ensemble_adjoint_gradient(fen_ensemble* e, int run, double* g_u, double* g_v) {
+  if (!e || run < 0 || run >= e->nruns || !g_u || !g_v) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  if (!e->abuf) return fen_internal_fail(FEN_ERR_STATE, "fen_ensemble_adjoint_setup first");
+  const long long N2 = (long long)e->n[run] * e->n[run];
+  const AdjLayout AL(N2, e->adj_nseg, e->adj_every);
+  std::vector<float> h(2 * N2);
+  EK(cudaMemcpy(h.data(), e->abuf + e->aoff[run] + AL.adj, 2 * N2 * sizeof(float), cudaMemcpyDeviceToHost));
+  for (long long k = 0; k < N2; ++k) {
+    g_u[k] = h[k];
+    g_v[k] = h[N2 + k];
+  }
+  return 0;
+}
+
+int fen_ensemble_adjoint_dts(fen_ensemble* e, int run, double* dt, double* dt_o) {
+  if (!e || run < 0 || run >= e->nruns || !dt || !dt_o) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
+  if (!e->adj_ready) return fen_internal_fail(FEN_ERR_STATE, "fen_ensemble_adjoint_forward first");
+  std::vector<double> h((size_t)2 * e->adj_nsteps);
+  EK(cudaMemcpy(h.data(), e->rec + (size_t)run * e->adj_nsteps * 2, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int s = 0; s < e->adj_nsteps; ++s) {
+    dt[s] = h[2 * s];
+    dt_o[s] = h[2 * s + 1];
+  }
+  return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
 
 // Autotuner: per grid size, the CTAs per run G (tile = N/G rows) among those that fit; then
 // the CTA size.  Each candidate advances a sample of the ensemble's own runs for `steps`

@@ -191,6 +191,21 @@ int fen_ensemble_set_config(fen_ensemble* ens, int threads, const int* groups);
  * NULL) and reuses them when present. */
 int fen_ensemble_tune(fen_ensemble* ens, int steps, const char* cache_path);
 long long fen_ensemble_launches(fen_ensemble* ens);
+/* Forward/adjoint pair of every run: the discrete adjoint of the ensemble step (FP32, the
+ * transpose of the step for the recorded dt sequence, as fen_adjoint_* does for one FP64
+ * context).  setup sizes an nsteps rollout with checkpoints every `every` steps (device
+ * storage of about (5 nsteps/every + 2 every + 7) n^2 floats per run); forward advances every
+ * run nsteps steps in one launch, saving checkpoints and the (dt, dt_o) of each step;
+ * seed sets the sensitivity of each run's loss to its final (u, v); backward sweeps every run
+ * back in one launch (recomputing each segment from its checkpoint) and gradient returns the
+ * gradient with respect to the run's initial (u, v).  Arrays are n*n doubles, x fastest. */
+int fen_ensemble_adjoint_setup(fen_ensemble* ens, int nsteps, int every);
+int fen_ensemble_adjoint_forward(fen_ensemble* ens, double* ms);
+int fen_ensemble_adjoint_seed(fen_ensemble* ens, int run, const double* lam_u, const double* lam_v);
+int fen_ensemble_adjoint_backward(fen_ensemble* ens, double* ms);
+int fen_ensemble_adjoint_gradient(fen_ensemble* ens, int run, double* g_u, double* g_v);
+/* The recorded (dt, dt_o) of each step of the last forward (nsteps doubles each). */
+int fen_ensemble_adjoint_dts(fen_ensemble* ens, int run, double* dt, double* dt_o);
 /* Dynamic + static shared memory per CTA for an n x n run on `groups` CTAs (0 if invalid);
  * host-only, no device needed. */
 size_t fen_ensemble_smem_bytes(int n, int groups);

@@ -77,11 +77,11 @@ class Step:
         gv = Fv_h * 0.5 * (jp(v) + v) + jm(Fv_h * 0.5 * (jp(v) + v)) + C_h * 0.25 * (jp(u) + u) + im(C_h * 0.25 * (jp(u) + u))
         return gu, gv
 
-    # the step
-    def forward(self, x):
+    # the step (S: optional constant body force on u, e.g. Kolmogorov forcing)
+    def forward(self, x, S=None):
         u, v, p, ou, ov = x
         Nu, Nv = self.adv(u, v)
-        du = Nu + self.nu * self.lap(u)
+        du = Nu + self.nu * self.lap(u) + (0.0 if S is None else S)
         dv = Nv + self.nu * self.lap(v)
         gx, gy = self.grad(p)
         us = u + self.dt * (-gx + self.A * du + self.B * ou)
