@@ -302,7 +302,7 @@ def form_adjoint(F, ndir=16, nsteps=500, every=50):
             "workload": "2D decaying turbulence 256^2, nu=2e-3, dt=2e-3, 500 steps, checkpoints every 50, FP64"}
 
 
-def form_ensemble(F, steps=2000, nruns=512, tune_steps=10, sizes=(64, 96, 128, 192, 256)):
+def form_ensemble(F, steps=2000, nruns=512, tune_steps=10, sizes=(64, 96, 128, 192, 256), adjoint=True):
     """Batched ensemble: 512 independent 2D Kolmogorov runs (N ~ U{64, 96, 128, 192, 256},
     Re ~ U[50, 500], forcing sin(4y), noise 1e-2, CFL 0.4) advanced `steps` steps in one
     persistent launch, FP32 with FP64 reductions, tile shapes from the autotuner."""
@@ -321,11 +321,24 @@ def form_ensemble(F, steps=2000, nruns=512, tune_steps=10, sizes=(64, 96, 128, 1
     launches = e.launches() - l0
     cells = int(np.sum(n.astype(np.int64) ** 2))
     st = [e.status(q) for q in range(nruns)]
+    # forward/adjoint pair of every run: loss 1/2 |u_T|^2 per run, checkpoints every 50 steps
+    adj = None
+    if adjoint:
+        e.adjoint_setup(steps, min(50, steps))
+        fwd_ms = e.adjoint_forward()
+        for q in range(nruns):
+            uT, vT, _ = e.download(q)
+            e.adjoint_seed(q, uT, vT)
+        bwd_ms = e.adjoint_backward()
+        g = [e.adjoint_gradient(q) for q in range(min(nruns, 4))]
+        adj = {"forward_ms": round(fwd_ms, 3), "backward_ms": round(bwd_ms, 3),
+               "ratio_backward_over_forward": round(bwd_ms / fwd_ms, 3), "checkpoint_every": min(50, steps),
+               "finite": bool(all(np.isfinite(x).all() for pair in g for x in pair))}
     e.destroy()
     return {"value": round(cells * steps / (ms / 1e3) / 1e6, 3), "unit": "Mcell-steps/s", "ms": round(ms, 3),
             "runs": nruns, "cells": cells, "steps": steps, "launches": launches, "config": cfg,
             "tune_s": round(tune_s, 2), "max_maxdiv": max(abs(s["maxdiv"]) for s in st),
-            "any_nan": any(s["nan"] for s in st),
+            "any_nan": any(s["nan"] for s in st), "adjoint_pair": adj,
             "workload": f"{nruns} 2D Kolmogorov runs, N~U{{64..256}}, Re~U[50,500], CFL 0.4, {steps} steps, FP32"}
 
 

@@ -800,7 +800,9 @@ struct Pk {
   }
 };
 
-template <int NT>
+// MODE 0: advance; 1: advance with checkpoints and the dt record; 2: backward sweep.  The
+// mode is a template parameter so the advance kernel carries no adjoint code (registers).
+template <int NT, int MODE>
 __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, int q, cg::cluster_group& cl,
                          unsigned char* smem, double* s_sc, float* s_f, double* s_rd, float* s_rf) {
   Pk<NT> k(a, P, D, q, cl, smem, s_sc, s_f, s_rd, s_rf);
@@ -837,7 +839,7 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
   __syncthreads();
   k.mu = (float)s_sc[4];
 
-  if (a.mode == 2) {
+  if (MODE == 2) {
     // ---- backward sweep: per segment, recompute from the checkpoint, then adjoint steps ----
     const AdjLayout AL(N2, a.nseg, a.every);
     float* ab = k.ablk;
@@ -890,7 +892,7 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
   __syncthreads();
   const AdjLayout AL(N2, a.nseg, a.every);
   for (int step = 0; step < a.nsteps; ++step) {
-    if (a.mode == 1 && step % a.every == 0 && k.ablk) {
+    if (MODE == 1 && step % a.every == 0 && k.ablk) {
       float* ck = k.ablk + AL.ck + (long long)(step / a.every) * 5 * N2;
       k.store_rows(S.u, ck);
       k.store_rows(S.v, ck + N2);
@@ -898,7 +900,7 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
       k.copy_rows(k.gdx, ck + 3 * N2);
       k.copy_rows(k.gdy, ck + 4 * N2);
     }
-    k.fwd_step(-1, a.mode == 1 ? step : -1);
+    k.fwd_step(-1, MODE == 1 ? step : -1);
   }
 
   // ---- store the state; kinetic energy and max div (FP64 across the run) ----
@@ -947,7 +949,7 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
   }
 }
 
-template <int NT>
+template <int NT, int MODE>
 __global__ void __launch_bounds__(NT, 1) k_ensemble(EnsArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_pack;
@@ -967,7 +969,7 @@ __global__ void __launch_bounds__(NT, 1) k_ensemble(EnsArgs a) {
     const Pack P = a.packs[pk];
     if (threadIdx.x == 0) s_D = a.cls[P.cls];
     __syncthreads();
-    run_pack<NT>(a, P, s_D, q, cl, smem, s_sc, s_f, s_rd, s_rf);
+    run_pack<NT, MODE>(a, P, s_D, q, cl, smem, s_sc, s_f, s_rd, s_rf);
     __syncthreads();
   }
 }
@@ -1098,8 +1100,9 @@ void set_g(ClassDesc& D, int G) {
   D.tabs = smem_bytes(D.N, G, nullptr, true) + kSmemReserve <= kSmemLimit;
 }
 
-const void* kernel_ptr(int threads) {
-  return threads == 512 ? (const void*)k_ensemble<512> : (const void*)k_ensemble<1024>;
+const void* kernel_ptr(int threads, int mode = 0) {
+  if (threads == 512) return mode == 0 ? (const void*)k_ensemble<512, 0> : mode == 1 ? (const void*)k_ensemble<512, 1> : (const void*)k_ensemble<512, 2>;
+  return mode == 0 ? (const void*)k_ensemble<1024, 0> : mode == 1 ? (const void*)k_ensemble<1024, 1> : (const void*)k_ensemble<1024, 2>;
 }
 
 // Pack the runs `subset` (all runs when empty) with the current G per class; uploads the
@@ -1143,7 +1146,8 @@ int build_packs(fen_ensemble* e, const std::vector<int>& subset) {
   e->npacks = (int)packs.size();
   e->smem = smem;
   const void* k = kernel_ptr(e->threads);
-  EK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1)));
+  for (int m = 0; m < 3; ++m)
+    EK(cudaFuncSetAttribute(kernel_ptr(e->threads, m), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1)));
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1197,8 +1201,15 @@ int launch(fen_ensemble* e, int nsteps, int mode = 0) {
   cfg.stream = e->stream;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  if (e->threads == 512) EK(cudaLaunchKernelEx(&cfg, k_ensemble<512>, a));
-  else EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024>, a));
+  if (e->threads == 512) {
+    if (mode == 0) EK(cudaLaunchKernelEx(&cfg, k_ensemble<512, 0>, a));
+    else if (mode == 1) EK(cudaLaunchKernelEx(&cfg, k_ensemble<512, 1>, a));
+    else EK(cudaLaunchKernelEx(&cfg, k_ensemble<512, 2>, a));
+  } else {
+    if (mode == 0) EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024, 0>, a));
+    else if (mode == 1) EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024, 1>, a));
+    else EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024, 2>, a));
+  }
   EK(cudaGetLastError());
   return 0;
 }
