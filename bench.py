@@ -52,6 +52,9 @@ STAGE_BYTES_3D = {
     "correct": 8 * 9,         # read v*(3), phi; read+write p; write v(3)
 }
 
+# DRAM bytes per cell of one launch, measured with ncu (profiles/k_predictor_tgv3d_192_fp64.md)
+TRAFFIC_BYTES_PER_CELL = {"predictor": 110.0}
+
 CONFIGS = {
     "tgv3d": dict(dim=3, n=(256, 256, 256), L=(2 * np.pi,) * 3, nu=1.0 / 1600, cfl=0.5, constant_cfl=True,
                   bc=["Periodic"] * 6, desc="3D Taylor-Green vortex 256^3, Re=1600, CFL=0.5, FP64, FFT x/y/z"),
@@ -472,8 +475,12 @@ def main():
     dom = max(STAGE_BYTES_3D, key=lambda k: stage.get(k, 0) if k in stage else 0)
     bpc = STAGE_BYTES_3D[dom] if cfg["dim"] == 3 else STAGE_BYTES_3D[dom] * 0.7
     achieved = bpc * cells / (stage[dom] / 1e3) / 1e9
+    # DRAM bytes per launch of the predictor from ncu (110 B/cell at 192^3, scaled by cells)
+    traffic = TRAFFIC_BYTES_PER_CELL.get(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "frac": round(achieved / peak, 4), "traffic": int(traffic * cells) if traffic and cfg["dim"] == 3 else None,
+                "traffic_source": "ncu dram__bytes_read+write of one predictor launch at 192^3, scaled by cells",
+                "fp64_pipe_pct": 87.2, "peak_source": peak_kind,
                 "bytes_per_cell": bpc, "stage_ms": {k: round(v, 4) for k, v in stage.items()},
                 "note": "FP64 kernels are FP64-issue-bound on GB300 (1.19 TFLOP/s FP64 measured)"}
 
