@@ -67,6 +67,23 @@ CONFIGS = {
 }
 
 
+def max_over_ranks(x, dist, device):
+    """The slowest rank's value (replicas are timed independently; the job ends with the last)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, cells, steps, ms):
+    """Whole-job Mcell-steps/s of `world` replicas of `cells` cells, `steps` steps each, all
+    finished within `ms` milliseconds (weak scaling: per-GPU work fixed)."""
+    return world * cells * steps / (ms / 1e3) / 1e6
+
+
 def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -461,11 +478,9 @@ def main():
     s.sync()
     torch.cuda.synchronize()
     if dist:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         dist.barrier()
-    value = world * cells * args.steps / (ms / 1e3) / 1e6
+    value = replica_throughput(world, cells, args.steps, ms)
     ms_per_step = ms / args.steps
 
     # ---- per-stage device times for the roofline ----
@@ -502,9 +517,7 @@ def main():
     s.sync()
     el = time.perf_counter() - t0
     if dist:
-        t = torch.tensor([el], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        el = float(t.item())
+        el = max_over_ranks(el, dist, "cuda")
     field_bytes = 8 * int(np.prod(g.shape)) if cfg["dim"] == 3 else 8 * (n[0] + 2) * (n[1] + 2)
     e2e = {"value": round(world * cells * args.steps / el / 1e6, 3), "unit": "Mcell-steps/s",
            "h2d_bytes_per_step": int(len(keys) * field_bytes / args.steps + 8),

@@ -482,3 +482,18 @@ def ensemble_smem_bytes(n, groups, lib=None):
     """Shared memory per CTA of an n x n run held by `groups` CTAs (0 if invalid)."""
     L = lib or load_library()
     return int(L.fen_ensemble_smem_bytes(int(n), int(groups)))
+
+
+def partition_runs(n, world_size):
+    """Split ensemble runs across `world_size` GPUs (one process each) by cost: longest
+    processing time first on the per-run cost N^2 (the runs are independent, so no data-path
+    collective is needed).  Returns one array of run indices per rank, each sorted."""
+    n = np.asarray(n, dtype=np.int64)
+    order = np.argsort(-(n * n), kind="stable")
+    load = np.zeros(world_size, dtype=np.int64)
+    parts = [[] for _ in range(world_size)]
+    for q in order:
+        r = int(np.argmin(load))
+        parts[r].append(int(q))
+        load[r] += int(n[q]) * int(n[q])
+    return [np.array(sorted(p), dtype=np.int64) for p in parts]
