@@ -30,6 +30,7 @@ LEFT, RIGHT, BOTTOM, TOP, FRONT, BACK = range(6)
 U, V, W, P, PHI = 0, 1, 2, 3, 4
 DVO_X, DVO_Y, DVO_Z = 5, 6, 7
 S_X, S_Y, S_Z = 8, 9, 10
+RHO, MU, P_O = 11, 12, 13  # cell density, cell viscosity, old pressure of the split
 FP64, MIXED = 0, 1
 SOLVER_NAMES = ["pp", "pn", "nn", "ppp", "ppn", "npn", "nnn", "pnp"]
 
@@ -72,7 +73,7 @@ _EXPORTS = [
     "fen_ensemble_status", "fen_ensemble_config", "fen_ensemble_set_config", "fen_ensemble_tune",
     "fen_ensemble_launches", "fen_ensemble_smem_bytes", "fen_ensemble_adjoint_setup", "fen_ensemble_adjoint_forward",
     "fen_ensemble_adjoint_seed", "fen_ensemble_adjoint_backward", "fen_ensemble_adjoint_gradient",
-    "fen_ensemble_adjoint_dts",
+    "fen_ensemble_adjoint_dts", "fen_set_split_pressure",
 ]
 
 
@@ -111,6 +112,7 @@ def load_library(path=None):
     L.fen_load_state.argtypes = [vp, ctypes.c_char_p]
     L.fen_save_fields.argtypes = [vp, ctypes.c_char_p, ip]
     L.fen_adjoint_setup.argtypes = [vp, ip, ip]
+    L.fen_set_split_pressure.argtypes = [vp, ctypes.c_double]
     L.fen_adjoint_forward.argtypes = [vp, ctypes.c_double]
     L.fen_adjoint_backward.argtypes = [vp, dp, dp, dp, dp, dp]
     cip = ctypes.POINTER(ctypes.c_int)
@@ -313,6 +315,12 @@ class Solver:
 
     def save_fields(self, step, directory="data"):
         self._check(self._L.fen_save_fields(self._h, directory.encode(), int(step)))
+
+    # -- variable-property path (navier_stokes.f90:80-136, 357-452; FP64) ---------------------
+    def set_split_pressure(self, rhomin):
+        """Dodd-Ferrante split pressure of FEN's multiphase step with minimum density rhomin
+        (p_o = FEN field P_O); density and viscosity fields are RHO and MU (set_field)."""
+        self._check(self._L.fen_set_split_pressure(self._h, float(rhomin)))
 
     # -- discrete adjoint (2D periodic FP64) ------------------------------------------------
     def adjoint_setup(self, nsteps, every):

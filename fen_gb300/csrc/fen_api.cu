@@ -26,6 +26,7 @@
 #include "../../include/fen_gpu.h"
 #include "fen_adjoint.cuh"
 #include "fen_kernels.cuh"
+#include "fen_varprop.cuh"
 #include "fen_types.cuh"
 
 using namespace fen;
@@ -112,6 +113,10 @@ struct fen_ctx {
   float* d32l[3] = {nullptr, nullptr, nullptr};    // increment lo (pairs with d32)
   float* dvo32l[3] = {nullptr, nullptr, nullptr};  // dv_o lo (pairs with dvo32)
   double* tmp64 = nullptr;                         // FP64 staging of dv_o pairs
+  // variable-property path (FP64)
+  double *rho = nullptr, *mu = nullptr, *p_o = nullptr;
+  int var_rho = 0, var_mu = 0, split = 0;
+  double rhomin = 1.0;
   float* S32[3] = {nullptr, nullptr, nullptr};
   int has_S = 0;
   // poisson
@@ -589,6 +594,7 @@ int launch_stage_t(fen_ctx* c, const Stage& s, int first_from_field, const void*
       a.pu = DFField{c->u32, c->u32l}; a.pv = DFField{c->v32, c->v32l}; a.pw = DFField{c->w32, c->w32l};
     } else {
       a.fu = (const T*)c->us; a.fv = (const T*)c->vs; a.fw = (const T*)c->ws;
+      if (c->var_rho && !c->split) a.rho_c = c->rho;
     }
   }
   return (c->dim == 3) ? launch_line_dim<T, 3>(c, s, ld, a) : launch_line_dim<T, 2>(c, s, ld, a);
@@ -674,6 +680,14 @@ int run_poisson(fen_ctx* c, bool from_field) {
 
 double rhof_of(fen_ctx* c) { return 0.5 * (c->prm.density + c->prm.density); }
 
+// The step takes FEN's variable-property branches when a density or viscosity field was
+// uploaded or the split pressure is on.
+bool var_path(const fen_ctx* c) { return c->var_rho || c->var_mu || c->split; }
+
+// Density of the Poisson scaling rho_over_dt: 1 with a density field (the loader multiplies
+// by rho(i,j,k)), rhomin with the split, else the constant density.
+double rho_scale(const fen_ctx* c) { return c->split ? c->rhomin : (c->var_rho ? 1.0 : c->prm.density); }
+
 template <typename T>
 PredArgs<T> pred_args(fen_ctx* c) {
   PredArgs<T> a;
@@ -738,6 +752,31 @@ int launch_predictor(fen_ctx* c, const StepScalars* sc) {
     pa.has_S = c->has_S;
     if (c->dim == 3) k_predictor_df<3><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
     else k_predictor_df<2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+  } else if (var_path(c)) {
+    VarArgs va;
+    memset(&va, 0, sizeof(va));
+    va.u = c->u; va.v = c->v; va.w = c->w; va.p = c->p;
+    va.us = c->us; va.vs = c->vs; va.ws = c->ws;
+    va.dox = c->dvo[0]; va.doy = c->dvo[1]; va.doz = c->dvo[2];
+    va.Sx = c->S[0]; va.Sy = c->S[1]; va.Sz = c->S[2];
+    va.rho = c->var_rho ? c->rho : nullptr;
+    va.mu = c->mu;
+    va.po = c->p_o;
+    va.density = c->prm.density;
+    va.viscosity = c->prm.viscosity;
+    for (int q = 0; q < 3; ++q) {
+      va.g[q] = c->prm.g[q];
+      va.id[q] = 1.0 / c->d[q];
+      va.id2[q] = 1.0 / (c->d[q] * c->d[q]);
+    }
+    va.irhomin = 1.0 / c->rhomin;
+    va.iso = c->iso;
+    va.has_S = c->has_S;
+    va.var_mu = c->var_mu;
+    va.split = c->split;
+    va.constant_cfl = c->prm.constant_cfl;
+    if (c->dim == 3) k_predictor_var<3><<<grid, 256, 0, c->stream>>>(c->L, sc, va);
+    else k_predictor_var<2><<<grid, 256, 0, c->stream>>>(c->L, sc, va);
   } else {
     PredArgs<double> pa = pred_args<double>(c);
     if (c->dim == 3) k_predictor<3><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
@@ -836,7 +875,7 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
   int e = 0;
   auto mark = [&]() { if (ev) cudaEventRecord(ev[e++], c->stream); };
   mark();
-  k_prologue<<<1, 32, 0, c->stream>>>(c->sc, c->prm.constant_cfl, c->prm.cfl, c->dmin, c->prm.density, rhof_of(c));
+  k_prologue<<<1, 32, 0, c->stream>>>(c->sc, c->prm.constant_cfl, c->prm.cfl, c->dmin, rho_scale(c), rhof_of(c));
   c->launches++;
   if ((r = launch_predictor(c, c->sc))) return r;
   mark();  // 1: predictor
@@ -908,19 +947,41 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
     double* f[1] = {c->phi};
     int ids[1] = {FEN_PHI};
     if ((r = ghost<double>(c, 1, f, ids))) return r;
-    CorrArgs<double> ca;
-    memset(&ca, 0, sizeof(ca));
-    ca.us = c->us; ca.vs = c->vs; ca.ws = c->ws; ca.phi = c->phi;
-    ca.u = c->u; ca.v = c->v; ca.w = c->w; ca.p = c->p;
-    for (int q = 0; q < 3; ++q) ca.id[q] = 1.0 / c->d[q];
-    ca.iso = c->iso;
-    ca.use_dev_dt = 1;
-    ca.rhof = rhof_of(c);
-    ca.rhof_one = (ca.rhof == 1.0);
-    if (c->dim == 3) k_correct<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
-    else k_correct<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
-    c->launches++;
-    CK(cudaGetLastError());
+    if (var_path(c)) {
+      CorrVarArgs va;
+      memset(&va, 0, sizeof(va));
+      va.us = c->us; va.vs = c->vs; va.ws = c->ws; va.phi = c->phi;
+      va.u = c->u; va.v = c->v; va.w = c->w; va.p = c->p; va.po = c->p_o;
+      va.rho = c->var_rho ? c->rho : nullptr;
+      va.density = c->prm.density;
+      va.irhomin = 1.0 / c->rhomin;
+      for (int q = 0; q < 3; ++q) va.id[q] = 1.0 / c->d[q];
+      va.iso = c->iso;
+      va.split = c->split;
+      if (c->dim == 3) k_correct_var<3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, va);
+      else k_correct_var<2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, va);
+      c->launches++;
+      CK(cudaGetLastError());
+      if (c->split) {
+        double* f[1] = {c->p_o};
+        int ids[1] = {FEN_P};
+        if ((r = ghost<double>(c, 1, f, ids))) return r;
+      }
+    } else {
+      CorrArgs<double> ca;
+      memset(&ca, 0, sizeof(ca));
+      ca.us = c->us; ca.vs = c->vs; ca.ws = c->ws; ca.phi = c->phi;
+      ca.u = c->u; ca.v = c->v; ca.w = c->w; ca.p = c->p;
+      for (int q = 0; q < 3; ++q) ca.id[q] = 1.0 / c->d[q];
+      ca.iso = c->iso;
+      ca.use_dev_dt = 1;
+      ca.rhof = rhof_of(c);
+      ca.rhof_one = (ca.rhof == 1.0);
+      if (c->dim == 3) k_correct<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
+      else k_correct<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ca);
+      c->launches++;
+      CK(cudaGetLastError());
+    }
   }
   mark();  // 6: phi ghost + correction
   {
@@ -1041,6 +1102,7 @@ int fen_ctx_destroy(fen_ctx* c) {
                  c->dphi32, c->res32, c->d32l[0], c->d32l[1], c->d32l[2], c->dvo32l[0], c->dvo32l[1], c->dvo32l[2]};
   for (float* b : fb) if (b) cudaFree(b);
   if (c->tmp64) cudaFree(c->tmp64);
+  for (double* b : {c->rho, c->mu, c->p_o}) if (b) cudaFree(b);
   for (int f = 0; f < 5; ++f) for (int q = 0; q < 6; ++q) if (c->bcval[f][q]) cudaFree(c->bcval[f][q]);
   if (c->specC) cudaFree(c->specC);
   if (c->specR) cudaFree(c->specR);
@@ -1148,11 +1210,39 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
   return 0;
 }
 
+// Density, viscosity and old-pressure fields of the variable-property path, allocated on
+// first use with FEN's initial values (rho%f = density, mu%f = viscosity, p_o = 0).
+int prop_field(fen_ctx* c, int f, double** out) {
+  double** slot = (f == FEN_RHO) ? &c->rho : (f == FEN_MU) ? &c->mu : &c->p_o;
+  if (!*slot) {
+    if (c->mixed) return fail(FEN_ERR_ARG, "the variable-property path runs in FP64 contexts only");
+    if (f == FEN_MU && c->dim == 3)
+      return fail(FEN_ERR_ARG, "variable viscosity is 2D only (FEN's 3D stress-divergence branch is empty)");
+    int r;
+    if ((r = alloc(slot, c->L.total))) return r;
+    const double v0 = (f == FEN_RHO) ? c->prm.density : (f == FEN_MU) ? c->prm.viscosity : 0.0;
+    if (v0 != 0.0) {
+      std::vector<double> h((size_t)c->L.total, v0);
+      CK(cudaMemcpy(*slot, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    drop_graph(c);
+  }
+  *out = *slot;
+  return 0;
+}
+
 int fen_upload(fen_ctx* c, int f, const double* host) {
   if (!c || !host) return fail(FEN_ERR_ARG, "null argument");
-  if (f < FEN_U || f > FEN_S_Z || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
+  if (f < FEN_U || f > FEN_P_O || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
   double* hrw = const_cast<double*>(host);
   int r;
+  if (f >= FEN_RHO) {
+    double* d;
+    if ((r = prop_field(c, f, &d))) return r;
+    if (f == FEN_RHO && !c->var_rho) { c->var_rho = 1; drop_graph(c); }
+    if (f == FEN_MU && !c->var_mu) { c->var_mu = 1; drop_graph(c); }
+    return relayout<double>(c, d, hrw, 0);
+  }
   if (f >= FEN_S_X && f <= FEN_S_Z) {
     // S is used in every component once any is set (dv += S/rhof, navier_stokes.f90:245-255)
     for (int q = 0; q < 3; ++q) {
@@ -1185,7 +1275,13 @@ int fen_upload(fen_ctx* c, int f, const double* host) {
 
 int fen_download(fen_ctx* c, int f, double* host) {
   if (!c || !host) return fail(FEN_ERR_ARG, "null argument");
-  if (f < FEN_U || f > FEN_S_Z || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
+  if (f < FEN_U || f > FEN_P_O || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
+  if (f >= FEN_RHO) {
+    double* d;
+    int r;
+    if ((r = prop_field(c, f, &d))) return r;
+    return relayout<double>(c, d, host, 1);
+  }
   if (f >= FEN_S_X && f <= FEN_S_Z) {
     if (!c->has_S) {
       const size_t nh = (size_t)(c->n[0] + 2) * (c->n[1] + 2) * host_planes(c);
@@ -1211,6 +1307,16 @@ int fen_download(fen_ctx* c, int f, double* host) {
 
 int fen_update_ghost_nodes(fen_ctx* c, int f) {
   if (!c) return fail(FEN_ERR_ARG, "null argument");
+  if (f >= FEN_RHO && f <= FEN_P_O) {  // rho, mu, p_o take p's boundary types
+    double* d;
+    int r;
+    if ((r = prop_field(c, f, &d))) return r;
+    double* p[1] = {d};
+    int ids[1] = {FEN_P};
+    if ((r = ghost<double>(c, 1, p, ids))) return r;
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+  }
   if (f < FEN_U || f > FEN_PHI || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "field has no ghost nodes");
   int ids[1] = {f};
   int r;
@@ -1591,7 +1697,7 @@ int adj_step(fen_ctx* c, const double* u, const double* v) {
 
 int fen_adjoint_setup(fen_ctx* c, int nsteps, int every) {
   if (!c || nsteps < 1 || every < 1) return fail(FEN_ERR_ARG, "bad argument");
-  if (c->dim != 2 || c->mixed || c->solver != S_PP || c->prm.constant_cfl || c->has_S)
+  if (c->dim != 2 || c->mixed || c->solver != S_PP || c->prm.constant_cfl || c->has_S || var_path(c))
     return fail(FEN_ERR_ARG, "the adjoint covers 2D periodic FP64 runs with fixed dt and no source field");
   auto& A = c->adj;
   for (double* b : A.ckpt) if (b) cudaFree(b);
@@ -1694,6 +1800,18 @@ int fen_adjoint_backward(fen_ctx* c, const double* lam_u, const double* lam_v, d
     ms[0] = A.bwd_ms;
     ms[1] = A.fwd_ms;
   }
+  return 0;
+}
+
+int fen_set_split_pressure(fen_ctx* c, double rhomin) {
+  if (!c || !(rhomin > 0.0)) return fail(FEN_ERR_ARG, "bad argument");
+  if (c->mixed) return fail(FEN_ERR_ARG, "the variable-property path runs in FP64 contexts only");
+  double* d;
+  int r;
+  if ((r = prop_field(c, FEN_P_O, &d))) return r;
+  c->split = 1;
+  c->rhomin = rhomin;
+  drop_graph(c);
   return 0;
 }
 

@@ -165,6 +165,7 @@ struct LineArgs {
   Layout L;
   const T *fu, *fv, *fw;  // predicted velocity for LD_DIV (the increment's hi part for LD_DIVMIX)
   const float *ful, *fvl, *fwl;  // LD_DIVMIX: the increment's lo part
+  const double* rho_c;           // LD_DIV with variable density: div * rho(i,j,k) * rho_over_dt (= 1/dt)
   DFField pu, pv, pw;     // pair velocity of the mixed form (LD_DIVMIX)
   F2 idp[3];              // 1/delta per axis as float pairs (LD_DIVMIX)
   const T* fsrc;          // LD_FIELD source
@@ -239,7 +240,11 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
           int j, k;
           row_jk<DIM>(line0 + l, outer, j, k);
           if (LD == LD_FIELD) x = a.fsrc[a.L.idx(i + 1, j, kst<DIM>(k))];
-          else if (LD == LD_DIV) x = div_at<T, DIM>(a, i + 1, j, k) * (T)a.sc->rho_over_dt;
+          else if (LD == LD_DIV) {
+            x = div_at<T, DIM>(a, i + 1, j, k);
+            if (a.rho_c) x = x * (T)a.rho_c[a.L.idx(i + 1, j, kst<DIM>(k))];
+            x = x * (T)a.sc->rho_over_dt;
+          }
           else {
             const F2 dd = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
                                       a.ful, a.fvl, a.fwl,

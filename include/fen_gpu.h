@@ -30,7 +30,11 @@ enum { FEN_LEFT = 0, FEN_RIGHT = 1, FEN_BOTTOM = 2, FEN_TOP = 3, FEN_FRONT = 4, 
 enum {
   FEN_U = 0, FEN_V = 1, FEN_W = 2, FEN_P = 3, FEN_PHI = 4,
   FEN_DVO_X = 5, FEN_DVO_Y = 6, FEN_DVO_Z = 7,
-  FEN_S_X = 8, FEN_S_Y = 9, FEN_S_Z = 10
+  FEN_S_X = 8, FEN_S_Y = 9, FEN_S_Z = 10,
+  /* cell-centred density and viscosity fields and the old pressure of the split
+   * (navier_stokes.f90:36, multiphase.f90:25): uploading FEN_RHO or FEN_MU switches the
+   * FP64 step to FEN's variable-property branches */
+  FEN_RHO = 11, FEN_MU = 12, FEN_P_O = 13
 };
 /* Arithmetic forms. */
 enum { FEN_FP64 = 0, FEN_MIXED = 1 };
@@ -131,6 +135,15 @@ int fen_adjoint_setup(fen_ctx* ctx, int nsteps, int every);
 int fen_adjoint_forward(fen_ctx* ctx, double dt);
 int fen_adjoint_backward(fen_ctx* ctx, const double* lam_u, const double* lam_v, double* g_u, double* g_v,
                          double* ms);
+
+/* Variable-property momentum path (FP64 contexts).  Upload FEN_RHO (cell density) and/or
+ * FEN_MU (cell viscosity; 2D only, as FEN's stress-divergence branch, navier_stokes.f90:
+ * 405-452) and fill their ghosts with fen_update_ghost_nodes (p's boundary rules).  The step
+ * then divides by the face densities center_to_face(rho) (fields.f90:175-206) and scales the
+ * Poisson right-hand side by rho(i,j,k)/dt.  fen_set_split_pressure turns on the Dodd-
+ * Ferrante split of FEN's multiphase step (navier_stokes.f90:80-96, 113, 174-184, 526-531,
+ * 557) with the minimum density rhomin; the old pressure is FEN_P_O (zero until uploaded). */
+int fen_set_split_pressure(fen_ctx* ctx, double rhomin);
 
 /* Synchronise the context stream. */
 int fen_sync(fen_ctx* ctx);

@@ -176,6 +176,12 @@ struct Oracle {
   int constant_CFL = 0;
   Field u, v, w, p, phi;
   std::vector<double> dv[3], dvo[3], S[3];
+  // variable-property path: cell-centred rho and mu (navier_stokes.f90:36, 761-775), the old
+  // pressure p_o of the Dodd-Ferrante split (multiphase.f90:25, navier_stokes.f90:80-96)
+  Field rho, mu, p_o;
+  int var_mu = 0;          // constant_viscosity = .false. (navier_stokes.f90:45, 405-452)
+  int split = 0;           // Dodd-Ferrante split pressure with rhomin (the MF branches)
+  double rhomin = 1.0, irhomin = 1.0;
   // poisson_mod state (poisson.f90:31-49)
   int solver = -1;
   std::vector<double> mwn[3];
@@ -358,29 +364,68 @@ static inline double lap_w_at(const Oracle& o, const double* F, size_t c) {
 }
 
 // compute_explicit_terms (navier_stokes.f90:217-257) with the constant-viscosity
-// diffusion branch (:384-404): dv = adv + mu*lap(v)/rhof + S/rhof.
+// center_to_face(rho, rhof) (fields.f90:175-206) at the q-face of cell c.
+static inline double rhof_at(const Oracle& o, size_t c, int q) {
+  const size_t so[3] = {1, o.nx(), o.plane()};
+  return 0.5 * (o.rho.f[c + so[q]] + o.rho.f[c]);
+}
+
+// compute_explicit_terms (navier_stokes.f90:217-257): advection, then add_diffusion
+// (:357-452): mu%f(i,j,k)*lap(v)/rhof with constant viscosity, the stress divergence
+// div(2 mu D)/rhof with variable viscosity (2D only: the reference's 3D branch is empty),
+// then S/rhof.
 static void compute_explicit_terms(Oracle& o, std::vector<double>* R) {
   for (int c = 0; c < o.dim; ++c) std::fill(R[c].begin(), R[c].end(), 0.0);
   add_advection(o, R);
-  const double rhof = 0.5 * (o.density + o.density);  // center_to_face of a constant field
-  const double mu = o.viscosity;
   const int K = (o.dim == 3) ? o.n[2] : 1;
   const double* F[3] = {o.u.f.data(), o.v.f.data(), o.w.f.data()};
+  const double* mu = o.mu.f.data();
+  if (!o.var_mu) {
+    OMP_FOR
+    for (int k = 1; k <= K; ++k)
+      for (int j = 1; j <= o.n[1]; ++j)
+        for (int i = 1; i <= o.n[0]; ++i) {
+          const size_t c = o.I(i, j, k);
+          R[0][c] = R[0][c] + mu[c] * lap_at(o, F[0], c) / rhof_at(o, c, 0);
+          R[1][c] = R[1][c] + mu[c] * lap_at(o, F[1], c) / rhof_at(o, c, 1);
+          if (o.dim == 3) R[2][c] = R[2][c] + mu[c] * lap_w_at(o, F[2], c) / rhof_at(o, c, 2);
+        }
+  } else if (o.dim == 2) {
+    const double idelta = 1.0 / o.d[0];
+    const size_t sy = o.nx();
+    const double* U = F[0];
+    const double* V = F[1];
+    OMP_FOR
+    for (int k = 1; k <= K; ++k)
+      for (int j = 1; j <= o.n[1]; ++j)
+        for (int i = 1; i <= o.n[0]; ++i) {
+          const size_t c = o.I(i, j, k);
+          const size_t ip = c + 1, im = c - 1, jp = c + sy, jm = c - sy;
+          const double tauxxip = 2.0 * mu[ip] * (U[ip] - U[c]) * idelta;
+          const double tauxxim = 2.0 * mu[c] * (U[c] - U[im]) * idelta;
+          const double dtauxxdx = (tauxxip - tauxxim) * idelta;
+          const double tauxyjp = 0.25 * (mu[c] + mu[ip] + mu[jp] + mu[ip + sy]) *
+                                 ((U[jp] - U[c]) * idelta + (V[ip] - V[c]) * idelta);
+          const double tauxyjm = 0.25 * (mu[jm] + mu[ip - sy] + mu[c] + mu[ip]) *
+                                 ((U[c] - U[jm]) * idelta + (V[ip - sy] - V[jm]) * idelta);
+          const double dtauxydy = (tauxyjp - tauxyjm) * idelta;
+          R[0][c] = R[0][c] + (dtauxxdx + dtauxydy) / rhof_at(o, c, 0);
+          const double tauyxip = tauxyjp;
+          const double tauyxim = 0.25 * (mu[im] + mu[c] + mu[im + sy] + mu[jp]) *
+                                 ((U[im + sy] - U[im]) * idelta + (V[c] - V[im]) * idelta);
+          const double dtauyxdx = (tauyxip - tauyxim) * idelta;
+          const double tauyyjp = 2.0 * mu[jp] * (V[jp] - V[c]) * idelta;
+          const double tauyyjm = 2.0 * mu[c] * (V[c] - V[jm]) * idelta;
+          const double dtauyydy = (tauyyjp - tauyyjm) * idelta;
+          R[1][c] = R[1][c] + (dtauyxdx + dtauyydy) / rhof_at(o, c, 1);
+        }
+  }
   OMP_FOR
   for (int k = 1; k <= K; ++k)
     for (int j = 1; j <= o.n[1]; ++j)
       for (int i = 1; i <= o.n[0]; ++i) {
         const size_t c = o.I(i, j, k);
-        R[0][c] = R[0][c] + mu * lap_at(o, F[0], c) / rhof;
-        R[1][c] = R[1][c] + mu * lap_at(o, F[1], c) / rhof;
-        if (o.dim == 3) R[2][c] = R[2][c] + mu * lap_w_at(o, F[2], c) / rhof;
-      }
-  OMP_FOR
-  for (int k = 1; k <= K; ++k)
-    for (int j = 1; j <= o.n[1]; ++j)
-      for (int i = 1; i <= o.n[0]; ++i) {
-        const size_t c = o.I(i, j, k);
-        for (int q = 0; q < o.dim; ++q) R[q][c] = R[q][c] + o.S[q][c] / rhof;
+        for (int q = 0; q < o.dim; ++q) R[q][c] = R[q][c] + o.S[q][c] / rhof_at(o, c, q);
       }
 }
 
@@ -780,8 +825,20 @@ static void step(Oracle& o, double* dtp) {
   if (o.constant_CFL) update_timestep(o, dtp);
   const double dt = *dtp;
   const int K = (o.dim == 3) ? o.n[2] : 1;
-  const double rhof = 0.5 * (o.density + o.density);
   const double idx = 1.0 / o.d[0], idy = 1.0 / o.d[1], idz = 1.0 / o.d[2];
+  // Dodd-Ferrante approximate pressure (:87-95), whole array then ghosts
+  std::vector<double> p_hat;
+  if (o.split) {
+    p_hat.resize(o.p.f.size());
+    for (size_t t = 0; t < p_hat.size(); ++t) {
+      if (o.constant_CFL) p_hat[t] = o.p_o.f[t] + (dt + o.dt_o) * (o.p.f[t] - o.p_o.f[t]) / o.dt_o;
+      else p_hat[t] = 2.0 * o.p.f[t] - o.p_o.f[t];
+    }
+    Field ph = o.p;
+    ph.f = p_hat;
+    update_ghost_nodes(o, ph);
+    p_hat = ph.f;
+  }
   // predicted_velocity_field (:140-213)
   const double A = 1.0 + 0.5 * dt / o.dt_o;
   const double B = -0.5 * dt / o.dt_o;
@@ -796,14 +853,19 @@ static void step(Oracle& o, double* dtp) {
       for (int i = 1; i <= o.n[0]; ++i) {
         const size_t c = o.I(i, j, k);
         for (int q = 0; q < o.dim; ++q) {
+          const double rhof = rhof_at(o, c, q);
           const double gp = (P[c + so[q]] - P[c]) * (o.iso ? idx : id[q]);  // gradient (fields.f90:55-58)
-          const double rhs = -gp / rhof + A * o.dv[q][c] + B * o.dvo[q][c] + o.g[q];
+          double rhs = -gp / rhof + A * o.dv[q][c] + B * o.dvo[q][c] + o.g[q];
+          if (o.split) {
+            const double gph = (p_hat[c + so[q]] - p_hat[c]) * (o.iso ? idx : id[q]);
+            rhs = rhs + gp / rhof - o.irhomin * gp - (1.0 / rhof - o.irhomin) * gph;
+          }
           Vc[q]->f[c] = Vc[q]->f[c] + dt * rhs;
         }
       }
   for (int q = 0; q < o.dim; ++q) o.dvo[q] = o.dv[q];
   for (int q = 0; q < o.dim; ++q) update_ghost_nodes(o, *Vc[q]);
-  // phi = div(v) * rho / dt (:111-122)
+  // phi = div(v) * rho / dt (:111-122); rhomin/dt with the split
   double* phi = o.phi.f.data();
   OMP_FOR
   for (int k = 1; k <= K; ++k)
@@ -811,7 +873,7 @@ static void step(Oracle& o, double* dtp) {
       for (int i = 1; i <= o.n[0]; ++i) {
         const size_t c = o.I(i, j, k);
         phi[c] = div_at(o, c);
-        phi[c] = phi[c] * o.density / dt;
+        phi[c] = o.split ? phi[c] * o.rhomin / dt : phi[c] * o.rho.f[c] / dt;
       }
   solve_poisson(o, o.phi);
   update_ghost_nodes(o, o.phi);
@@ -823,11 +885,13 @@ static void step(Oracle& o, double* dtp) {
         const size_t c = o.I(i, j, k);
         for (int q = 0; q < o.dim; ++q) {
           const double gphi = (phi[c + so[q]] - phi[c]) * (o.iso ? idx : id[q]);
-          Vc[q]->f[c] = Vc[q]->f[c] - gphi * dt / rhof;
+          if (o.split) Vc[q]->f[c] = Vc[q]->f[c] - gphi * dt * o.irhomin;
+          else Vc[q]->f[c] = Vc[q]->f[c] - gphi * dt / rhof_at(o, c, q);
         }
       }
   for (int q = 0; q < o.dim; ++q) update_ghost_nodes(o, *Vc[q]);
-  // update_pressure (:550-566): whole array, then ghosts
+  // update_pressure (:550-566): p_o = p with the split; whole array, then ghosts
+  if (o.split) o.p_o.f = o.p.f;
   for (size_t t = 0; t < o.p.f.size(); ++t) o.p.f[t] = o.p.f[t] + o.phi.f[t];
   update_ghost_nodes(o, o.p);
   // checks (:570-619)
@@ -887,6 +951,11 @@ void* or_create(const or_params* P) {
   alloc_field(*o, o->w, 'z', 3);
   alloc_field(*o, o->p, 'c', 0);
   alloc_field(*o, o->phi, 'c', 0);
+  alloc_field(*o, o->rho, 'c', 0);  // rho, mu, p_o take p's boundary types (navier_stokes.f90:780-1016)
+  alloc_field(*o, o->mu, 'c', 0);
+  alloc_field(*o, o->p_o, 'c', 0);
+  std::fill(o->rho.f.begin(), o->rho.f.end(), P->density);   // rho%f = density
+  std::fill(o->mu.f.begin(), o->mu.f.end(), P->viscosity);   // mu%f = viscosity
   for (int q = 0; q < 3; ++q) {
     o->dv[q].assign(o->total(), 0.0);
     o->dvo[q].assign(o->total(), 0.0);
@@ -909,12 +978,27 @@ double* or_field(void* h, int id) {
     case 5: case 6: case 7: return o->dvo[id - 5].data();
     case 8: case 9: case 10: return o->S[id - 8].data();
     case 11: case 12: case 13: return o->dv[id - 11].data();
+    case 14: return o->rho.f.data();
+    case 15: return o->mu.f.data();
+    case 16: return o->p_o.f.data();
   }
   return nullptr;
 }
 
+// constant_viscosity = .not. var_mu; split: the MF pressure split with rhomin (solver.f90:91-92)
+void or_set_properties(void* h, int var_mu, int split, double rhomin) {
+  Oracle* o = (Oracle*)h;
+  o->var_mu = var_mu;
+  o->split = split;
+  o->rhomin = rhomin;
+  o->irhomin = 1.0 / rhomin;
+}
+
 static Field* fld(Oracle* o, int id) {
-  switch (id) { case 0: return &o->u; case 1: return &o->v; case 2: return &o->w; case 3: return &o->p; case 4: return &o->phi; }
+  switch (id) {
+    case 0: return &o->u; case 1: return &o->v; case 2: return &o->w; case 3: return &o->p; case 4: return &o->phi;
+    case 14: return &o->rho; case 15: return &o->mu; case 16: return &o->p_o;
+  }
   return nullptr;
 }
 

@@ -24,6 +24,7 @@ PERIODIC, WALL, INFLOW, OUTFLOW = 0, 1, 2, 3
 U, V, W, P, PHI = 0, 1, 2, 3, 4
 DVO = (5, 6, 7)
 S = (8, 9, 10)
+RHO, MU, P_O = 14, 15, 16  # cell-centred density, viscosity, old pressure (split)
 DV = (11, 12, 13)
 SOLVERS = ["pp", "pn", "nn", "ppp", "ppn", "npn", "nnn", "pnp"]
 
@@ -73,6 +74,7 @@ def lib():
         L.or_set_timestep.restype = ctypes.c_double
         L.or_set_timestep.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.or_set_dt_o.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.or_set_properties.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double]
         L.or_get_dt_o.restype = ctypes.c_double
         L.or_get_dt_o.argtypes = [ctypes.c_void_p]
         L.or_step.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
@@ -156,6 +158,11 @@ class Oracle:
 
     def add_advection(self):
         lib().or_add_advection(self._h)
+
+    def set_properties(self, var_mu=False, split=False, rhomin=1.0):
+        """constant_viscosity = not var_mu; split: the Dodd-Ferrante pressure split with rhomin.
+        Density and viscosity fields are the writable views field(RHO), field(MU)."""
+        lib().or_set_properties(self._h, int(var_mu), int(split), float(rhomin))
 
     def set_timestep(self, U):
         return lib().or_set_timestep(self._h, U)
