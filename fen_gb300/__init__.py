@@ -73,7 +73,7 @@ _EXPORTS = [
     "fen_ensemble_status", "fen_ensemble_config", "fen_ensemble_set_config", "fen_ensemble_tune",
     "fen_ensemble_launches", "fen_ensemble_smem_bytes", "fen_ensemble_adjoint_setup", "fen_ensemble_adjoint_forward",
     "fen_ensemble_adjoint_seed", "fen_ensemble_adjoint_backward", "fen_ensemble_adjoint_gradient",
-    "fen_ensemble_adjoint_dts", "fen_set_split_pressure",
+    "fen_ensemble_adjoint_dts", "fen_set_split_pressure", "fen_set_ibm_forcing", "fen_get_ibm_force",
 ]
 
 
@@ -113,6 +113,9 @@ def load_library(path=None):
     L.fen_save_fields.argtypes = [vp, ctypes.c_char_p, ip]
     L.fen_adjoint_setup.argtypes = [vp, ip, ip]
     L.fen_set_split_pressure.argtypes = [vp, ctypes.c_double]
+    cip_ = ctypes.POINTER(ctypes.c_int)
+    L.fen_set_ibm_forcing.argtypes = [vp, ip, ip, cip_, cip_, cip_, dp, dp]
+    L.fen_get_ibm_force.argtypes = [vp, ip, dp]
     L.fen_adjoint_forward.argtypes = [vp, ctypes.c_double]
     L.fen_adjoint_backward.argtypes = [vp, dp, dp, dp, dp, dp]
     cip = ctypes.POINTER(ctypes.c_int)
@@ -321,6 +324,30 @@ class Solver:
         """Dodd-Ferrante split pressure of FEN's multiphase step with minimum density rhomin
         (p_o = FEN field P_O); density and viscosity fields are RHO and MU (set_field)."""
         self._check(self._L.fen_set_split_pressure(self._h, float(rhomin)))
+
+    def set_ibm_forcing(self, comp, ijk, nnbr, nbr_ijk=None, w=None, c0=None):
+        """apply_ibm_forcing hook (navier_stokes.f90:106-108): forced points of one velocity
+        component (Fortran (i, j, k) per row of ijk), each taking c0 + sum w_q v*(nbr_q) with
+        up to 8 neighbours (nbr_ijk shape (n, 8, 3), w shape (n, 8)); nnbr = 0 with c0 the
+        solid velocity forces a solid point."""
+        ijk = np.ascontiguousarray(ijk, dtype=np.int32).reshape(-1, 3)
+        n = ijk.shape[0]
+        nn = np.ascontiguousarray(nnbr, dtype=np.int32).reshape(n)
+        nb = np.ascontiguousarray(nbr_ijk if nbr_ijk is not None else np.zeros((n, 8, 3)), dtype=np.int32).reshape(n, 8, 3)
+        ww = np.ascontiguousarray(w if w is not None else np.zeros((n, 8)), dtype=np.float64).reshape(n, 8)
+        cc = np.ascontiguousarray(c0 if c0 is not None else np.zeros(n), dtype=np.float64).reshape(n)
+        cip = ctypes.POINTER(ctypes.c_int)
+        self._check(self._L.fen_set_ibm_forcing(self._h, int(comp), n, ijk.ctypes.data_as(cip), nn.ctypes.data_as(cip),
+                                                nb.ctypes.data_as(cip), _dp(ww), _dp(cc)))
+        self._ibm_n = getattr(self, "_ibm_n", {})
+        self._ibm_n[comp] = n
+
+    def ibm_force(self, comp):
+        """Fe = (vs - v*)/dt of the forced points of the last step."""
+        out = np.zeros(getattr(self, "_ibm_n", {}).get(comp, 0))
+        if out.size:
+            self._check(self._L.fen_get_ibm_force(self._h, int(comp), _dp(out)))
+        return out
 
     # -- discrete adjoint (2D periodic FP64) ------------------------------------------------
     def adjoint_setup(self, nsteps, every):

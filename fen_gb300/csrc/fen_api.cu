@@ -117,6 +117,13 @@ struct fen_ctx {
   double *rho = nullptr, *mu = nullptr, *p_o = nullptr;
   int var_rho = 0, var_mu = 0, split = 0;
   double rhomin = 1.0;
+  // IBM forcing lists per velocity component (device arrays)
+  struct Ibm {
+    long long *idx = nullptr, *nidx = nullptr;
+    int* nn = nullptr;
+    double *w = nullptr, *c0 = nullptr, *vs = nullptr, *fe = nullptr;
+    int n = 0;
+  } ibm[3];
   float* S32[3] = {nullptr, nullptr, nullptr};
   int has_S = 0;
   // poisson
@@ -889,6 +896,20 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
     double* f[3] = {c->us, c->vs, c->ws};
     int ids[3] = {FEN_U, FEN_V, FEN_W};
     if ((r = ghost<double>(c, c->dim, f, ids))) return r;
+    if (c->ibm[0].n + c->ibm[1].n + c->ibm[2].n > 0) {
+      // apply_ibm_forcing (navier_stokes.f90:106-108), then the boundary conditions again
+      for (int q = 0; q < c->dim; ++q) {
+        auto& I = c->ibm[q];
+        if (!I.n) continue;
+        IbmArgs ia{I.idx, I.nn, I.nidx, I.w, I.c0, I.vs, I.fe, f[q], I.n};
+        const int g = std::min(cdiv(I.n, 256), 152 * 8);
+        k_ibm_target<<<g, 256, 0, c->stream>>>(ia);
+        k_ibm_apply<<<g, 256, 0, c->stream>>>(ia, c->sc);
+        c->launches += 2;
+      }
+      CK(cudaGetLastError());
+      if ((r = ghost<double>(c, c->dim, f, ids))) return r;
+    }
   }
   mark();  // 2: ghost v* (or its increment)
   {
@@ -1103,6 +1124,10 @@ int fen_ctx_destroy(fen_ctx* c) {
   for (float* b : fb) if (b) cudaFree(b);
   if (c->tmp64) cudaFree(c->tmp64);
   for (double* b : {c->rho, c->mu, c->p_o}) if (b) cudaFree(b);
+  for (auto& I : c->ibm) {
+    void* bs[] = {I.idx, I.nidx, I.nn, I.w, I.c0, I.vs, I.fe};
+    for (void* b : bs) if (b) cudaFree(b);
+  }
   for (int f = 0; f < 5; ++f) for (int q = 0; q < 6; ++q) if (c->bcval[f][q]) cudaFree(c->bcval[f][q]);
   if (c->specC) cudaFree(c->specC);
   if (c->specR) cudaFree(c->specR);
@@ -1799,6 +1824,62 @@ int fen_adjoint_backward(fen_ctx* c, const double* lam_u, const double* lam_v, d
   if (ms) {
     ms[0] = A.bwd_ms;
     ms[1] = A.fwd_ms;
+  }
+  return 0;
+}
+
+int fen_set_ibm_forcing(fen_ctx* c, int comp, int npoints, const int* ijk, const int* nnbr, const int* nbr_ijk,
+                        const double* w, const double* c0) {
+  if (!c || comp < 0 || comp >= c->dim || npoints < 0) return fail(FEN_ERR_ARG, "bad argument");
+  if (c->mixed) return fail(FEN_ERR_ARG, "the IBM forcing hook runs in FP64 contexts only");
+  if (npoints > 0 && (!ijk || !nnbr || !c0)) return fail(FEN_ERR_ARG, "null argument");
+  auto& I = c->ibm[comp];
+  void* bs[] = {I.idx, I.nidx, I.nn, I.w, I.c0, I.vs, I.fe};
+  for (void* b : bs) if (b) cudaFree(b);
+  I = fen_ctx::Ibm();
+  drop_graph(c);
+  if (npoints == 0) return 0;
+  const int K = (c->dim == 3) ? c->n[2] : 1;
+  auto lin = [&](const int* q, long long* out) -> bool {
+    const int i = q[0], j = q[1], k = (c->dim == 3) ? q[2] : 1;
+    if (i < 0 || i > c->n[0] + 1 || j < 0 || j > c->n[1] + 1 || k < 0 || k > K + 1) return false;
+    *out = c->L.idx(i, j, c->dim == 3 ? k : 0);
+    return true;
+  };
+  std::vector<long long> idx(npoints), nidx((size_t)8 * npoints, 0);
+  std::vector<int> nn(npoints);
+  std::vector<double> ww((size_t)8 * npoints, 0.0), cc(c0, c0 + npoints);
+  for (int p = 0; p < npoints; ++p) {
+    if (!lin(ijk + 3 * p, &idx[p])) return fail(FEN_ERR_ARG, "forced point outside the grid");
+    const int i = ijk[3 * p], j = ijk[3 * p + 1], k = (c->dim == 3) ? ijk[3 * p + 2] : 1;
+    if (i < 1 || i > c->n[0] || j < 1 || j > c->n[1] || k < 1 || k > K) return fail(FEN_ERR_ARG, "forced point is not interior");
+    nn[p] = nnbr[p];
+    if (nn[p] < 0 || nn[p] > 8 || (nn[p] > 0 && (!nbr_ijk || !w))) return fail(FEN_ERR_ARG, "stencil size must be 0..8");
+    for (int q = 0; q < nn[p]; ++q) {
+      if (!lin(nbr_ijk + 3 * (8 * p + q), &nidx[(size_t)8 * p + q])) return fail(FEN_ERR_ARG, "stencil point outside the grid");
+      ww[(size_t)8 * p + q] = w[(size_t)8 * p + q];
+    }
+  }
+  int r;
+  if ((r = alloc(&I.idx, npoints)) || (r = alloc(&I.nidx, 8LL * npoints)) || (r = alloc(&I.nn, npoints)) ||
+      (r = alloc(&I.w, 8LL * npoints)) || (r = alloc(&I.c0, npoints)) || (r = alloc(&I.vs, npoints)) ||
+      (r = alloc(&I.fe, npoints)))
+    return r;
+  CK(cudaMemcpy(I.idx, idx.data(), idx.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(I.nidx, nidx.data(), nidx.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(I.nn, nn.data(), nn.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(I.w, ww.data(), ww.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(I.c0, cc.data(), cc.size() * sizeof(double), cudaMemcpyHostToDevice));
+  I.n = npoints;
+  return 0;
+}
+
+int fen_get_ibm_force(fen_ctx* c, int comp, double* fe) {
+  if (!c || comp < 0 || comp >= c->dim || !fe) return fail(FEN_ERR_ARG, "bad argument");
+  const auto& I = c->ibm[comp];
+  if (I.n) {
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(fe, I.fe, I.n * sizeof(double), cudaMemcpyDeviceToHost));
   }
   return 0;
 }

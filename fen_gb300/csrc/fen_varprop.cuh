@@ -189,3 +189,43 @@ __global__ void __launch_bounds__(256) k_correct_var(Layout L, const StepScalars
 }
 
 }  // namespace fen
+
+namespace fen {
+
+// IBM forcing hook (apply_ibm_forcing, navier_stokes.f90:106-108; eulerian_ibm.f90:194-268):
+// after the predictor, each forced velocity point takes the target
+//   vs = c0 + sum_k w_k v*(nbr_k)   (k < nn <= 8)
+// (solid points: nn = 0 and c0 the solid velocity; interface points: the interpolation of
+// the solid-boundary velocity and nearby fluid values), and the forcing Fe = (vs - v*)/dt
+// is recorded.  All targets are evaluated from the unforced v* before any point is written.
+struct IbmArgs {
+  const long long* idx;   // forced point (layout index)
+  const int* nn;          // stencil size
+  const long long* nidx;  // [8 * point] neighbour layout indices
+  const double* w;        // [8 * point] weights
+  const double* c0;       // constant term
+  double* vs;             // targets
+  double* fe;             // forcing (vs - v*)/dt
+  double* v;              // the velocity component v*
+  int n;
+};
+
+__global__ void __launch_bounds__(256) k_ibm_target(IbmArgs a) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+    double s = a.c0[p];
+    const int m = a.nn[p];
+    for (int k = 0; k < m; ++k) s = s + a.w[8 * p + k] * a.v[a.nidx[8 * p + k]];
+    a.vs[p] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_ibm_apply(IbmArgs a, const StepScalars* __restrict__ sc) {
+  const double dt = sc->dt;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += gridDim.x * blockDim.x) {
+    const long long c = a.idx[p];
+    a.fe[p] = (a.vs[p] - a.v[c]) / dt;
+    a.v[c] = a.vs[p];
+  }
+}
+
+}  // namespace fen

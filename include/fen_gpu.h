@@ -145,6 +145,18 @@ int fen_adjoint_backward(fen_ctx* ctx, const double* lam_u, const double* lam_v,
  * 557) with the minimum density rhomin; the old pressure is FEN_P_O (zero until uploaded). */
 int fen_set_split_pressure(fen_ctx* ctx, double rhomin);
 
+/* IBM forcing hook (apply_ibm_forcing, navier_stokes.f90:106-108; eulerian_ibm.f90:194-268),
+ * FP64 contexts.  After the predictor, every listed point of velocity component comp
+ * (0 x, 1 y, 2 z; Fortran indices ijk[3p..3p+2], interior) takes the target
+ *   vs = c0[p] + sum_{q < nnbr[p]} w[8p+q] * v*(nbr_ijk[3(8p+q)..])    (nnbr <= 8)
+ * computed from the unforced v*: solid points carry nnbr = 0 and the solid velocity in c0,
+ * interface points the interpolation the caller's solid geometry defines.  The velocity
+ * ghosts are refilled afterwards.  npoints = 0 removes the component's list.
+ * fen_get_ibm_force returns FEN's forcing Fe = (vs - v*)/dt of the last step (npoints values). */
+int fen_set_ibm_forcing(fen_ctx* ctx, int comp, int npoints, const int* ijk, const int* nnbr, const int* nbr_ijk,
+                        const double* w, const double* c0);
+int fen_get_ibm_force(fen_ctx* ctx, int comp, double* fe);
+
 /* Synchronise the context stream. */
 int fen_sync(fen_ctx* ctx);
 /* Number of kernels this library launched on the context since creation. */

@@ -180,6 +180,13 @@ struct Oracle {
   // pressure p_o of the Dodd-Ferrante split (multiphase.f90:25, navier_stokes.f90:80-96)
   Field rho, mu, p_o;
   int var_mu = 0;          // constant_viscosity = .false. (navier_stokes.f90:45, 405-452)
+  // IBM forcing lists per component (apply_ibm_forcing, navier_stokes.f90:106-108):
+  // target vs = c0 + sum_q w_q v*(nbr_q), evaluated from the unforced v*, and Fe = (vs - v*)/dt
+  struct Ibm {
+    std::vector<size_t> idx, nidx;
+    std::vector<int> nn;
+    std::vector<double> w, c0, fe;
+  } ibm[3];
   int split = 0;           // Dodd-Ferrante split pressure with rhomin (the MF branches)
   double rhomin = 1.0, irhomin = 1.0;
   // poisson_mod state (poisson.f90:31-49)
@@ -865,6 +872,27 @@ static void step(Oracle& o, double* dtp) {
       }
   for (int q = 0; q < o.dim; ++q) o.dvo[q] = o.dv[q];
   for (int q = 0; q < o.dim; ++q) update_ghost_nodes(o, *Vc[q]);
+  // apply_ibm_forcing (:106-108): targets from the unforced v*, then the forcing, then bcs
+  bool forced = false;
+  for (int q = 0; q < o.dim; ++q) {
+    Oracle::Ibm& I = o.ibm[q];
+    const size_t np = I.idx.size();
+    if (!np) continue;
+    forced = true;
+    std::vector<double> vs(np);
+    for (size_t p = 0; p < np; ++p) {
+      double s = I.c0[p];
+      for (int k = 0; k < I.nn[p]; ++k) s = s + I.w[8 * p + k] * Vc[q]->f[I.nidx[8 * p + k]];
+      vs[p] = s;
+    }
+    I.fe.assign(np, 0.0);
+    for (size_t p = 0; p < np; ++p) {
+      I.fe[p] = (vs[p] - Vc[q]->f[I.idx[p]]) / dt;
+      Vc[q]->f[I.idx[p]] = vs[p];
+    }
+  }
+  if (forced)
+    for (int q = 0; q < o.dim; ++q) update_ghost_nodes(o, *Vc[q]);
   // phi = div(v) * rho / dt (:111-122); rhomin/dt with the split
   double* phi = o.phi.f.data();
   OMP_FOR
@@ -983,6 +1011,34 @@ double* or_field(void* h, int id) {
     case 16: return o->p_o.f.data();
   }
   return nullptr;
+}
+
+void or_set_ibm(void* h, int comp, int np, const int* ijk, const int* nnbr, const int* nbr_ijk, const double* w,
+                const double* c0) {
+  Oracle* o = (Oracle*)h;
+  Oracle::Ibm& I = o->ibm[comp];
+  I = Oracle::Ibm();
+  for (int p = 0; p < np; ++p) {
+    const int k = (o->dim == 3) ? ijk[3 * p + 2] : 1;
+    I.idx.push_back(o->I(ijk[3 * p], ijk[3 * p + 1], k));
+    I.nn.push_back(nnbr[p]);
+    I.c0.push_back(c0[p]);
+    for (int q = 0; q < 8; ++q) {
+      if (q < nnbr[p]) {
+        const int* n3 = nbr_ijk + 3 * (8 * p + q);
+        I.nidx.push_back(o->I(n3[0], n3[1], (o->dim == 3) ? n3[2] : 1));
+        I.w.push_back(w[8 * p + q]);
+      } else {
+        I.nidx.push_back(0);
+        I.w.push_back(0.0);
+      }
+    }
+  }
+}
+
+const double* or_ibm_force(void* h, int comp) {
+  Oracle* o = (Oracle*)h;
+  return o->ibm[comp].fe.empty() ? nullptr : o->ibm[comp].fe.data();
 }
 
 // constant_viscosity = .not. var_mu; split: the MF pressure split with rhomin (solver.f90:91-92)

@@ -57,6 +57,7 @@ def lib():
     if _lib is None:
         _lib = ctypes.CDLL(build())
         L = _lib
+        dp_ = ctypes.POINTER(ctypes.c_double)
         L.or_create.restype = ctypes.c_void_p
         L.or_create.argtypes = [ctypes.POINTER(_Params)]
         L.or_destroy.argtypes = [ctypes.c_void_p]
@@ -75,6 +76,10 @@ def lib():
         L.or_set_timestep.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.or_set_dt_o.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.or_set_properties.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        ip_ = ctypes.POINTER(ctypes.c_int)
+        L.or_set_ibm.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ip_, ip_, ip_, dp_, dp_]
+        L.or_ibm_force.restype = dp_
+        L.or_ibm_force.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.or_get_dt_o.restype = ctypes.c_double
         L.or_get_dt_o.argtypes = [ctypes.c_void_p]
         L.or_step.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
@@ -163,6 +168,20 @@ class Oracle:
         """constant_viscosity = not var_mu; split: the Dodd-Ferrante pressure split with rhomin.
         Density and viscosity fields are the writable views field(RHO), field(MU)."""
         lib().or_set_properties(self._h, int(var_mu), int(split), float(rhomin))
+
+    def set_ibm(self, comp, ijk, nnbr, nbr_ijk, w, c0):
+        """IBM forcing list of one velocity component (see include/fen_gpu.h fen_set_ibm_forcing)."""
+        a = [np.ascontiguousarray(x, dtype=np.int32) for x in (ijk, nnbr, nbr_ijk)]
+        b = [np.ascontiguousarray(x, dtype=np.float64) for x in (w, c0)]
+        self._ibm_keep = getattr(self, "_ibm_keep", {})
+        self._ibm_keep[comp] = (a, b)
+        ip_ = ctypes.POINTER(ctypes.c_int)
+        lib().or_set_ibm(self._h, int(comp), len(b[1]), a[0].ctypes.data_as(ip_), a[1].ctypes.data_as(ip_),
+                         a[2].ctypes.data_as(ip_), _dp(b[0]), _dp(b[1]))
+
+    def ibm_force(self, comp, npoints):
+        ptr = lib().or_ibm_force(self._h, int(comp))
+        return np.ctypeslib.as_array(ptr, shape=(npoints,)).copy() if ptr else np.zeros(npoints)
 
     def set_timestep(self, U):
         return lib().or_set_timestep(self._h, U)
