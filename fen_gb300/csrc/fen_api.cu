@@ -786,8 +786,12 @@ int launch_predictor(fen_ctx* c, const StepScalars* sc) {
     else k_predictor_var<2><<<grid, 256, 0, c->stream>>>(c->L, sc, va);
   } else {
     PredArgs<double> pa = pred_args<double>(c);
-    if (c->dim == 3) k_predictor<3><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
-    else k_predictor<2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+    if (c->dim == 3) {
+      const dim3 tg(cdiv(c->n[0], kTX), cdiv(c->n[1], kTY), cdiv(c->n[2], kTZ));
+      k_predictor_tile<<<tg, dim3(kTX, kTY), 0, c->stream>>>(c->L, sc, pa);
+    } else {
+      k_predictor<2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+    }
   }
   c->launches++;
   CK(cudaGetLastError());

@@ -141,6 +141,137 @@ __global__ void __launch_bounds__(256) k_predictor(Layout L, const StepScalars* 
   }
 }
 
+// 3D FP64 predictor with flux sharing between cells.  The six products a cell owns on its
+// + faces/edges (1/4 folded into the scale q),
+//   Fuu = (u(i+1) + u)^2, Fvv = (v(j+1) + v)^2, Fww = (w(k+1) + w)^2,
+//   Euv = (u(j+1) + u)(v(i+1) + v), Euw = (u(k+1) + u)(w(i+1) + w), Evw = (v(k+1) + v)(w(j+1) + w),
+// are formed once: the - face values come from the x neighbour lane (warp shuffle), the
+// y neighbour row (shared memory) and the previous k of the z walk (registers); halo lanes,
+// rows and the first k compute theirs directly (FP64 issue counts active lanes only).  The
+// discrete operator is FEN's (navier_stokes.f90:297-353); diffusion and AB2 as k_predictor.
+constexpr int kTX = 32, kTY = 8, kTZ = 16;
+
+__device__ __forceinline__ void flux6(const double* __restrict__ U, const double* __restrict__ V,
+                                      const double* __restrict__ W, long long c, long long sy, long long sz, double& fuu,
+                                      double& fvv, double& fww, double& euv, double& euw, double& evw) {
+  const double uc = U[c], vc = V[c], wc = W[c];
+  const double su = U[c + 1] + uc, sv = V[c + sy] + vc, sw = W[c + sz] + wc;
+  fuu = su * su;
+  fvv = sv * sv;
+  fww = sw * sw;
+  euv = (U[c + sy] + uc) * (V[c + 1] + vc);
+  euw = (U[c + sz] + uc) * (W[c + 1] + wc);
+  evw = (V[c + sz] + vc) * (W[c + sy] + wc);
+}
+
+static __global__ void __launch_bounds__(kTX * kTY) k_predictor_tile(Layout L, const StepScalars* __restrict__ sc,
+                                                              PredArgs<double> a) {
+  __shared__ double sh[2][3][kTY][kTX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = 1 + blockIdx.x * kTX + tx, j0 = 1 + blockIdx.y * kTY + ty;
+  const bool act = (i0 <= L.n0) && (j0 <= L.n1);
+  const int i = min(i0, L.n0), j = min(j0, L.n1);
+  const int k0 = 1 + blockIdx.z * kTZ, k1 = min(L.n2, k0 + kTZ - 1);
+  const double A = sc->A, B = sc->B;
+  const double dt = a.use_dev_dt ? sc->dt : a.dt_host;
+  const double idx = a.id[0], idy = a.iso ? a.id[0] : a.id[1], idz = a.iso ? a.id[0] : a.id[2];
+  const double qx = 0.25 * idx, qy = 0.25 * idy, qz = 0.25 * idz;
+  const double irho = a.rhof_one ? 1.0 : 1.0 / a.rhof;
+  const double mx = a.rhof_one ? a.mu * a.id2[0] : a.mu * a.id2[0] / a.rhof;
+  const double my = a.iso ? mx : (a.rhof_one ? a.mu * a.id2[1] : a.mu * a.id2[1] / a.rhof);
+  const double mz = a.iso ? mx : (a.rhof_one ? a.mu * a.id2[2] : a.mu * a.id2[2] / a.rhof);
+  const double gx = idx * irho, gy = idy * irho, gz = idz * irho;
+  const long long sy = L.sx, sz = L.sp;
+  const double* __restrict__ U = a.u;
+  const double* __restrict__ V = a.v;
+  const double* __restrict__ W = a.w;
+  const double* __restrict__ P = a.p;
+  // z-minus fluxes of the first k of the chunk
+  double pww, puw, pvw;
+  {
+    const long long c = L.idx(i, j, k0) - sz;
+    double f0, f1, f2, f3, f4, f5;
+    flux6(U, V, W, c, sy, sz, f0, f1, f2, f3, f4, f5);
+    pww = f2;
+    puw = f4;
+    pvw = f5;
+  }
+  int buf = 0;
+  for (int k = k0; k <= k1; ++k, buf ^= 1) {
+    const long long c = L.idx(i, j, k);
+    double fuu, fvv, fww, euv, euw, evw;
+    flux6(U, V, W, c, sy, sz, fuu, fvv, fww, euv, euw, evw);
+    // x-minus: the lane to the left; lane 0 computes its own
+    double xuu = __shfl_up_sync(0xffffffffu, fuu, 1);
+    double xuv = __shfl_up_sync(0xffffffffu, euv, 1);
+    double xuw = __shfl_up_sync(0xffffffffu, euw, 1);
+    if (tx == 0) {
+      double f0, f1, f2, f3, f4, f5;
+      flux6(U, V, W, c - 1, sy, sz, f0, f1, f2, f3, f4, f5);
+      xuu = f0;
+      xuv = f3;
+      xuw = f4;
+    }
+    // y-minus: the row below through shared memory; row 0 computes its own
+    sh[buf][0][ty][tx] = euv;
+    sh[buf][1][ty][tx] = fvv;
+    sh[buf][2][ty][tx] = evw;
+    __syncthreads();
+    double yuv, yvv, yvw;
+    if (ty > 0) {
+      yuv = sh[buf][0][ty - 1][tx];
+      yvv = sh[buf][1][ty - 1][tx];
+      yvw = sh[buf][2][ty - 1][tx];
+    } else {
+      double f0, f1, f2, f3, f4, f5;
+      flux6(U, V, W, c - sy, sy, sz, f0, f1, f2, f3, f4, f5);
+      yuv = f3;
+      yvv = f1;
+      yvw = f5;
+    }
+    const double ax = fma(euw - puw, qz, fma(euv - yuv, qy, (fuu - xuu) * qx));
+    const double ay = fma(evw - pvw, qz, fma(fvv - yvv, qy, (euv - xuv) * qx));
+    const double az = fma(fww - pww, qz, fma(evw - yvw, qy, (euw - xuw) * qx));
+    pww = fww;
+    puw = euw;
+    pvw = evw;
+    if (act) {
+      const double uc = U[c], vc = V[c], wc = W[c];
+      const double uip = U[c + 1], uim = U[c - 1], ujp = U[c + sy], ujm = U[c - sy], ukp = U[c + sz], ukm = U[c - sz];
+      const double vip = V[c + 1], vim = V[c - 1], vjp = V[c + sy], vjm = V[c - sy], vkp = V[c + sz], vkm = V[c - sz];
+      const double wip = W[c + 1], wim = W[c - 1], wjp = W[c + sy], wjm = W[c - sy], wkp = W[c + sz], wkm = W[c - sz];
+      double dvx, dvy, dvz;
+      if (a.iso) {
+        dvx = fma(mx, fma(-6.0, uc, ((uip + uim) + (ujp + ujm)) + (ukp + ukm)), -ax);
+        dvy = fma(mx, fma(-6.0, vc, ((vip + vim) + (vjp + vjm)) + (vkp + vkm)), -ay);
+        dvz = fma(mx, fma(-6.0, wc, ((wip + wim) + (wjp + wjm)) + (wkp + wkm)), -az);
+      } else {
+        dvx = fma(mz, fma(-2.0, uc, ukp + ukm), fma(my, fma(-2.0, uc, ujp + ujm), fma(mx, fma(-2.0, uc, uip + uim), -ax)));
+        dvy = fma(mz, fma(-2.0, vc, vkp + vkm), fma(my, fma(-2.0, vc, vjp + vjm), fma(mx, fma(-2.0, vc, vip + vim), -ay)));
+        dvz = fma(mz, fma(-2.0, wc, wkp + wkm), fma(my, fma(-2.0, wc, wjp + wjm), fma(mx, fma(-2.0, wc, wip + wim), -az)));
+      }
+      if (a.has_S) {
+        dvx = fma(a.Sx[c], irho, dvx);
+        dvy = fma(a.Sy[c], irho, dvy);
+        dvz = fma(a.Sz[c], irho, dvz);
+      }
+      const double pc = P[c];
+      double rx = fma(-gx, P[c + 1] - pc, a.g[0]);
+      double ry = fma(-gy, P[c + sy] - pc, a.g[1]);
+      double rz = fma(-gz, P[c + sz] - pc, a.g[2]);
+      rx = fma(A, dvx, fma(B, a.dox[c], rx));
+      ry = fma(A, dvy, fma(B, a.doy[c], ry));
+      rz = fma(A, dvz, fma(B, a.doz[c], rz));
+      a.us[c] = fma(dt, rx, uc);
+      a.vs[c] = fma(dt, ry, vc);
+      a.ws[c] = fma(dt, rz, wc);
+      a.dox[c] = dvx;
+      a.doy[c] = dvy;
+      a.doz[c] = dvz;
+    }
+  }
+}
+
 // ------------------------------------------------------------------------------------
 // Line transforms.  One kernel template covers every 1D stage of every solver:
 //   CONTIG = true : lines along x (contiguous), the first and last stages;
