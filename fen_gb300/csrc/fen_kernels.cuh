@@ -164,6 +164,32 @@ __device__ __forceinline__ void flux6(const double* __restrict__ U, const double
   evw = (V[c + sz] + vc) * (W[c + sy] + wc);
 }
 
+// The three + fluxes of cell c that the x, y or z neighbour needs as its - fluxes.
+__device__ __forceinline__ void flux_x(const double* __restrict__ U, const double* __restrict__ V,
+                                       const double* __restrict__ W, long long c, long long sy, long long sz, double& fuu,
+                                       double& euv, double& euw) {
+  const double uc = U[c], su = U[c + 1] + uc;
+  fuu = su * su;
+  euv = (U[c + sy] + uc) * (V[c + 1] + V[c]);
+  euw = (U[c + sz] + uc) * (W[c + 1] + W[c]);
+}
+__device__ __forceinline__ void flux_y(const double* __restrict__ U, const double* __restrict__ V,
+                                       const double* __restrict__ W, long long c, long long sy, long long sz, double& euv,
+                                       double& fvv, double& evw) {
+  const double vc = V[c], sv = V[c + sy] + vc;
+  fvv = sv * sv;
+  euv = (U[c + sy] + U[c]) * (V[c + 1] + vc);
+  evw = (V[c + sz] + vc) * (W[c + sy] + W[c]);
+}
+__device__ __forceinline__ void flux_z(const double* __restrict__ U, const double* __restrict__ V,
+                                       const double* __restrict__ W, long long c, long long sy, long long sz, double& euw,
+                                       double& evw, double& fww) {
+  const double wc = W[c], sw = W[c + sz] + wc;
+  fww = sw * sw;
+  euw = (U[c + sz] + U[c]) * (W[c + 1] + wc);
+  evw = (V[c + sz] + V[c]) * (W[c + sy] + wc);
+}
+
 static __global__ void __launch_bounds__(kTX * kTY) k_predictor_tile(Layout L, const StepScalars* __restrict__ sc,
                                                               PredArgs<double> a) {
   __shared__ double sh[2][3][kTY][kTX];
@@ -188,14 +214,7 @@ static __global__ void __launch_bounds__(kTX * kTY) k_predictor_tile(Layout L, c
   const double* __restrict__ P = a.p;
   // z-minus fluxes of the first k of the chunk
   double pww, puw, pvw;
-  {
-    const long long c = L.idx(i, j, k0) - sz;
-    double f0, f1, f2, f3, f4, f5;
-    flux6(U, V, W, c, sy, sz, f0, f1, f2, f3, f4, f5);
-    pww = f2;
-    puw = f4;
-    pvw = f5;
-  }
+  flux_z(U, V, W, L.idx(i, j, k0) - sz, sy, sz, puw, pvw, pww);
   int buf = 0;
   for (int k = k0; k <= k1; ++k, buf ^= 1) {
     const long long c = L.idx(i, j, k);
@@ -205,13 +224,7 @@ static __global__ void __launch_bounds__(kTX * kTY) k_predictor_tile(Layout L, c
     double xuu = __shfl_up_sync(0xffffffffu, fuu, 1);
     double xuv = __shfl_up_sync(0xffffffffu, euv, 1);
     double xuw = __shfl_up_sync(0xffffffffu, euw, 1);
-    if (tx == 0) {
-      double f0, f1, f2, f3, f4, f5;
-      flux6(U, V, W, c - 1, sy, sz, f0, f1, f2, f3, f4, f5);
-      xuu = f0;
-      xuv = f3;
-      xuw = f4;
-    }
+    if (tx == 0) flux_x(U, V, W, c - 1, sy, sz, xuu, xuv, xuw);
     // y-minus: the row below through shared memory; row 0 computes its own
     sh[buf][0][ty][tx] = euv;
     sh[buf][1][ty][tx] = fvv;
@@ -223,11 +236,7 @@ static __global__ void __launch_bounds__(kTX * kTY) k_predictor_tile(Layout L, c
       yvv = sh[buf][1][ty - 1][tx];
       yvw = sh[buf][2][ty - 1][tx];
     } else {
-      double f0, f1, f2, f3, f4, f5;
-      flux6(U, V, W, c - sy, sy, sz, f0, f1, f2, f3, f4, f5);
-      yuv = f3;
-      yvv = f1;
-      yvw = f5;
+      flux_y(U, V, W, c - sy, sy, sz, yuv, yvv, yvw);
     }
     const double ax = fma(euw - puw, qz, fma(euv - yuv, qy, (fuu - xuu) * qx));
     const double ay = fma(evw - pvw, qz, fma(fvv - yvv, qy, (euv - xuv) * qx));
