@@ -52,8 +52,21 @@ STAGE_BYTES_3D = {
     "correct": 8 * 9,         # read v*(3), phi; read+write p; write v(3)
 }
 
-# DRAM bytes per cell of one launch, measured with ncu (profiles/k_predictor_tgv3d_192_fp64.md)
-TRAFFIC_BYTES_PER_CELL = {"predictor": 110.0}
+# DRAM bytes per cell of one launch, measured with ncu (profiles/k_predictor_tile_tgv3d_192_fp64.md)
+TRAFFIC_BYTES_PER_CELL = {"predictor": 99.6}
+# FP64 thread instructions per cell of one launch (same capture: DADD + DMUL + DFMA)
+FP64_INSTR_PER_CELL = {"predictor": 72.0}
+
+
+def fp64_issue(kernel, cells, ms):
+    """Achieved FP64 instruction rate of `kernel` against the GB300 issue peak (2 FP64 thread
+    instructions per SM per cycle x 152 SMs x the maximum SM clock)."""
+    if kernel not in FP64_INSTR_PER_CELL or not ms:
+        return None
+    peak = 2 * 152 * 2.07e9 / 1e9
+    got = FP64_INSTR_PER_CELL[kernel] * cells / (ms / 1e3) / 1e9
+    return {"achieved": round(got, 1), "peak": round(peak, 1), "unit": "G FP64 instr/s", "frac": round(got / peak, 4),
+            "instr_per_cell": FP64_INSTR_PER_CELL[kernel]}
 
 CONFIGS = {
     "tgv3d": dict(dim=3, n=(256, 256, 256), L=(2 * np.pi,) * 3, nu=1.0 / 1600, cfl=0.5, constant_cfl=True,
@@ -494,8 +507,11 @@ def main():
     traffic = TRAFFIC_BYTES_PER_CELL.get(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": int(traffic * cells) if traffic and cfg["dim"] == 3 else None,
-                "traffic_source": "ncu dram__bytes_read+write of one predictor launch at 192^3, scaled by cells",
-                "fp64_pipe_pct": 87.2, "peak_source": peak_kind,
+                "traffic_source": "ncu dram__bytes_read+write of one predictor launch at 192^3 (99.6 B/cell), scaled by cells",
+                "fp64_pipe_pct": 85.7, "peak_source": peak_kind,
+                # FP64 issue bound: instructions per cell of the tiled predictor (ncu, 192^3)
+                # against 2 FP64 thread instructions per SM per cycle (ncu peak_sustained)
+                "fp64_issue": fp64_issue(dom, cells, stage.get(dom)) if cfg["dim"] == 3 else None,
                 "bytes_per_cell": bpc, "stage_ms": {k: round(v, 4) for k, v in stage.items()},
                 "note": "FP64 kernels are FP64-issue-bound on GB300 (1.19 TFLOP/s FP64 measured)"}
 
