@@ -609,12 +609,17 @@ int launch_stage_t(fen_ctx* c, const Stage& s, int first_from_field, const void*
 
 int launch_thomas(fen_ctx* c, const Stage& s) {
   const bool real = (c->solver == S_NN || c->solver == S_NNN);
+  ThomasArgs ta = s.ta;
+  ta.split2 = 0;
   if (real) {
-    if (c->mixed) k_thomas<float, double><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
-    else k_thomas<double, double><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
+    if (c->mixed) k_thomas<float, double><<<s.tgrid, 128, 0, c->stream>>>(ta);
+    else k_thomas<double, double><<<s.tgrid, 128, 0, c->stream>>>(ta);
   } else {
-    if (c->mixed) k_thomas<float2, double2><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
-    else k_thomas<double2, double2><<<s.tgrid, 128, 0, c->stream>>>(s.ta);
+    // complex right-hand sides: real and imaginary parts as two real systems per column
+    ta.split2 = 1;
+    const dim3 g(cdiv(2LL * ta.ncol, 128), s.tgrid.y, s.tgrid.z);
+    if (c->mixed) k_thomas<float, double><<<g, 128, 0, c->stream>>>(ta);
+    else k_thomas<double, double><<<g, 128, 0, c->stream>>>(ta);
   }
   c->launches++;
   CK(cudaGetLastError());

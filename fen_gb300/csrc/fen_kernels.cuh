@@ -566,6 +566,7 @@ struct ThomasArgs {
   const double* c1;           // [sys][row] forward coefficients
   const double* fac;          // [sys][row] reciprocal factor (FORM3) or divisor (2D form); last row: raw pivot
   int form3;
+  int split2;                 // complex data swept as two real systems: thread 2c + part, part 0 re / 1 im
 };
 
 // Elimination arithmetic: r - a d as one fused multiply-add, then the row factor.
@@ -621,41 +622,88 @@ template <> __device__ __forceinline__ double2 tback<double2, double2>(double2 v
 template <> __device__ __forceinline__ float tback<double, float>(double v) { return narrow(v); }
 template <> __device__ __forceinline__ float2 tback<double2, float2>(double2 v) { return make_float2(narrow(v.x), narrow(v.y)); }
 
+// One system per thread.  The rows are swept in batches of kTB: the batch's right-hand
+// sides and table values are loaded first (independent loads, their latencies overlap),
+// then the batch's dependent elimination steps run in registers.  The arithmetic and its
+// order are the plain Thomas recurrence.
+constexpr int kTB = 8;
+
 template <typename VS, typename VC>
 __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
   typedef ThomasOps<VC> O;
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tcol = blockIdx.x * blockDim.x + threadIdx.x;
+  const int col = a.split2 ? (tcol >> 1) : tcol;
   const int outer = blockIdx.y;
   if (col >= a.ncol) return;
-  VS* X = reinterpret_cast<VS*>(a.x) + (long long)col * a.s_col + (long long)outer * a.s_outer;
+  // split2: the real and imaginary parts of one complex system are two real systems with the
+  // same coefficients, swept by neighbouring threads (twice the threads, coalesced loads)
+  const int w = a.split2 ? 2 : 1;
+  VS* X = reinterpret_cast<VS*>(a.x) + ((long long)col * a.s_col + (long long)outer * a.s_outer) * w + (tcol & (w - 1));
   const long long sys = (long long)outer * a.ncol + col;
   const long long ns = (long long)a.ncol * a.nouter;  // tables are [row][system]
   const double* c1 = a.c1 + sys;
   const double* f = a.fac + sys;
   const int n = a.n;
+  const long long sr = a.s_row * w;
   // forward sweep: d1 overwrites the right-hand side
   VC d = tconv<VS, VC>(X[0]);
   d = a.form3 ? O::mul(d, f[0]) : O::div(d, f[0]);
   X[0] = tback<VC, VS>(d);
-  for (int t = 1; t < n - 1; ++t) {
-    VC r = tconv<VS, VC>(X[(long long)t * a.s_row]);
+  int t = 1;
+  for (; t + kTB <= n - 1; t += kTB) {
+    VS xb[kTB];
+    double fb[kTB], ab[kTB];
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      xb[q] = X[(long long)(t + q) * sr];
+      fb[q] = f[(long long)(t + q) * ns];
+      ab[q] = a.a[t + q];
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      VC r = O::sub_amul(tconv<VS, VC>(xb[q]), ab[q], d);
+      d = a.form3 ? O::mul(r, fb[q]) : O::div(r, fb[q]);
+      xb[q] = tback<VC, VS>(d);
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) X[(long long)(t + q) * sr] = xb[q];
+  }
+  for (; t < n - 1; ++t) {
+    VC r = tconv<VS, VC>(X[(long long)t * sr]);
     r = O::sub_amul(r, a.a[t], d);
     d = a.form3 ? O::mul(r, f[t * ns]) : O::div(r, f[t * ns]);
-    X[(long long)t * a.s_row] = tback<VC, VS>(d);
+    X[(long long)t * sr] = tback<VC, VS>(d);
   }
   {
     const double piv = f[(n - 1) * ns];
-    VC r = tconv<VS, VC>(X[(long long)(n - 1) * a.s_row]);
+    VC r = tconv<VS, VC>(X[(long long)(n - 1) * sr]);
     if (piv != 0.0) d = O::div(O::sub_amul(r, a.a[n - 1], d), piv);
     else d = O::zero();
   }
   // backward sweep
   VC xn = d;
-  X[(long long)(n - 1) * a.s_row] = tback<VC, VS>(xn);
-  for (int t = n - 2; t >= 0; --t) {
-    VC dt = tconv<VS, VC>(X[(long long)t * a.s_row]);
+  X[(long long)(n - 1) * sr] = tback<VC, VS>(xn);
+  t = n - 2;
+  for (; t - kTB + 1 >= 0; t -= kTB) {
+    VS xb[kTB];
+    double cb[kTB];
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      xb[q] = X[(long long)(t - q) * sr];
+      cb[q] = c1[(long long)(t - q) * ns];
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      xn = O::sub_amul(tconv<VS, VC>(xb[q]), cb[q], xn);
+      xb[q] = tback<VC, VS>(xn);
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) X[(long long)(t - q) * sr] = xb[q];
+  }
+  for (; t >= 0; --t) {
+    VC dt = tconv<VS, VC>(X[(long long)t * sr]);
     xn = O::sub_amul(dt, c1[t * ns], xn);
-    X[(long long)t * a.s_row] = tback<VC, VS>(xn);
+    X[(long long)t * sr] = tback<VC, VS>(xn);
   }
 }
 
