@@ -174,14 +174,21 @@ namespace {
 
 int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-// Radix schedule 4*, 2, 3* (the Stockham stages of fen_fft.cuh).
-bool make_plan(int M, FFTPlan& P) {
+// Radix schedule: the largest power-of-two radices up to maxr first (fft_max_radix gives the
+// kernels' limits), then 3s; the earlier radices' product is then a power of two at every
+// power-of-two pass.
+bool make_plan(int M, FFTPlan& P, int maxr) {
   P.M = M;
   P.nst = 0;
   int m = M;
+  if (maxr >= 16)
+    while (m % 16 == 0) { P.R[P.nst++] = 16; m /= 16; }
+  if (maxr >= 8)
+    while (m % 8 == 0) { P.R[P.nst++] = 8; m /= 8; }
   while (m % 4 == 0) { P.R[P.nst++] = 4; m /= 4; }
-  while (m % 2 == 0) { P.R[P.nst++] = 2; m /= 2; }
+  if (m % 2 == 0) { P.R[P.nst++] = 2; m /= 2; }
   while (m % 3 == 0) { P.R[P.nst++] = 3; m /= 3; }
+  fft_plan_magic(P);
   return m == 1 && P.nst <= kMaxStages;
 }
 
@@ -206,7 +213,8 @@ int upload_table(fen_ctx* c, const std::vector<double2>& h, const double2** out6
 // Twiddles of one axis of real length n (periodic: r2c/c2c; Neumann: DCT).
 int make_axis(fen_ctx* c, int ax, int n) {
   FFTPlan ph, pf;
-  if (n % 2 != 0 || !make_plan(n / 2, ph) || !make_plan(n, pf))
+  const int maxr = c->mixed ? (ax == 0 ? kFftMaxR32Row : kFftMaxR32Col) : kFftMaxR64;
+  if (n % 2 != 0 || !make_plan(n / 2, ph, maxr) || !make_plan(n, pf, maxr))
     return fail(FEN_ERR_ARG, "grid size " + std::to_string(n) + " must be 2^a 3^b with a >= 1");
   c->plan_half[ax] = ph;
   c->plan_full[ax] = pf;

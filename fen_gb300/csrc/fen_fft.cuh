@@ -2,7 +2,7 @@
 //
 // FEN calls FFTW once per 1D line (dfftw_execute_dft_r2c / dft / dft_c2r / r2r with
 // REDFT10 and REDFT01, poisson.f90:336-593, 967-1432).  Here one CTA transforms a batch of
-// lines staged in shared memory with a mixed-radix (4, 2, 3) Stockham autosort FFT.  Real
+// lines staged in shared memory with a mixed-radix (16, 8, 4, 2, 3) Stockham autosort FFT.  Real
 // transforms use the half-length complex FFT with the usual even/odd packing, and the DCTs
 // use Makhoul's reordering, so every transform costs one complex FFT of length n/2.
 // Transform definitions follow FFTW's documented ones: unnormalised, forward sign -1,
@@ -14,13 +14,37 @@
 namespace fen {
 
 constexpr int kMaxStages = 16;
+// Largest FFT radices compiled (build-time tuning knobs; see fft_max_radix).
+#ifndef FEN_FFT_MAXR64
+#define FEN_FFT_MAXR64 8
+#endif
+#ifndef FEN_FFT_MAXR32_COL
+#define FEN_FFT_MAXR32_COL 16
+#endif
 
 // Radix schedule of one complex FFT length, built on the host.
 struct FFTPlan {
   int M;                       // complex length
   int nst;                     // stages
-  int R[kMaxStages];           // radices, 4s first, then 2, then 3
+  int R[kMaxStages];           // radices: 16s or 8s first, then at most one 4 and one 2, then 3s
+  unsigned nsm[kMaxStages];    // fast-division multiplier of the stage's span Ns (fft_magic)
 };
+
+// Multiplier m of the fast division n / d = umulhi(n, m), m = floor(2^32 / d) + 1 (0 for
+// d = 1); exact for n * d < 2^32, which holds for every index here.  32-bit arithmetic only:
+// floor(2^32 / d) = floor((2^32 - 1) / d) unless d is a power of two.
+__host__ __device__ inline unsigned fft_magic(unsigned d) {
+  return d > 1 ? 0xffffffffu / d + 1u + ((d & (d - 1)) == 0 ? 1u : 0u) : 0u;
+}
+
+// Fill the fast-division multipliers of a plan's radix schedule.
+inline void fft_plan_magic(FFTPlan& P) {
+  unsigned ns = 1;
+  for (int s = 0; s < P.nst; ++s) {
+    P.nsm[s] = fft_magic(ns);
+    ns *= (unsigned)P.R[s];
+  }
+}
 
 // Twiddle tables of one transform axis (device pointers; values computed on the host in
 // FP64 with libm cos/sin, stored as double2 for FP64 kernels and rounded to float2 for FP32).
@@ -69,56 +93,139 @@ __device__ __forceinline__ void dft3(T2& a, T2& b, T2& c) {
   c = csub(m, q);
 }
 
-// One complex FFT of length P.M on `nl` lines held in shared memory.  Element (line l,
-// position p) lives at buf[l * ls + p * es].  Threads are mapped line-fastest so that, with
-// es = number of lines and ls = 1, every load and store is bank-conflict free.  Returns the
-// buffer holding the result (a or b).
-template <int DIR, typename T2>
+// Division by a run-time constant d with multiplier fft_magic(d).
+struct FastDiv {
+  unsigned d, m;
+};
+__device__ __forceinline__ int fdivi(int n, FastDiv f) { return f.d > 1 ? (int)__umulhi((unsigned)n, f.m) : n; }
+
+// cos(2 pi m/16), m = 0..15 (the in-register radix-8/16 rotations).
+__device__ __forceinline__ double cos16d(int m) {
+  switch (m & 15) {
+    case 0: return 1.0;
+    case 1: case 15: return 0.92387953251128674;
+    case 2: case 14: return 0.70710678118654752;
+    case 3: case 13: return 0.38268343236508977;
+    case 4: case 12: return 0.0;
+    case 5: case 11: return -0.38268343236508977;
+    case 6: case 10: return -0.70710678118654752;
+    case 8: return -1.0;
+    default: return -0.92387953251128674;  // 7, 9
+  }
+}
+
+// v * exp(DIR 2 pi i m / R) for R | 16 and m known at compile time after unrolling.
+template <int DIR, int R, typename T2>
+__device__ __forceinline__ T2 rot16(T2 v, int m) {
+  typedef decltype(T2::x) T;
+  const int e = (m * (16 / R)) & 15;
+  if (e == 0) return v;
+  if (e == 4) return DIR < 0 ? mk<T2>(v.y, -v.x) : mk<T2>(-v.y, v.x);
+  if (e == 8) return mk<T2>(-v.x, -v.y);
+  if (e == 12) return DIR < 0 ? mk<T2>(-v.y, v.x) : mk<T2>(v.y, -v.x);
+  const T c = (T)cos16d(e), s = (T)DIR * (T)cos16d(e + 12);
+  return mk<T2>(fmx(v.x, c, -(v.y * s)), fmx(v.x, s, v.y * c));
+}
+
+// In-register DFT of size R in natural order (R = 2, 3, 4, 8, 16); 8 and 16 are A x B
+// compositions (DFT-A over the stride-B subsequences, twiddles w_R^(n2 k1), DFT-B).
+template <int DIR, int R, typename T2>
+__device__ __forceinline__ void dft_r(T2 (&x)[16]);
+template <int DIR, int A, int B, typename T2>
+__device__ __forceinline__ void dft_ab(T2 (&x)[16]) {
+  T2 y[A * B];
+#pragma unroll
+  for (int n2 = 0; n2 < B; ++n2) {
+    T2 tt[16];
+#pragma unroll
+    for (int n1 = 0; n1 < A; ++n1) tt[n1] = x[B * n1 + n2];
+    dft_r<DIR, A, T2>(tt);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) y[n2 * A + k1] = rot16<DIR, A * B, T2>(tt[k1], n2 * k1);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < A; ++k1) {
+    T2 tt[16];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) tt[n2] = y[n2 * A + k1];
+    dft_r<DIR, B, T2>(tt);
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) x[k1 + A * k2] = tt[k2];
+  }
+}
+template <int DIR, int R, typename T2>
+__device__ __forceinline__ void dft_r(T2 (&x)[16]) {
+  if (R == 2) dft2<DIR>(x[0], x[1]);
+  else if (R == 3) dft3<DIR>(x[0], x[1], x[2]);
+  else if (R == 4) dft4<DIR>(x[0], x[1], x[2], x[3]);
+  else if (R == 8) dft_ab<DIR, 4, 2, T2>(x);
+  else if (R == 16) dft_ab<DIR, 4, 4, T2>(x);
+}
+
+// One radix-R Stockham pass over nl lines (element (line l, position p) at buf[l*ls + p*es]),
+// lines fastest over threads (strided layouts stay bank-conflict free).
+template <int DIR, int R, typename T2>
+__device__ __forceinline__ void fft_pass_r(const T2* __restrict__ src0, T2* __restrict__ dst0, int work, FastDiv fnl,
+                                           int ls, int es, int Ns, FastDiv fns, bool ns_pow2, int nb, int tstep,
+                                           const double2* __restrict__ tw) {
+  for (int t = threadIdx.x; t < work; t += blockDim.x) {
+    const int j = fdivi(t, fnl);
+    const int l = t - j * (int)fnl.d;
+    const int k = ns_pow2 ? (j & (Ns - 1)) : j - fdivi(j, fns) * Ns;
+    const T2* src = src0 + l * ls;
+    T2* dst = dst0 + l * ls;
+    T2 v[16];
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = src[(j + q * nb) * es];
+    if (Ns > 1) {
+#pragma unroll
+      for (int q = 1; q < R; ++q) {
+        const T2 w = ldtw<T2>(tw, q * k * tstep);
+        v[q] = (DIR < 0) ? cmul(v[q], w) : cmulc(v[q], w);
+      }
+    }
+    dft_r<DIR, R, T2>(v);
+    const int o = (j - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; ++q) dst[(o + q * Ns) * es] = v[q];
+  }
+}
+
+// Largest radix compiled per kernel; the host's plans (make_plan's maxr) match.  FP64
+// transforms are FP64-issue bound and gain from radix 8 (fewer twiddle products and adds).
+// FP32 column transforms take radix 16; FP32 x-line transforms stay at radix 4, whose low
+// register count keeps the SM fully occupied for their memory-bound load and store phases.
+constexpr int kFftMaxR64 = FEN_FFT_MAXR64;
+constexpr int kFftMaxR32Row = 4;
+constexpr int kFftMaxR32Col = FEN_FFT_MAXR32_COL;
+template <typename T, bool CONTIG>
+__host__ __device__ constexpr int fft_max_radix() {
+  return sizeof(T) == 8 ? kFftMaxR64 : (CONTIG ? kFftMaxR32Row : kFftMaxR32Col);
+}
+
+// One complex FFT of length P.M on `nl` lines held in shared memory, radix schedule P.R
+// (16, 8, 4, 2, 3; none above MAXR).  Returns the buffer holding the result (a or b).
+template <int DIR, int MAXR, typename T2>
 __device__ T2* smem_fft(T2* a, T2* b, int nl, int ls, int es, const FFTPlan& P, const double2* tw) {
   const int M = P.M;
+  const FastDiv fnl{(unsigned)nl, fft_magic((unsigned)nl)};
   int Ns = 1;
   for (int s = 0; s < P.nst; ++s) {
     const int R = P.R[s];
     const int nb = M / R;
     const int tstep = M / (Ns * R);
     const int work = nl * nb;
-    for (int t = threadIdx.x; t < work; t += blockDim.x) {
-      const int l = t % nl;
-      const int j = t / nl;
-      const int k = j % Ns;
-      const T2* src = a + l * ls;
-      T2* dst = b + l * ls;
-      const int idxD = (j - k) * R + k;
-      if (R == 4) {
-        T2 v0 = src[(j) * es], v1 = src[(j + nb) * es], v2 = src[(j + 2 * nb) * es], v3 = src[(j + 3 * nb) * es];
-        if (Ns > 1) {
-          T2 w1 = ldtw<T2>(tw, k * tstep), w2 = ldtw<T2>(tw, 2 * k * tstep), w3 = ldtw<T2>(tw, 3 * k * tstep);
-          if (DIR < 0) { v1 = cmul(v1, w1); v2 = cmul(v2, w2); v3 = cmul(v3, w3); }
-          else { v1 = cmulc(v1, w1); v2 = cmulc(v2, w2); v3 = cmulc(v3, w3); }
-        }
-        dft4<DIR>(v0, v1, v2, v3);
-        dst[(idxD) * es] = v0; dst[(idxD + Ns) * es] = v1; dst[(idxD + 2 * Ns) * es] = v2; dst[(idxD + 3 * Ns) * es] = v3;
-      } else if (R == 2) {
-        T2 v0 = src[(j) * es], v1 = src[(j + nb) * es];
-        if (Ns > 1) {
-          T2 w1 = ldtw<T2>(tw, k * tstep);
-          v1 = (DIR < 0) ? cmul(v1, w1) : cmulc(v1, w1);
-        }
-        dft2<DIR>(v0, v1);
-        dst[(idxD) * es] = v0; dst[(idxD + Ns) * es] = v1;
-      } else {  // R == 3
-        T2 v0 = src[(j) * es], v1 = src[(j + nb) * es], v2 = src[(j + 2 * nb) * es];
-        if (Ns > 1) {
-          T2 w1 = ldtw<T2>(tw, k * tstep), w2 = ldtw<T2>(tw, 2 * k * tstep);
-          if (DIR < 0) { v1 = cmul(v1, w1); v2 = cmul(v2, w2); }
-          else { v1 = cmulc(v1, w1); v2 = cmulc(v2, w2); }
-        }
-        dft3<DIR>(v0, v1, v2);
-        dst[(idxD) * es] = v0; dst[(idxD + Ns) * es] = v1; dst[(idxD + 2 * Ns) * es] = v2;
-      }
-    }
+    const bool p2 = (Ns & (Ns - 1)) == 0;
+    const FastDiv fns{(unsigned)Ns, P.nsm[s]};
+    if (MAXR >= 16 && R == 16) fft_pass_r<DIR, (MAXR >= 16 ? 16 : 2), T2>(a, b, work, fnl, ls, es, Ns, fns, p2, nb, tstep, tw);
+    else if (MAXR >= 8 && R == 8) fft_pass_r<DIR, (MAXR >= 8 ? 8 : 2), T2>(a, b, work, fnl, ls, es, Ns, fns, p2, nb, tstep, tw);
+    else if (R == 4) fft_pass_r<DIR, 4, T2>(a, b, work, fnl, ls, es, Ns, fns, p2, nb, tstep, tw);
+    else if (R == 2) fft_pass_r<DIR, 2, T2>(a, b, work, fnl, ls, es, Ns, fns, p2, nb, tstep, tw);
+    else fft_pass_r<DIR, 3, T2>(a, b, work, fnl, ls, es, Ns, fns, p2, nb, tstep, tw);
     __syncthreads();
-    T2* t = a; a = b; b = t;
+    T2* t = a;
+    a = b;
+    b = t;
     Ns *= R;
   }
   return a;

@@ -441,9 +441,9 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
   // ---------------- transform ----------------
   T2* res;
   if (OP == OP_R2C || OP == OP_DCT2 || OP == OP_C2C_F || OP == OP_C2C_SOLVE)
-    res = smem_fft<-1>(bufA, bufB, nl, 1, nl, a.plan, a.tw.wM);
+    res = smem_fft<-1, fft_max_radix<T, CONTIG>()>(bufA, bufB, nl, 1, nl, a.plan, a.tw.wM);
   else
-    res = smem_fft<+1>(bufA, bufB, nl, 1, nl, a.plan, a.tw.wM);
+    res = smem_fft<+1, fft_max_radix<T, CONTIG>()>(bufA, bufB, nl, 1, nl, a.plan, a.tw.wM);
 
   if (OP == OP_C2C_SOLVE) {
     // normalise and divide by the eigenvalue sum, zero mode -> 0 (poisson.f90:458-471, 991-1005)
@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     }
     __syncthreads();
     T2* other = (res == bufA) ? bufB : bufA;
-    res = smem_fft<+1>(res, other, nl, 1, nl, a.plan, a.tw.wM);
+    res = smem_fft<+1, fft_max_radix<T, CONTIG>()>(res, other, nl, 1, nl, a.plan, a.tw.wM);
   }
 
   // ---------------- store ----------------

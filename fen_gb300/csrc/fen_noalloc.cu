@@ -85,9 +85,12 @@ bool make_plan_local(int M, FFTPlan& P) {
   P.M = M;
   P.nst = 0;
   int m = M;
+  if (kFftMaxR64 >= 8)
+    while (m % 8 == 0) { P.R[P.nst++] = 8; m /= 8; }
   while (m % 4 == 0) { P.R[P.nst++] = 4; m /= 4; }
-  while (m % 2 == 0) { P.R[P.nst++] = 2; m /= 2; }
+  if (m % 2 == 0) { P.R[P.nst++] = 2; m /= 2; }
   while (m % 3 == 0) { P.R[P.nst++] = 3; m /= 3; }
+  fft_plan_magic(P);
   return m == 1 && P.nst <= kMaxStages;
 }
 
