@@ -25,9 +25,9 @@ __global__ void __launch_bounds__(256) k_adj_div2(Layout L, const double* __rest
                                                   const double* __restrict__ y, double s, double idx, double idy,
                                                   double* __restrict__ out) {
   const long long ncell = (long long)L.n0 * L.n1;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const int j = 1 + (int)(t / L.n0);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j;
     const long long c = L.idx(i, j, 0);
     const double d = (x[c] - x[c - 1]) * idx + (y[c] - y[c - L.sx]) * idy;
     out[c] = (a ? a[c] : 0.0) + s * d;
@@ -39,9 +39,9 @@ __global__ void __launch_bounds__(256) k_adj_grad2(Layout L, const double* __res
                                                    const double* __restrict__ b, double f, double idx, double idy,
                                                    double* __restrict__ uo, double* __restrict__ vo) {
   const long long ncell = (long long)L.n0 * L.n1;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const int j = 1 + (int)(t / L.n0);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j;
     const long long c = L.idx(i, j, 0);
     uo[c] = u[c] - f * (b[c + 1] - b[c]) * idx;
     vo[c] = v[c] - f * (b[c + L.sx] - b[c]) * idy;
@@ -53,9 +53,9 @@ __global__ void __launch_bounds__(256) k_adj_dv2(Layout L, const double* __restr
                                                  double* __restrict__ dou, double* __restrict__ dov, double dtA, double dtB,
                                                  double* __restrict__ dhu, double* __restrict__ dhv) {
   const long long ncell = (long long)L.n0 * L.n1;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const int j = 1 + (int)(t / L.n0);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j;
     const long long c = L.idx(i, j, 0);
     dhu[c] = dou[c] + dtA * us[c];
     dhv[c] = dov[c] + dtA * vs[c];
@@ -72,9 +72,9 @@ __global__ void __launch_bounds__(256) k_adj_state2(Layout L, const double* __re
                                                     double* __restrict__ uo, double* __restrict__ vo) {
   const long long ncell = (long long)L.n0 * L.n1;
   const long long sy = L.sx;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const int j = 1 + (int)(t / L.n0);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j;
     const long long c = L.idx(i, j, 0);
     // flux adjoints: F_u at i+1/2, i-1/2; F_v at j+1/2, j-1/2; C at (i,j), (i,j-1), (i-1,j)
     const double Fu_p = (hu[c + 1] - hu[c]) * idx, Fu_m = (hu[c] - hu[c - 1]) * idx;

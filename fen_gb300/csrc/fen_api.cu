@@ -557,7 +557,9 @@ LineArgs<float> typed_args<float>(const Stage& s) {
 
 template <typename T, int DIM, bool CONTIG, int OP, int LD, int ST>
 int launch_line_t(fen_ctx* c, const Stage& s, const LineArgs<T>& a) {
-  auto kern = k_line<T, DIM, CONTIG, OP, LD, ST>;
+  void (*kern)(LineArgs<T>);
+  if constexpr (sizeof(T) == 4 && CONTIG) kern = k_line_row32<DIM, OP, LD, ST>;
+  else kern = k_line<T, DIM, CONTIG, OP, LD, ST>;
   if (s.smem > 200 * 1024) return fail(FEN_ERR_ARG, "transform length too large for one CTA");
   if (g_attr_only) {
     CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));

@@ -98,6 +98,11 @@ struct FastDiv {
   unsigned d, m;
 };
 __device__ __forceinline__ int fdivi(int n, FastDiv f) { return f.d > 1 ? (int)__umulhi((unsigned)n, f.m) : n; }
+// (q, r) = (t / d, t % d) for 0 <= t, t * d < 2^32.
+__device__ __forceinline__ void divmod(int t, FastDiv f, int& q, int& r) {
+  q = fdivi(t, f);
+  r = t - q * (int)f.d;
+}
 
 // cos(2 pi m/16), m = 0..15 (the in-register radix-8/16 rotations).
 __device__ __forceinline__ double cos16d(int m) {

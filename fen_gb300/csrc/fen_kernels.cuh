@@ -37,8 +37,7 @@ struct PredArgs {
 // result differs from FEN's operation order by rounding only.
 template <int DIM>
 __global__ void __launch_bounds__(256) k_predictor(Layout L, const StepScalars* __restrict__ sc, PredArgs<double> a) {
-  const unsigned n0 = L.n0, n1 = L.n1;
-  const unsigned ncell = n0 * n1 * (unsigned)L.n2;
+  const long long ncell = (long long)L.n0 * L.n1 * L.n2;
   const double A = sc->A, B = sc->B;
   const double dt = a.use_dev_dt ? sc->dt : a.dt_host;
   const double idx = a.id[0], idy = a.iso ? a.id[0] : a.id[1], idz = a.iso ? a.id[0] : a.id[2];
@@ -55,11 +54,9 @@ __global__ void __launch_bounds__(256) k_predictor(Layout L, const StepScalars* 
   const double* __restrict__ V = a.v;
   const double* __restrict__ W = a.w;
   const double* __restrict__ P = a.p;
-  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < ncell; t += gridDim.x * blockDim.x) {
-    const unsigned r = t / n0;
-    const int i = 1 + (int)(t - r * n0);
-    const int j = 1 + (int)(r % n1);
-    const int k = 1 + (int)(r / n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     const double uc = U[c], uip = U[c + 1], uim = U[c - 1], ujp = U[c + sy], ujm = U[c - sy];
     const double vc = V[c], vip = V[c + 1], vim = V[c - 1], vjp = V[c + sy], vjm = V[c - sy];
@@ -346,7 +343,7 @@ __device__ __forceinline__ T div_at(const LineArgs<T>& a, int i, int j, int k) {
 }
 
 template <typename T, int DIM, bool CONTIG, int OP, int LD, int ST>
-__global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
+__device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   typedef typename cpx<T>::t T2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = a.n;
@@ -359,6 +356,9 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
   const int outer = blockIdx.y;
   const int nlv = min(nl, a.nlines - line0);  // valid lines in this CTA
   const int tid = threadIdx.x, nth = blockDim.x;
+  // element -> (line, position) splits by multiply-high division (no per-element divide)
+  const FastDiv fN{(unsigned)n, fft_magic((unsigned)n)}, fM{(unsigned)M, fft_magic((unsigned)M)};
+  const FastDiv fM1{(unsigned)(M + 1), fft_magic((unsigned)(M + 1))}, fL{(unsigned)nl, fft_magic((unsigned)nl)};
   // position-major smem: element (l, p) at p*nl + l
   auto S = [&](int l, int p) -> T2& { return bufA[(size_t)p * nl + l]; };
   T* Sr = reinterpret_cast<T*>(bufA);  // real view: real slot r of line l at (r/2 * nl + l)*2 + (r&1)
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     const int work = nl * n;
     for (int t = tid; t < work; t += nth) {
       int l, i;
-      if (CONTIG) { l = t / n; i = t % n; } else { l = t % nl; i = t / nl; }
+      if (CONTIG) divmod(t, fN, l, i); else divmod(t, fL, i, l);
       T x = 0;
       if (l < nlv) {
         if (LD == LD_FIELD || LD == LD_DIV || LD == LD_DIVMIX) {
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     const int work = nl * M;
     for (int t = tid; t < work; t += nth) {
       int l, kk;
-      if (CONTIG) { l = t / M; kk = t % M; } else { l = t % nl; kk = t / nl; }
+      if (CONTIG) divmod(t, fM, l, kk); else divmod(t, fL, kk, l);
       T2 z = mk<T2>(0, 0);
       if (l < nlv) {
         const long long base = (long long)(line0 + l) * a.in_line + (long long)outer * a.in_outer;
@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     const int work = nl * M;
     for (int t = tid; t < work; t += nth) {
       int l, p;
-      if (CONTIG) { l = t / M; p = t % M; } else { l = t % nl; p = t / nl; }
+      if (CONTIG) divmod(t, fM, l, p); else divmod(t, fL, p, l);
       T2 z = mk<T2>(0, 0);
       if (l < nlv) z = inC[(long long)(line0 + l) * a.in_line + (long long)p * a.in_pos + (long long)outer * a.in_outer];
       S(l, p) = z;
@@ -449,7 +449,8 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     // normalise and divide by the eigenvalue sum, zero mode -> 0 (poisson.f90:458-471, 991-1005)
     const int work = nl * M;
     for (int t = tid; t < work; t += nth) {
-      const int l = t % nl, p = t / nl;
+      int l, p;
+      divmod(t, fL, p, l);
       if (l < nlv) {
         T2& z = res[(size_t)p * nl + l];
         if (a.inv_lam) {
@@ -480,7 +481,7 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     const int work = nl * (M + 1);
     for (int t = tid; t < work; t += nth) {
       int l, kk;
-      if (CONTIG) { l = t / (M + 1); kk = t % (M + 1); } else { l = t % nl; kk = t / nl; }
+      if (CONTIG) divmod(t, fM1, l, kk); else divmod(t, fL, kk, l);
       if (l < nlv) {
         T2 X = r2c_post(res + l, nl, M, kk, a.tw.wN);
         if (do_scale) X = mk<T2>(X.x * scale, X.y * scale);
@@ -491,7 +492,7 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     const int work = nl * (M + 1);
     for (int t = tid; t < work; t += nth) {
       int l, kk;
-      if (CONTIG) { l = t / (M + 1); kk = t % (M + 1); } else { l = t % nl; kk = t / nl; }
+      if (CONTIG) divmod(t, fM1, l, kk); else divmod(t, fL, kk, l);
       if (l < nlv) {
         const T2 Vk = r2c_post(res + l, nl, M, kk, a.tw.wN);
         const T2 qv = cmul(ldtw<T2>(a.tw.wD, kk), Vk);
@@ -507,7 +508,7 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     const int work = nl * n;
     for (int t = tid; t < work; t += nth) {
       int l, i;
-      if (CONTIG) { l = t / n; i = t % n; } else { l = t % nl; i = t / nl; }
+      if (CONTIG) divmod(t, fN, l, i); else divmod(t, fL, i, l);
       if (l < nlv) {
         int q = i;  // index into v (the c2r output)
         if (OP == OP_DCT3) q = (i & 1) ? (n - 1 - (i >> 1)) : (i >> 1);
@@ -539,7 +540,7 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
     const int work = nl * M;
     for (int t = tid; t < work; t += nth) {
       int l, p;
-      if (CONTIG) { l = t / M; p = t % M; } else { l = t % nl; p = t / nl; }
+      if (CONTIG) divmod(t, fM, l, p); else divmod(t, fL, p, l);
       if (l < nlv) {
         T2 z = R(l, p);
         if (do_scale) z = mk<T2>(z.x * scale, z.y * scale);
@@ -547,6 +548,18 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
       }
     }
   }
+}
+
+template <typename T, int DIM, bool CONTIG, int OP, int LD, int ST>
+__global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
+  line_body<T, DIM, CONTIG, OP, LD, ST>(a);
+}
+
+// FP32 x-line transforms are memory-latency bound: compiled for 6 resident CTAs per SM
+// (<= 40 registers), where the default register choice would leave 4.
+template <int DIM, int OP, int LD, int ST>
+__global__ void __launch_bounds__(256, 6) k_line_row32(LineArgs<float> a) {
+  line_body<float, DIM, true, OP, LD, ST>(a);
 }
 
 // ------------------------------------------------------------------------------------
@@ -767,11 +780,9 @@ __global__ void __launch_bounds__(256) k_correct(Layout L, const StepScalars* __
   const T idx = (T)a.id[0];
   const T idy = a.iso ? idx : (T)a.id[1];
   const T idz = a.iso ? idx : (T)a.id[2];
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long r = t / L.n0;
-    const int j = 1 + (int)(r % L.n1);
-    const int k = 1 + (int)(r / L.n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     const T ph = a.phi[c];
     a.u[c] = a.us[c] - (a.phi[c + 1] - ph) * idx * f;
@@ -799,11 +810,9 @@ __global__ void __launch_bounds__(256) k_mean_subtract(Layout L, const double* p
   if (blockIdx.x == 0 && threadIdx.x == 0) sc->mean = m;
   const T mt = (T)m;
   const long long ncell = (long long)L.n0 * L.n1 * L.n2;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long r = t / L.n0;
-    const int j = 1 + (int)(r % L.n1);
-    const int k = 1 + (int)(r / L.n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     phi[c] = phi[c] - mt;
   }
@@ -829,11 +838,9 @@ __global__ void __launch_bounds__(256) k_checks(Layout L, CheckArgs<T> a) {
   T md = -INFINITY, mv = 0;
   bool bad = false;
   const T idx = (T)a.id[0];
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long r = t / L.n0;
-    const int j = 1 + (int)(r % L.n1);
-    const int k = 1 + (int)(r / L.n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     const T uc = a.u[c], vc = a.v[c];
     T vel = fabs(uc) + fabs(vc);

@@ -146,18 +146,15 @@ struct PredDFArgs {
 
 template <int DIM>
 __global__ void __launch_bounds__(256) k_predictor_df(Layout L, const StepScalars* __restrict__ sc, PredDFArgs a) {
-  const unsigned n0 = L.n0, n1 = L.n1;
-  const unsigned ncell = n0 * n1 * (unsigned)L.n2;
+  const long long ncell = (long long)L.n0 * L.n1 * L.n2;
   const DF A = DF{sc->Ap[0], sc->Ap[1]}, B = DF{sc->Bp[0], sc->Bp[1]}, DT = DF{sc->dtp[0], sc->dtp[1]};
   const DF qx = DF{a.qx.hi, a.qx.lo}, qy = DF{a.qy.hi, a.qy.lo}, qz = DF{a.qz.hi, a.qz.lo};
   const DF mx = DF{a.mx.hi, a.mx.lo}, my = DF{a.my.hi, a.my.lo}, mz = DF{a.mz.hi, a.mz.lo};
   const long long sy = L.sx, sz = L.sp;
   const DFField U = a.u, V = a.v, W = a.w, P = a.p;
-  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < ncell; t += gridDim.x * blockDim.x) {
-    const unsigned r = t / n0;
-    const int i = 1 + (int)(t - r * n0);
-    const int j = 1 + (int)(r % n1);
-    const int k = 1 + (int)(r / n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     const DF uc = dfv(U, c), uip = dfv(U, c + 1), uim = dfv(U, c - 1), ujp = dfv(U, c + sy), ujm = dfv(U, c - sy);
     const DF vc = dfv(V, c), vip = dfv(V, c + 1), vim = dfv(V, c - 1), vjp = dfv(V, c + sy), vjm = dfv(V, c - sy);
@@ -275,11 +272,9 @@ __global__ void __launch_bounds__(256) k_correct_df(Layout L, const StepScalars*
   const float idx = (float)a.id[0];
   const float idy = a.iso ? idx : (float)a.id[1];
   const float idz = a.iso ? idx : (float)a.id[2];
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long r = t / L.n0;
-    const int j = 1 + (int)(r % L.n1);
-    const int k = 1 + (int)(r / L.n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     const float ph = a.phi[c];
     const float* q = a.dphi;
@@ -328,11 +323,9 @@ __global__ void __launch_bounds__(256) k_checks_df(Layout L, CheckDFArgs a) {
   const long long ncell = (long long)L.n0 * L.n1 * L.n2;
   float md = -INFINITY, mv = 0.0f;
   bool bad = false;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long r = t / L.n0;
-    const int j = 1 + (int)(r % L.n1);
-    const int k = 1 + (int)(r / L.n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     float vel = fabsf(a.u.hi[c]) + fabsf(a.v.hi[c]);
     float d = 0.0f;
@@ -392,11 +385,9 @@ template <int DIM>
 __global__ void __launch_bounds__(256) k_residual_df(Layout L, const StepScalars* __restrict__ sc, ResidualArgs a) {
   const long long ncell = (long long)L.n0 * L.n1 * L.n2;
   const F2 rod = split_d(sc->rho_over_dt);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long rr = t / L.n0;
-    const int j = 1 + (int)(rr % L.n1);
-    const int k = 1 + (int)(rr / L.n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     const F2 dv = div_df<DIM>(L, a.u, a.v, a.w, a.du, a.dv, a.dw, a.dul, a.dvl, a.dwl, a.idp, i, j, k);
     const F2 b = mul_pair(dv.hi, dv.lo, rod);

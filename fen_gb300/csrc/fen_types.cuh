@@ -28,6 +28,33 @@ struct Layout {
   }
 };
 
+// Interior-cell walk of a grid-stride loop over t = t0, t0 + stride, ... (Fortran order, i
+// fastest).  The 0-based (i, j, k) advance by the stride's own (si, sj, sk) with carries, so
+// the 64-bit divisions by n0 and n1 happen once per thread instead of once per cell.
+struct CellWalk {
+  long long t0, stride;
+  int i, j, k, si, sj, sk;
+  __device__ __forceinline__ CellWalk(const Layout& L, long long t, long long s) : t0(t), stride(s) {
+    long long r = t / L.n0;
+    i = (int)(t - r * L.n0);
+    j = (int)(r % L.n1);
+    k = (int)(r / L.n1);
+    r = s / L.n0;
+    si = (int)(s - r * L.n0);
+    sj = (int)(r % L.n1);
+    sk = (int)(r / L.n1);
+  }
+  __device__ __forceinline__ void next(const Layout& L) {
+    i += si;
+    int c = i >= L.n0;
+    if (c) i -= L.n0;
+    j += sj + c;
+    c = j >= L.n1;
+    if (c) j -= L.n1;
+    k += sk + c;
+  }
+};
+
 // Storage plane of Fortran plane k.
 template <int DIM>
 __host__ __device__ __forceinline__ int kst(int k) { return DIM == 3 ? k : 0; }

@@ -47,11 +47,9 @@ __global__ void __launch_bounds__(256) k_predictor_var(Layout L, const StepScala
   const double* V = a.v;
   const double* W = a.w;
   const double q = 0.25;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long r = t / L.n0;
-    const int j = 1 + (int)(r % L.n1);
-    const int k = 1 + (int)(r / L.n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     const long long so[3] = {1, sy, sz};
     const double uc = U[c], vc = V[c];
@@ -164,11 +162,9 @@ __global__ void __launch_bounds__(256) k_correct_var(Layout L, const StepScalars
   const long long ncell = (long long)L.n0 * L.n1 * L.n2;
   const double dt = sc->dt;
   const double idx = a.id[0], idy = a.iso ? a.id[0] : a.id[1], idz = a.iso ? a.id[0] : a.id[2];
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(t % L.n0);
-    const long long r = t / L.n0;
-    const int j = 1 + (int)(r % L.n1);
-    const int k = 1 + (int)(r / L.n1);
+  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
+    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     const long long so[3] = {1, L.sx, L.sp};
     const double idq[3] = {idx, idy, idz};
