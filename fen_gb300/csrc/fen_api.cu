@@ -106,7 +106,7 @@ struct fen_ctx {
   // mixed-form FP32 fields: the state as hi/lo pairs, phi, the increment dt*rhs, dv_o, S
   float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr, *p32 = nullptr, *phi32 = nullptr;
   float *u32l = nullptr, *v32l = nullptr, *w32l = nullptr, *p32l = nullptr;
-  float *dphi32 = nullptr, *res32 = nullptr;  // refinement: correction of phi, residual
+  float* dphi32 = nullptr;  // refinement: correction of phi
   int refine = 0;
   float* d32[3] = {nullptr, nullptr, nullptr};
   float* dvo32[3] = {nullptr, nullptr, nullptr};
@@ -580,6 +580,10 @@ int launch_line_dim(fen_ctx* c, const Stage& s, int ld, const LineArgs<T>& a) {
     if (s.op == OP_DCT2 && ld == LD_DIV) return launch_line_t<T, DIM, true, OP_DCT2, LD_DIV, ST_REAL>(c, s, a);
     if (s.op == OP_DCT2 && ld == LD_DIVMIX) return launch_line_t<T, DIM, true, OP_DCT2, LD_DIVMIX, ST_REAL>(c, s, a);
     if (s.op == OP_DCT2 && ld == LD_FIELD) return launch_line_t<T, DIM, true, OP_DCT2, LD_FIELD, ST_REAL>(c, s, a);
+    if constexpr (sizeof(T) == 4) {
+      if (s.op == OP_R2C && ld == LD_RESID) return launch_line_t<T, DIM, true, OP_R2C, LD_RESID, ST_CPLX>(c, s, a);
+      if (s.op == OP_DCT2 && ld == LD_RESID) return launch_line_t<T, DIM, true, OP_DCT2, LD_RESID, ST_REAL>(c, s, a);
+    }
     if (s.op == OP_C2R) return launch_line_t<T, DIM, true, OP_C2R, LD_CPLX, ST_FIELD>(c, s, a);
     if (s.op == OP_DCT3) return launch_line_t<T, DIM, true, OP_DCT3, LD_REAL, ST_FIELD>(c, s, a);
   } else {
@@ -594,13 +598,25 @@ int launch_line_dim(fen_ctx* c, const Stage& s, int ld, const LineArgs<T>& a) {
   return fail(FEN_ERR_ARG, "unsupported transform stage");
 }
 
+// launch_stage's first_from_field: 1 loads the first transform from a field, kFirstResidual
+// forms the mixed refinement's residual from v* and the field phi.
+constexpr int kFirstResidual = 2;
+
 template <typename T>
 int launch_stage_t(fen_ctx* c, const Stage& s, int first_from_field, const void* field_src, void* dst) {
   LineArgs<T> a = typed_args<T>(s);
   if (dst && s.st == ST_FIELD) a.fdst = (T*)dst;
   for (int q = 0; q < 3; ++q) a.idp[q] = split_d(1.0 / c->d[q]);
   int ld = s.ld;
-  if (first_from_field) {
+  if (first_from_field == kFirstResidual) {
+    // mixed refinement: the first transform forms its own right-hand side from v* and phi
+    ld = LD_RESID;
+    a.fsrc = (const T*)field_src;
+    a.fu = (const T*)c->d32[0]; a.fv = (const T*)c->d32[1]; a.fw = (const T*)c->d32[2];
+    a.ful = c->d32l[0]; a.fvl = c->d32l[1]; a.fwl = c->d32l[2];
+    a.pu = DFField{c->u32, c->u32l}; a.pv = DFField{c->v32, c->v32l}; a.pw = DFField{c->w32, c->w32l};
+    for (int q = 0; q < 3; ++q) a.id2p[q] = split_d(1.0 / (c->d[q] * c->d[q]));
+  } else if (first_from_field) {
     ld = LD_FIELD;
     a.fsrc = (const T*)field_src;
   } else if (s.ld == LD_DIV) {
@@ -678,15 +694,16 @@ int ghost(fen_ctx* c, int nf, T* const* ptr, const int* ids, bool homogeneous = 
 int launch_mean(fen_ctx* c, float* target32 = nullptr) {
   const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
   const int grid = std::min(cdiv(ncell, 256), 152 * 8);
+  k_mean_reduce<<<1, 1024, 0, c->stream>>>(c->partial, c->npartial, c->mean_div, c->sc);
   if (c->mixed) {
     float* t = target32 ? target32 : c->phi32;
-    if (c->dim == 3) k_mean_subtract<float, 3><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, t);
-    else k_mean_subtract<float, 2><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, t);
+    if (c->dim == 3) k_mean_subtract<float, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, t);
+    else k_mean_subtract<float, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, t);
   } else {
-    if (c->dim == 3) k_mean_subtract<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, c->phi);
-    else k_mean_subtract<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, c->phi);
+    if (c->dim == 3) k_mean_subtract<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, c->phi);
+    else k_mean_subtract<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, c->phi);
   }
-  c->launches++;
+  c->launches += 2;
   CK(cudaGetLastError());
   return 0;
 }
@@ -947,24 +964,10 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
     if ((r = ghost<float>(c, 1, f, ids))) return r;
     if (c->refine) {
       // one iterative-refinement solve: r = b - L_h phi (double-float), L_h dphi = r (FP32)
-      ResidualArgs ra;
-      memset(&ra, 0, sizeof(ra));
-      ra.u = DFField{c->u32, c->u32l}; ra.v = DFField{c->v32, c->v32l}; ra.w = DFField{c->w32, c->w32l};
-      ra.du = c->d32[0]; ra.dv = c->d32[1]; ra.dw = c->d32[2];
-      ra.dul = c->d32l[0]; ra.dvl = c->d32l[1]; ra.dwl = c->d32l[2];
-      ra.phi = c->phi32;
-      ra.r = c->res32;
-      for (int q = 0; q < 3; ++q) {
-        ra.idp[q] = split_d(1.0 / c->d[q]);
-        ra.id2p[q] = split_d(1.0 / (c->d[q] * c->d[q]));
-      }
-      if (c->dim == 3) k_residual_df<3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ra);
-      else k_residual_df<2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, ra);
-      c->launches++;
-      CK(cudaGetLastError());
+      // (the residual is formed inside the first transform's load, kFirstResidual)
       const size_t ns = c->stages.size();
       for (size_t q = 0; q < ns; ++q)
-        if ((r = launch_stage(c, c->stages[q], q == 0, c->res32, c->dphi32))) return r;
+        if ((r = launch_stage(c, c->stages[q], q == 0 ? kFirstResidual : 0, c->phi32, c->dphi32))) return r;
       if (c->needs_mean && (r = launch_mean(c, c->dphi32))) return r;
       float* g[1] = {c->dphi32};
       if ((r = ghost<float>(c, 1, g, ids))) return r;
@@ -1139,7 +1142,7 @@ int fen_ctx_destroy(fen_ctx* c) {
   for (double* b : bufs) if (b) cudaFree(b);
   float* fb[] = {c->u32, c->v32, c->w32, c->p32, c->u32l, c->v32l, c->w32l, c->p32l, c->phi32, c->d32[0],
                  c->d32[1], c->d32[2], c->dvo32[0], c->dvo32[1], c->dvo32[2], c->S32[0], c->S32[1], c->S32[2],
-                 c->dphi32, c->res32, c->d32l[0], c->d32l[1], c->d32l[2], c->dvo32l[0], c->dvo32l[1], c->dvo32l[2]};
+                 c->dphi32, c->d32l[0], c->d32l[1], c->d32l[2], c->dvo32l[0], c->dvo32l[1], c->dvo32l[2]};
   for (float* b : fb) if (b) cudaFree(b);
   if (c->tmp64) cudaFree(c->tmp64);
   for (double* b : {c->rho, c->mu, c->p_o}) if (b) cudaFree(b);
@@ -1234,7 +1237,7 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
     for (float** f : fl)
       if ((r = alloc(f, L.total))) { fen_ctx_destroy(c); return r; }
     if ((r = alloc(&c->tmp64, L.total))) { fen_ctx_destroy(c); return r; }
-    if (c->refine && ((r = alloc(&c->dphi32, L.total)) || (r = alloc(&c->res32, L.total)))) { fen_ctx_destroy(c); return r; }
+    if (c->refine && (r = alloc(&c->dphi32, L.total))) { fen_ctx_destroy(c); return r; }
   } else {
     double** fl[] = {&c->phi, &c->us, &c->vs, &c->ws, &c->dvo[0], &c->dvo[1], &c->dvo[2]};
     for (double** f : fl)
@@ -1711,8 +1714,9 @@ int adj_step(fen_ctx* c, const double* u, const double* v) {
     if ((r = launch_stage(c, c->stages[q], q == 0, A.fh, A.bh))) return r;
   if (c->needs_mean) {
     const int g2 = std::min(cdiv((long long)c->n[0] * c->n[1], 256), 152 * 8);
-    k_mean_subtract<double, 2><<<g2, 256, 0, c->stream>>>(c->L, c->partial, c->npartial, c->mean_div, c->sc, A.bh);
-    c->launches++;
+    k_mean_reduce<<<1, 1024, 0, c->stream>>>(c->partial, c->npartial, c->mean_div, c->sc);
+    k_mean_subtract<double, 2><<<g2, 256, 0, c->stream>>>(c->L, c->sc, A.bh);
+    c->launches += 2;
   }
   {
     double* f[1] = {A.bh};

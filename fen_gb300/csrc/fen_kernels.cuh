@@ -284,7 +284,7 @@ static __global__ void __launch_bounds__(kTX * kTY) k_predictor_tile(Layout L, c
 //   CONTIG = false: lines along y or z (strided), a tile of consecutive columns per CTA.
 // ------------------------------------------------------------------------------------
 enum { OP_R2C = 0, OP_C2R, OP_C2C_F, OP_C2C_I, OP_C2C_SOLVE, OP_DCT2, OP_DCT3 };
-enum { LD_FIELD = 0, LD_DIV, LD_REAL, LD_CPLX, LD_DIVMIX };
+enum { LD_FIELD = 0, LD_DIV, LD_REAL, LD_CPLX, LD_DIVMIX, LD_RESID };
 enum { ST_FIELD = 0, ST_REAL, ST_CPLX };
 
 template <typename T>
@@ -304,7 +304,8 @@ struct LineArgs {
   const float *ful, *fvl, *fwl;  // LD_DIVMIX: the increment's lo part
   const double* rho_c;           // LD_DIV with variable density: div * rho(i,j,k) * rho_over_dt (= 1/dt)
   DFField pu, pv, pw;     // pair velocity of the mixed form (LD_DIVMIX)
-  F2 idp[3];              // 1/delta per axis as float pairs (LD_DIVMIX)
+  F2 idp[3];              // 1/delta per axis as float pairs (LD_DIVMIX, LD_RESID)
+  F2 id2p[3];             // 1/delta^2 per axis as float pairs (LD_RESID)
   const T* fsrc;          // LD_FIELD source
   T* fdst;                // ST_FIELD destination
   double* partial;        // ST_FIELD: per-CTA line sums (mean removal), may be null
@@ -371,12 +372,14 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   if (OP == OP_R2C || OP == OP_DCT2) {
     // n reals per line -> packed complex (DCT2 reorders first: v_m = x_2m, v_{n-1-m} = x_2m+1)
     const int work = nl * n;
+    F2 rod{0.f, 0.f};
+    if (LD == LD_RESID) rod = split_d(a.sc->rho_over_dt);
     for (int t = tid; t < work; t += nth) {
       int l, i;
       if (CONTIG) divmod(t, fN, l, i); else divmod(t, fL, i, l);
       T x = 0;
       if (l < nlv) {
-        if (LD == LD_FIELD || LD == LD_DIV || LD == LD_DIVMIX) {
+        if (LD == LD_FIELD || LD == LD_DIV || LD == LD_DIVMIX || LD == LD_RESID) {
           int j, k;
           row_jk<DIM>(line0 + l, outer, j, k);
           if (LD == LD_FIELD) x = a.fsrc[a.L.idx(i + 1, j, kst<DIM>(k))];
@@ -385,11 +388,24 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
             if (a.rho_c) x = x * (T)a.rho_c[a.L.idx(i + 1, j, kst<DIM>(k))];
             x = x * (T)a.sc->rho_over_dt;
           }
-          else {
+          else if (LD == LD_DIVMIX) {
             const F2 dd = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
                                       a.ful, a.fvl, a.fwl,
                                       a.idp, i + 1, j, k);
             x = (T)(dd.hi + dd.lo) * (T)a.sc->rho_over_dt;
+          } else {
+            // refinement right-hand side r = rho/dt D v* - L_h phi in double-float (phi = fsrc)
+            const long long c = a.L.idx(i + 1, j, kst<DIM>(k));
+            const F2 dd = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
+                                      a.ful, a.fvl, a.fwl,
+                                      a.idp, i + 1, j, k);
+            const F2 b = mul_pair(dd.hi, dd.lo, rod);
+            const float* ph = (const float*)a.fsrc;
+            F2 lap = add_pair(lap_term(ph, c, 1, a.id2p[0]), lap_term(ph, c, a.L.sx, a.id2p[1]));
+            if (DIM == 3) lap = add_pair(lap, lap_term(ph, c, a.L.sp, a.id2p[2]));
+            float s, e;
+            two_sum(b.hi, -lap.hi, s, e);
+            x = (T)(s + (e + (b.lo - lap.lo)));
           }
         } else {
           x = inR[(long long)(line0 + l) * a.in_line + (long long)i * a.in_pos + (long long)outer * a.in_outer];
@@ -794,10 +810,11 @@ __global__ void __launch_bounds__(256) k_correct(Layout L, const StepScalars* __
 
 // Mean removal over the interior (poisson.f90:491-503, 1159-1171): every CTA sums the
 // per-line partials in the same order, then subtracts mean/float(nx*ny*nz).
-template <typename T, int DIM>
-__global__ void __launch_bounds__(256) k_mean_subtract(Layout L, const double* partial, int npart, double ncell_f,
-                                                       StepScalars* sc, T* phi) {
-  __shared__ double red[256];
+// Mean of phi from the per-CTA partial sums of the inverse transform (one CTA; the result
+// goes to sc->mean for k_mean_subtract and the host).
+static __global__ void __launch_bounds__(1024) k_mean_reduce(const double* __restrict__ partial, int npart, double ncell_f,
+                                                      StepScalars* sc) {
+  __shared__ double red[1024];
   double s = 0.0;
   for (int q = threadIdx.x; q < npart; q += blockDim.x) s += partial[q];
   red[threadIdx.x] = s;
@@ -806,9 +823,12 @@ __global__ void __launch_bounds__(256) k_mean_subtract(Layout L, const double* p
     if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
     __syncthreads();
   }
-  const double m = red[0] / ncell_f;
-  if (blockIdx.x == 0 && threadIdx.x == 0) sc->mean = m;
-  const T mt = (T)m;
+  if (threadIdx.x == 0) sc->mean = red[0] / ncell_f;
+}
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(256) k_mean_subtract(Layout L, const StepScalars* __restrict__ sc, T* phi) {
+  const T mt = (T)sc->mean;
   const long long ncell = (long long)L.n0 * L.n1 * L.n2;
   CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
   for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {

@@ -357,21 +357,12 @@ __global__ void __launch_bounds__(256) k_checks_df(Layout L, CheckDFArgs a) {
 }
 
 // ------------------------------------------------------------------------------------
-// Iterative refinement residual: r = b - L_h phi, b = div(v*) rho/dt, in double-float
-// arithmetic.  L_h is the 3/5/7-point Laplacian the fast solver inverts exactly (periodic
-// axes by their modified wavenumbers, wall axes by the Neumann/Dirichlet tridiagonal),
-// applied with phi's ghost cells filled by its boundary rules.
+// Iterative refinement residual r = b - L_h phi, b = div(v*) rho/dt, in double-float
+// arithmetic (formed in the first transform's load, LD_RESID).  L_h is the 3/5/7-point
+// Laplacian the fast solver inverts exactly (periodic axes by their modified wavenumbers,
+// wall axes by the Neumann/Dirichlet tridiagonal), applied with phi's ghost cells filled by
+// its boundary rules.  One axis' term (f[c+s] - 2 f[c] + f[c-s]) / delta^2:
 // ------------------------------------------------------------------------------------
-struct ResidualArgs {
-  DFField u, v, w;
-  const float *du, *dv, *dw;
-  const float *dul, *dvl, *dwl;
-  const float* phi;
-  float* r;
-  F2 idp[3];
-  F2 id2p[3];
-};
-
 __device__ __forceinline__ F2 lap_term(const float* f, long long c, long long s, F2 id2) {
   float a, ea, b, eb;
   two_sum(f[c + s], -f[c], a, ea);
@@ -379,24 +370,6 @@ __device__ __forceinline__ F2 lap_term(const float* f, long long c, long long s,
   float d, ed;
   two_sum(a, -b, d, ed);
   return mul_pair(d, ed + (ea - eb), id2);
-}
-
-template <int DIM>
-__global__ void __launch_bounds__(256) k_residual_df(Layout L, const StepScalars* __restrict__ sc, ResidualArgs a) {
-  const long long ncell = (long long)L.n0 * L.n1 * L.n2;
-  const F2 rod = split_d(sc->rho_over_dt);
-  CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
-  for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
-    const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
-    const long long c = L.idx(i, j, kst<DIM>(k));
-    const F2 dv = div_df<DIM>(L, a.u, a.v, a.w, a.du, a.dv, a.dw, a.dul, a.dvl, a.dwl, a.idp, i, j, k);
-    const F2 b = mul_pair(dv.hi, dv.lo, rod);
-    F2 lap = add_pair(lap_term(a.phi, c, 1, a.id2p[0]), lap_term(a.phi, c, L.sx, a.id2p[1]));
-    if (DIM == 3) lap = add_pair(lap, lap_term(a.phi, c, L.sp, a.id2p[2]));
-    float s, e;
-    two_sum(b.hi, -lap.hi, s, e);
-    a.r[c] = s + (e + (b.lo - lap.lo));
-  }
 }
 
 // ------------------------------------------------------------------------------------

@@ -192,7 +192,8 @@ extern "C" int fen_poisson_pp2d_noalloc(const double* rhs, double* phi, int nx, 
   // subtract the mean (:491-503)
   const int npart = (int)(gx.x * gx.y);
   const int gm = std::min(cdiv((long long)nx * ny, 256), 152 * 8);
-  k_mean_subtract<double, 2><<<gm, 256, 0, st>>>(L, part, npart, (double)(float)((long long)nx * ny), sc, phi);
+  k_mean_reduce<<<1, 1024, 0, st>>>(part, npart, (double)(float)((long long)nx * ny), sc);
+  k_mean_subtract<double, 2><<<gm, 256, 0, st>>>(L, sc, phi);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fen_internal_fail(FEN_ERR_CUDA, (std::string("fen_poisson_pp2d_noalloc: ") + cudaGetErrorString(e)).c_str());
