@@ -854,8 +854,8 @@ int launch_checks(fen_ctx* c, int want_div) {
   a.iso = c->iso;
   a.want_div = want_div;
   a.pdiv = c->pdiv; a.pvel = c->pvel; a.nan_flag = c->nan_flag;
-  if (c->dim == 3) k_checks<double, 3><<<c->nred, 256, 0, c->stream>>>(c->L, a);
-  else k_checks<double, 2><<<c->nred, 256, 0, c->stream>>>(c->L, a);
+  if (c->dim == 3) k_checks<3><<<c->nred, 256, 0, c->stream>>>(c->L, a);
+  else k_checks<2><<<c->nred, 256, 0, c->stream>>>(c->L, a);
   c->launches++;
   CK(cudaGetLastError());
   k_finalize<<<1, 256, 0, c->stream>>>(c->pdiv, c->pvel, c->nred, c->sc, c->dmin, 0.0, 1, c->nan_flag);

@@ -793,17 +793,18 @@ __global__ void __launch_bounds__(256) k_correct(Layout L, const StepScalars* __
   const long long ncell = (long long)L.n0 * L.n1 * L.n2;
   const T dt = (T)(a.use_dev_dt ? sc->dt : a.dt_host);
   const T f = a.rhof_one ? dt : (T)((double)dt / a.rhof);
-  const T idx = (T)a.id[0];
-  const T idy = a.iso ? idx : (T)a.id[1];
-  const T idz = a.iso ? idx : (T)a.id[2];
+  // v = v* - dt/rho (phi(+1) - phi) / delta as one FMA per component with g = dt/(rho delta)
+  const T gx = -(T)a.id[0] * f;
+  const T gy = a.iso ? gx : -(T)a.id[1] * f;
+  const T gz = a.iso ? gx : -(T)a.id[2] * f;
   CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
   for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
     const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
     const T ph = a.phi[c];
-    a.u[c] = a.us[c] - (a.phi[c + 1] - ph) * idx * f;
-    a.v[c] = a.vs[c] - (a.phi[c + L.sx] - ph) * idy * f;
-    if (DIM == 3) a.w[c] = a.ws[c] - (a.phi[c + L.sp] - ph) * idz * f;
+    a.u[c] = fmx(a.phi[c + 1] - ph, gx, a.us[c]);
+    a.v[c] = fmx(a.phi[c + L.sx] - ph, gy, a.vs[c]);
+    if (DIM == 3) a.w[c] = fmx(a.phi[c + L.sp] - ph, gz, a.ws[c]);
     a.p[c] = a.p[c] + ph;
   }
 }
@@ -852,46 +853,53 @@ struct CheckArgs {
   int* nan_flag;
 };
 
-template <typename T, int DIM>
-__global__ void __launch_bounds__(256) k_checks(Layout L, CheckArgs<T> a) {
+// Order-preserving int64 key of a double's bits: key(x) < key(y) iff x < y for non-NaN x, y,
+// and the map is its own inverse.  The diagnostics take their maxima on the integer pipe
+// (GB300's FP64 pipe is narrow); NaNs are detected from the bits and left out of the maxima.
+__device__ __forceinline__ long long okey(long long b) { return b ^ ((b >> 63) & 0x7fffffffffffffffLL); }
+__device__ __forceinline__ bool nan_bits(long long b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+
+template <int DIM>
+__global__ void __launch_bounds__(256) k_checks(Layout L, CheckArgs<double> a) {
   const long long ncell = (long long)L.n0 * L.n1 * L.n2;
-  T md = -INFINITY, mv = 0;
+  const long long kneg = okey(__double_as_longlong(-INFINITY));
+  long long md = kneg, mv = 0;  // keys of -inf and +0
   bool bad = false;
-  const T idx = (T)a.id[0];
+  const double idx = a.id[0];
+  const double idy = a.iso ? idx : a.id[1], idz = a.iso ? idx : a.id[2];
   CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
   for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
     const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
     const long long c = L.idx(i, j, kst<DIM>(k));
-    const T uc = a.u[c], vc = a.v[c];
-    T vel = fabs(uc) + fabs(vc);
-    T d = 0;
-    if (a.want_div) {
-      if (a.iso) d = (uc - a.u[c - 1]) * idx + (vc - a.v[c - L.sx]) * idx;
-      else d = (uc - a.u[c - 1]) * (T)a.id[0] + (vc - a.v[c - L.sx]) * (T)a.id[1];
-    }
+    const double uc = a.u[c], vc = a.v[c];
+    double vel = fabs(uc) + fabs(vc);
+    double d = 0;
+    if (a.want_div) d = fma(vc - a.v[c - L.sx], idy, (uc - a.u[c - 1]) * idx);
     if (DIM == 3) {
-      const T wc = a.w[c];
+      const double wc = a.w[c];
       vel = vel + fabs(wc);
-      if (a.want_div) d = d + (wc - a.w[c - L.sp]) * (a.iso ? idx : (T)a.id[2]);
+      if (a.want_div) d = fma(wc - a.w[c - L.sp], idz, d);
     }
-    if (vel != vel || d != d) bad = true;
-    if (vel > mv) mv = vel;
-    if (d > md) md = d;
+    const long long bv = __double_as_longlong(vel), bd = __double_as_longlong(d);
+    const bool nv = nan_bits(bv), nd = nan_bits(bd);
+    bad |= nv | nd;
+    mv = max(mv, nv ? 0LL : bv);  // vel >= +0: its bits are its key
+    md = max(md, nd ? kneg : okey(bd));
   }
-  __shared__ double r1[256], r2[256];
-  r1[threadIdx.x] = (double)md;
-  r2[threadIdx.x] = (double)mv;
+  __shared__ long long r1[256], r2[256];
+  r1[threadIdx.x] = md;
+  r2[threadIdx.x] = mv;
   __syncthreads();
   for (int h = blockDim.x / 2; h > 0; h >>= 1) {
     if (threadIdx.x < h) {
-      r1[threadIdx.x] = fmax(r1[threadIdx.x], r1[threadIdx.x + h]);
-      r2[threadIdx.x] = fmax(r2[threadIdx.x], r2[threadIdx.x + h]);
+      r1[threadIdx.x] = max(r1[threadIdx.x], r1[threadIdx.x + h]);
+      r2[threadIdx.x] = max(r2[threadIdx.x], r2[threadIdx.x + h]);
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    a.pdiv[blockIdx.x] = r1[0];
-    a.pvel[blockIdx.x] = r2[0];
+    a.pdiv[blockIdx.x] = __longlong_as_double(okey(r1[0]));
+    a.pvel[blockIdx.x] = __longlong_as_double(r2[0]);
   }
   if (bad) atomicOr(a.nan_flag, 1);
 }
