@@ -637,15 +637,19 @@ int launch_thomas(fen_ctx* c, const Stage& s) {
   const bool real = (c->solver == S_NN || c->solver == S_NNN);
   ThomasArgs ta = s.ta;
   ta.split2 = 0;
+  // 64-thread CTAs: a sweep is a latency-bound recurrence, so the systems are spread over as
+  // many SMs as possible
+  constexpr int kTh = 64;
   if (real) {
-    if (c->mixed) k_thomas<float, double><<<s.tgrid, 128, 0, c->stream>>>(ta);
-    else k_thomas<double, double><<<s.tgrid, 128, 0, c->stream>>>(ta);
+    const dim3 g(cdiv(ta.ncol, kTh), s.tgrid.y, s.tgrid.z);
+    if (c->mixed) k_thomas<float, double><<<g, kTh, 0, c->stream>>>(ta);
+    else k_thomas<double, double><<<g, kTh, 0, c->stream>>>(ta);
   } else {
     // complex right-hand sides: real and imaginary parts as two real systems per column
     ta.split2 = 1;
-    const dim3 g(cdiv(2LL * ta.ncol, 128), s.tgrid.y, s.tgrid.z);
-    if (c->mixed) k_thomas<float, double><<<g, 128, 0, c->stream>>>(ta);
-    else k_thomas<double, double><<<g, 128, 0, c->stream>>>(ta);
+    const dim3 g(cdiv(2LL * ta.ncol, kTh), s.tgrid.y, s.tgrid.z);
+    if (c->mixed) k_thomas<float, double><<<g, kTh, 0, c->stream>>>(ta);
+    else k_thomas<double, double><<<g, kTh, 0, c->stream>>>(ta);
   }
   c->launches++;
   CK(cudaGetLastError());
@@ -789,8 +793,12 @@ int launch_predictor(fen_ctx* c, const StepScalars* sc) {
     pa.irho = split_d(1.0 / rhof);
     pa.iso = c->iso;
     pa.has_S = c->has_S;
-    if (c->dim == 3) k_predictor_df<3><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
-    else k_predictor_df<2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+    if (c->dim == 3) {
+      const dim3 tg(cdiv(c->n[0], kDTX), cdiv(c->n[1], kDTY), cdiv(c->n[2], kDTZ));
+      k_predictor_df_tile<<<tg, dim3(kDTX, kDTY), 0, c->stream>>>(c->L, sc, pa);
+    } else {
+      k_predictor_df<2><<<grid, 256, 0, c->stream>>>(c->L, sc, pa);
+    }
   } else if (var_path(c)) {
     VarArgs va;
     memset(&va, 0, sizeof(va));

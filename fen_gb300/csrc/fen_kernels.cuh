@@ -328,6 +328,8 @@ __device__ __forceinline__ void row_jk(int line, int outer, int& j, int& k) { j 
 
 template <typename T, int DIM>
 __device__ __forceinline__ T div_at(const LineArgs<T>& a, int i, int j, int k) {
+  // (u_i - u_{i-1}) / dx + (v_j - v_{j-1}) / dy + (w_k - w_{k-1}) / dz in FEN's operation
+  // order (the Poisson right-hand side sets the pressure's rounding level)
   const Layout& L = a.L;
   const long long c = L.idx(i, j, kst<DIM>(k));
   const T* U = a.fu; const T* V = a.fv; const T* W = a.fw;
@@ -620,17 +622,21 @@ template <> struct ThomasOps<double2> {
 // solve (FP32 storage, FP64 elimination) widens and narrows by rewriting the IEEE fields:
 // exact widening, round-to-nearest-even narrowing.  Zero, subnormal, infinite and NaN
 // values (and results outside the normal FP32 range) take the hardware conversion.
+// The rare cases go through calls that cannot be inlined: a plain conversion there would be
+// if-converted into a select and then execute on the FP64 pipe for every element.
+static __device__ __noinline__ double widen_rare(float f) { return (double)f; }
+static __device__ __noinline__ float narrow_rare(double d) { return (float)d; }
 __device__ __forceinline__ double widen(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned ex = u & 0x7F800000u;
-  if (ex == 0u || ex == 0x7F800000u) return (double)f;
+  if (ex == 0u || ex == 0x7F800000u) return widen_rare(f);
   const unsigned hi = (u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + 0x38000000u);
   return __hiloint2double((int)hi, (int)(u << 29));
 }
 __device__ __forceinline__ float narrow(double d) {
   const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
   const unsigned e = (hi >> 20) & 0x7FFu;
-  if (e < 897u || e > 1150u) return (float)d;  // FP32 exponent 1..254 only
+  if (e < 897u || e > 1150u) return narrow_rare(d);  // FP32 exponent 1..254 only
   unsigned f = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
   const unsigned rem = lo & 0x1FFFFFFFu;
   if (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) f += 1u;  // carries into the exponent

@@ -222,6 +222,140 @@ __global__ void __launch_bounds__(256) k_predictor_df(Layout L, const StepScalar
   }
 }
 
+// ------------------------------------------------------------------------------------
+// Tiled double-float predictor (3D): the face and edge products are formed once per face
+// and shared (the - values from the left lane by shuffle, from the row below through shared
+// memory and from the previous k in registers), as in the FP64 k_predictor_tile.  Each sum
+// is formed upper + lower, so the sharing cell and the per-cell formula see the same pairs.
+// ------------------------------------------------------------------------------------
+constexpr int kDTX = 32, kDTY = 8, kDTZ = 16;
+
+// Products on the + sides of cell c: fuu (i+1/2), fvv (j+1/2), fww (k+1/2), euv (i+1/2, j+1/2),
+// euw (i+1/2, k+1/2), evw (j+1/2, k+1/2) (the 1/4 is folded into q).
+__device__ __forceinline__ void dflux6(const DFField& U, const DFField& V, const DFField& W, long long c, long long sy,
+                                       long long sz, DF& fuu, DF& fvv, DF& fww, DF& euv, DF& euw, DF& evw) {
+  const DF uc = dfv(U, c), vc = dfv(V, c), wc = dfv(W, c);
+  fuu = dsq(dadd(dfv(U, c + 1), uc));
+  fvv = dsq(dadd(dfv(V, c + sy), vc));
+  fww = dsq(dadd(dfv(W, c + sz), wc));
+  euv = dmul(dadd(dfv(U, c + sy), uc), dadd(dfv(V, c + 1), vc));
+  euw = dmul(dadd(dfv(U, c + sz), uc), dadd(dfv(W, c + 1), wc));
+  evw = dmul(dadd(dfv(V, c + sz), vc), dadd(dfv(W, c + sy), wc));
+}
+// The three products a cell's +x neighbour needs (fuu, euv, euw of cell c).
+__device__ __forceinline__ void dflux_x(const DFField& U, const DFField& V, const DFField& W, long long c, long long sy,
+                                        long long sz, DF& fuu, DF& euv, DF& euw) {
+  const DF uc = dfv(U, c);
+  fuu = dsq(dadd(dfv(U, c + 1), uc));
+  euv = dmul(dadd(dfv(U, c + sy), uc), dadd(dfv(V, c + 1), dfv(V, c)));
+  euw = dmul(dadd(dfv(U, c + sz), uc), dadd(dfv(W, c + 1), dfv(W, c)));
+}
+// ... its +y neighbour needs (euv, fvv, evw of cell c).
+__device__ __forceinline__ void dflux_y(const DFField& U, const DFField& V, const DFField& W, long long c, long long sy,
+                                        long long sz, DF& euv, DF& fvv, DF& evw) {
+  const DF vc = dfv(V, c);
+  fvv = dsq(dadd(dfv(V, c + sy), vc));
+  euv = dmul(dadd(dfv(U, c + sy), dfv(U, c)), dadd(dfv(V, c + 1), vc));
+  evw = dmul(dadd(dfv(V, c + sz), vc), dadd(dfv(W, c + sy), dfv(W, c)));
+}
+// ... its +z neighbour needs (euw, evw, fww of cell c).
+__device__ __forceinline__ void dflux_z(const DFField& U, const DFField& V, const DFField& W, long long c, long long sy,
+                                        long long sz, DF& euw, DF& evw, DF& fww) {
+  const DF wc = dfv(W, c);
+  fww = dsq(dadd(dfv(W, c + sz), wc));
+  euw = dmul(dadd(dfv(U, c + sz), dfv(U, c)), dadd(dfv(W, c + 1), wc));
+  evw = dmul(dadd(dfv(V, c + sz), dfv(V, c)), dadd(dfv(W, c + sy), wc));
+}
+__device__ __forceinline__ DF shfl_up_df(DF v) {
+  return DF{__shfl_up_sync(0xffffffffu, v.h, 1), __shfl_up_sync(0xffffffffu, v.l, 1)};
+}
+
+static __global__ void __launch_bounds__(kDTX * kDTY) k_predictor_df_tile(Layout L, const StepScalars* __restrict__ sc,
+                                                                        PredDFArgs a) {
+  __shared__ DF sh[2][3][kDTY][kDTX];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = 1 + blockIdx.x * kDTX + tx, j0 = 1 + blockIdx.y * kDTY + ty;
+  const bool act = (i0 <= L.n0) && (j0 <= L.n1);
+  const int i = min(i0, L.n0), j = min(j0, L.n1);
+  const int k0 = 1 + blockIdx.z * kDTZ, k1 = min(L.n2, k0 + kDTZ - 1);
+  const DF A = DF{sc->Ap[0], sc->Ap[1]}, B = DF{sc->Bp[0], sc->Bp[1]}, DT = DF{sc->dtp[0], sc->dtp[1]};
+  const DF qx = DF{a.qx.hi, a.qx.lo}, qy = DF{a.qy.hi, a.qy.lo}, qz = DF{a.qz.hi, a.qz.lo};
+  const DF mx = DF{a.mx.hi, a.mx.lo}, my = DF{a.my.hi, a.my.lo}, mz = DF{a.mz.hi, a.mz.lo};
+  const long long sy = L.sx, sz = L.sp;
+  const DFField U = a.u, V = a.v, W = a.w, P = a.p;
+  // z-minus products of the first k of the chunk
+  DF puw, pvw, pww;
+  dflux_z(U, V, W, L.idx(i, j, k0) - sz, sy, sz, puw, pvw, pww);
+  int buf = 0;
+  for (int k = k0; k <= k1; ++k, buf ^= 1) {
+    const long long c = L.idx(i, j, k);
+    DF fuu, fvv, fww, euv, euw, evw;
+    dflux6(U, V, W, c, sy, sz, fuu, fvv, fww, euv, euw, evw);
+    // x-minus: the lane to the left; lane 0 forms its own
+    DF xuu = shfl_up_df(fuu), xuv = shfl_up_df(euv), xuw = shfl_up_df(euw);
+    if (tx == 0) dflux_x(U, V, W, c - 1, sy, sz, xuu, xuv, xuw);
+    // y-minus: the row below through shared memory; row 0 forms its own
+    sh[buf][0][ty][tx] = euv;
+    sh[buf][1][ty][tx] = fvv;
+    sh[buf][2][ty][tx] = evw;
+    __syncthreads();
+    DF yuv, yvv, yvw;
+    if (ty > 0) {
+      yuv = sh[buf][0][ty - 1][tx];
+      yvv = sh[buf][1][ty - 1][tx];
+      yvw = sh[buf][2][ty - 1][tx];
+    } else {
+      dflux_y(U, V, W, c - sy, sy, sz, yuv, yvv, yvw);
+    }
+    DF ax = dmul(dsub(fuu, xuu), qx);
+    ax = dadd(ax, dmul(dsub(euv, yuv), qy));
+    ax = dadd(ax, dmul(dsub(euw, puw), qz));
+    DF ay = dmul(dsub(euv, xuv), qx);
+    ay = dadd(ay, dmul(dsub(fvv, yvv), qy));
+    ay = dadd(ay, dmul(dsub(evw, pvw), qz));
+    DF az = dmul(dsub(euw, xuw), qx);
+    az = dadd(az, dmul(dsub(evw, yvw), qy));
+    az = dadd(az, dmul(dsub(fww, pww), qz));
+    puw = euw;
+    pvw = evw;
+    pww = fww;
+    if (act) {
+      const DF uc = dfv(U, c), vc = dfv(V, c), wc = dfv(W, c);
+      DF lu = dmul(d2(dfv(U, c + 1), uc, dfv(U, c - 1)), mx);
+      lu = dadd(lu, dmul(d2(dfv(U, c + sy), uc, dfv(U, c - sy)), my));
+      lu = dadd(lu, dmul(d2(dfv(U, c + sz), uc, dfv(U, c - sz)), mz));
+      DF lv = dmul(d2(dfv(V, c + 1), vc, dfv(V, c - 1)), mx);
+      lv = dadd(lv, dmul(d2(dfv(V, c + sy), vc, dfv(V, c - sy)), my));
+      lv = dadd(lv, dmul(d2(dfv(V, c + sz), vc, dfv(V, c - sz)), mz));
+      DF lw = dmul(d2(dfv(W, c + 1), wc, dfv(W, c - 1)), mx);
+      lw = dadd(lw, dmul(d2(dfv(W, c + sy), wc, dfv(W, c - sy)), my));
+      lw = dadd(lw, dmul(d2(dfv(W, c + sz), wc, dfv(W, c - sz)), mz));
+      DF dx = dsub(lu, ax), dy = dsub(lv, ay), dz = dsub(lw, az);
+      if (a.has_S) {
+        const DF ir = DF{a.irho.hi, a.irho.lo};
+        dx = dadd(dx, dmul(DF{a.Sx[c], 0.f}, ir));
+        dy = dadd(dy, dmul(DF{a.Sy[c], 0.f}, ir));
+        dz = dadd(dz, dmul(DF{a.Sz[c], 0.f}, ir));
+      }
+      // AB2 with the pressure gradient (fields.f90:55-58, navier_stokes.f90:169-198)
+      const DF pc = dfv(P, c);
+      DF rx = dsub(DF{a.g[0].hi, a.g[0].lo}, dmul(dsub(dfv(P, c + 1), pc), DF{a.gx.hi, a.gx.lo}));
+      DF ry = dsub(DF{a.g[1].hi, a.g[1].lo}, dmul(dsub(dfv(P, c + sy), pc), DF{a.gy.hi, a.gy.lo}));
+      DF rz = dsub(DF{a.g[2].hi, a.g[2].lo}, dmul(dsub(dfv(P, c + sz), pc), DF{a.gz.hi, a.gz.lo}));
+      rx = dadd(rx, dadd(dmul(A, dx), dmul(B, DF{a.dox[c], a.doxl[c]})));
+      ry = dadd(ry, dadd(dmul(A, dy), dmul(B, DF{a.doy[c], a.doyl[c]})));
+      rz = dadd(rz, dadd(dmul(A, dz), dmul(B, DF{a.doz[c], a.dozl[c]})));
+      const DF ix = dmul(DT, rx), iy = dmul(DT, ry), iz = dmul(DT, rz);
+      a.du[c] = ix.h; a.dul[c] = ix.l;
+      a.dv[c] = iy.h; a.dvl[c] = iy.l;
+      a.dw[c] = iz.h; a.dwl[c] = iz.l;
+      a.dox[c] = dx.h; a.doxl[c] = dx.l;
+      a.doy[c] = dy.h; a.doyl[c] = dy.l;
+      a.doz[c] = dz.h; a.dozl[c] = dz.l;
+    }
+  }
+}
+
 // One axis term of div(v*) as a pair: ((vA - vB) + (dA - dB)) * id with v* = v + d, both
 // differences taken error-free on the pairs (d may be null: div(v)).
 __device__ __forceinline__ F2 div_term(const DFField& V, const float* d, const float* dl, long long ca, long long cb,
