@@ -529,7 +529,7 @@ def main():
     for step in range(1, args.steps + 1):
         dt2 = s.advance_solution(step, dt2)
     for k in keys:
-        outb[k].numpy()[...] = s.get_field(fid[k])
+        s.get_field(fid[k], out=outb[k].numpy())
     s.sync()
     el = time.perf_counter() - t0
     if dist:

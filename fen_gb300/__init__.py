@@ -234,8 +234,15 @@ class Solver:
             raise ValueError(f"field shape {a.shape} != {self.grid.shape}")
         self._check(self._L.fen_upload(self._h, fid, _dp(a)))
 
-    def get_field(self, fid):
-        a = self.zeros()
+    def get_field(self, fid, out=None):
+        """Download field `fid`; into `out` (a C-contiguous float64 array of the grid's shape,
+        e.g. a pinned host buffer) when given, else into a new array."""
+        if out is None:
+            a = self.zeros()
+        else:
+            a = out
+            if a.shape != self.grid.shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"out must be a C-contiguous float64 array of shape {self.grid.shape}")
         self._check(self._L.fen_download(self._h, fid, _dp(a)))
         return a
 
