@@ -637,9 +637,7 @@ int launch_thomas(fen_ctx* c, const Stage& s) {
   const bool real = (c->solver == S_NN || c->solver == S_NNN);
   ThomasArgs ta = s.ta;
   ta.split2 = 0;
-  // 64-thread CTAs: a sweep is a latency-bound recurrence, so the systems are spread over as
-  // many SMs as possible
-  constexpr int kTh = 64;
+  constexpr int kTh = 128;  // (64-thread CTAs measured no faster)
   if (real) {
     const dim3 g(cdiv(ta.ncol, kTh), s.tgrid.y, s.tgrid.z);
     if (c->mixed) k_thomas<float, double><<<g, kTh, 0, c->stream>>>(ta);
