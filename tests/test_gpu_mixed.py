@@ -101,6 +101,49 @@ def test_mixed_channel_matches_fp64(fen_lib):
     assert e[F.P] < 1e-5, e
 
 
+def test_mixed_partial_tiles_match_fp64(fen_lib):
+    # 3D sizes that leave partial predictor tiles in x (48 = 32 + 16), y (12 = 8 + 4) and z
+    # (18 = 16 + 2 planes per walk), anisotropic spacing; start: a few seeded Fourier modes
+    n = (48, 12, 18)
+    L = (3.0, 1.25, 0.75)
+    rng = np.random.Generator(np.random.PCG64(8))
+    shape = (n[2] + 2, n[1] + 2, n[0] + 2)
+    x = [(np.arange(n[q]) + 0.5) * L[q] / n[q] for q in range(3)]
+    Z, Y, X = np.meshgrid(x[2], x[1], x[0], indexing="ij")
+    init = {}
+    for fid in (F.U, F.V, F.W):
+        a = np.zeros(shape)
+        for _ in range(4):
+            k = rng.integers(1, 3, size=3)
+            ph = rng.uniform(0, 2 * np.pi, size=3)
+            a[1:-1, 1:-1, 1:-1] += rng.uniform(-1, 1) * (np.sin(2 * np.pi * k[0] * X / L[0] + ph[0])
+                                                        * np.sin(2 * np.pi * k[1] * Y / L[1] + ph[1])
+                                                        * np.sin(2 * np.pi * k[2] * Z / L[2] + ph[2]))
+        init[fid] = a
+    s64, s32 = _run_pair(3, n, L, ["Periodic"] * 6, init, 50, viscosity=0.02, CFL=0.4, constant_CFL=True,
+                         aniso=True)
+    e = _errors(s64, s32, 3)
+    for fid in (F.U, F.V, F.W):
+        assert e[fid] < 1e-6, e
+    assert e[F.P] < 1e-5, e
+
+
+def test_mixed_2d_and_refinement(fen_lib):
+    # 2D TGV: the mixed form with one refinement solve stays within 1e-6 of FP64; without it
+    # (refine=0) the FP32 Poisson error is left in the state and the error is larger
+    N, L = 64, 2 * np.pi
+    u, v, p = C.tgv2d_fields(N, L)
+    init = {F.U: u, F.V: v, F.P: p}
+    errs = []
+    for refine in (1, 0):
+        s64, s32 = _run_pair(2, (N, N, 1), (L, L, L / N), ["Periodic"] * 4, init, 200, viscosity=0.01,
+                             refine=refine)
+        errs.append(_errors(s64, s32, 2))
+    for fid in (F.U, F.V):
+        assert errs[0][fid] < 1e-6, errs
+        assert errs[1][fid] > errs[0][fid], errs
+
+
 def test_mixed_ghost_pairs_keep_fp64_values(fen_lib):
     # pairs carry ~48 bits: an FP64 upload, ghost fill and download round-trip to ~1e-14
     n = (12, 8, 6)
