@@ -49,7 +49,10 @@ int fen_internal_fail(int code, const char* msg);
 namespace fen {
 namespace ens {
 
-constexpr int kCl = 8;                 // CTAs per cluster
+#ifndef FEN_ENS_CLUSTER
+#define FEN_ENS_CLUSTER 8
+#endif
+constexpr int kCl = FEN_ENS_CLUSTER;   // CTAs per cluster (above 8: non-portable cluster size)
 constexpr size_t kSmemLimit = 232448;  // opt-in dynamic shared memory per CTA (227 KB)
 constexpr size_t kSmemReserve = 1024;  // static shared memory of the kernel + slack
 
@@ -1045,7 +1048,7 @@ bool plan_len(int M, FFTPlan& P) {
 }
 
 bool g_feasible(int N, int G) {
-  if (G != 1 && G != 2 && G != 4 && G != 8) return false;
+  if (G < 1 || G > kCl || (G & (G - 1)) != 0) return false;
   if (N % G != 0 || N / G < 2) return false;
   return smem_bytes(N, G) + kSmemReserve <= kSmemLimit;
 }
@@ -1146,8 +1149,10 @@ int build_packs(fen_ensemble* e, const std::vector<int>& subset) {
   e->npacks = (int)packs.size();
   e->smem = smem;
   const void* k = kernel_ptr(e->threads);
-  for (int m = 0; m < 3; ++m)
+  for (int m = 0; m < 3; ++m) {
     EK(cudaFuncSetAttribute(kernel_ptr(e->threads, m), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1)));
+    if (kCl > 8) EK(cudaFuncSetAttribute(kernel_ptr(e->threads, m), cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  }
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1161,7 +1166,9 @@ int build_packs(fen_ensemble* e, const std::vector<int>& subset) {
   cfg.numAttrs = 1;
   int nc = 0;
   EK(cudaOccupancyMaxActiveClusters(&nc, k, &cfg));
-  if (nc < 1) return fen_internal_fail(FEN_ERR_CUDA, "no cluster of 8 CTAs fits this device with the ensemble's shared memory");
+  if (nc < 1)
+    return fen_internal_fail(FEN_ERR_CUDA, ("no cluster of " + std::to_string(kCl) +
+                                            " CTAs fits this device with the ensemble's shared memory").c_str());
   e->nclusters = nc;
   if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
   if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
@@ -1287,7 +1294,7 @@ int fen_ensemble_create(int nruns, const int* n, const double* viscosity, double
                                ("ensemble run " + std::to_string(q) + ": N must be 2^a 3^b with a >= 2, b <= 1, N >= 8").c_str());
     if (!(viscosity[q] > 0)) return fen_internal_fail(FEN_ERR_ARG, "viscosity must be positive");
     bool ok = false;
-    for (int G = 1; G <= 8; G *= 2) ok = ok || g_feasible(n[q], G);
+    for (int G = 1; G <= kCl; G *= 2) ok = ok || g_feasible(n[q], G);
     if (!ok) return fen_internal_fail(FEN_ERR_ARG, ("ensemble run " + std::to_string(q) + ": N = " + std::to_string(n[q]) +
                                                     " does not fit a cluster's shared memory").c_str());
   }
