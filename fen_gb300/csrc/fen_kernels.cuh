@@ -522,7 +522,12 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
       }
     }
   } else if (OP == OP_C2R || OP == OP_DCT3) {
+    // line sums for the mean removal: FP64 in the FP64 path; in FP32 kernels a compensated
+    // pair per thread (two-sum on the FP32 pipe, the per-thread error far below FP64's),
+    // converted once and reduced across the CTA in FP64
+    const bool want_sum = (ST == ST_FIELD) && a.partial != nullptr;
     double lsum = 0.0;
+    float lsh = 0.f, lsl = 0.f;
     const int work = nl * n;
     for (int t = tid; t < work; t += nth) {
       int l, i;
@@ -537,13 +542,23 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
           int j, k;
           row_jk<DIM>(line0 + l, outer, j, k);
           a.fdst[a.L.idx(i + 1, j, kst<DIM>(k))] = x;
-          lsum += (double)x;
+          if (want_sum) {
+            if constexpr (sizeof(T) == 8) {
+              lsum += x;
+            } else {
+              float s, e;
+              two_sum(lsh, (float)x, s, e);
+              lsh = s;
+              lsl += e;
+            }
+          }
         } else {
           outR[(long long)(line0 + l) * a.out_line + (long long)i * a.out_pos + (long long)outer * a.out_outer] = x;
         }
       }
     }
-    if (ST == ST_FIELD && a.partial) {
+    if (want_sum) {
+      if constexpr (sizeof(T) == 4) lsum = (double)lsh + (double)lsl;
       // deterministic CTA sum (fixed tree order)
       __shared__ double red[256];
       red[tid] = lsum;
