@@ -107,6 +107,7 @@ struct fen_ctx {
   float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr, *p32 = nullptr, *phi32 = nullptr;
   float *u32l = nullptr, *v32l = nullptr, *w32l = nullptr, *p32l = nullptr;
   float* dphi32 = nullptr;  // refinement: correction of phi
+  float *dv32h = nullptr, *dv32l = nullptr;  // refinement: pair divergence of v* from the first transform
   int refine = 0;
   float* d32[3] = {nullptr, nullptr, nullptr};
   float* dvo32[3] = {nullptr, nullptr, nullptr};
@@ -610,11 +611,10 @@ int launch_stage_t(fen_ctx* c, const Stage& s, int first_from_field, const void*
   int ld = s.ld;
   if (first_from_field == kFirstResidual) {
     // mixed refinement: the first transform forms its own right-hand side from v* and phi
+    if (!c->dv32h) return fail(FEN_ERR_STATE, "refinement without its divergence buffer");
     ld = LD_RESID;
     a.fsrc = (const T*)field_src;
-    a.fu = (const T*)c->d32[0]; a.fv = (const T*)c->d32[1]; a.fw = (const T*)c->d32[2];
-    a.ful = c->d32l[0]; a.fvl = c->d32l[1]; a.fwl = c->d32l[2];
-    a.pu = DFField{c->u32, c->u32l}; a.pv = DFField{c->v32, c->v32l}; a.pw = DFField{c->w32, c->w32l};
+    a.dvh = c->dv32h; a.dvl = c->dv32l;
     for (int q = 0; q < 3; ++q) a.id2p[q] = split_d(1.0 / (c->d[q] * c->d[q]));
   } else if (first_from_field) {
     ld = LD_FIELD;
@@ -625,6 +625,7 @@ int launch_stage_t(fen_ctx* c, const Stage& s, int first_from_field, const void*
       a.fu = (const T*)c->d32[0]; a.fv = (const T*)c->d32[1]; a.fw = (const T*)c->d32[2];
       a.ful = c->d32l[0]; a.fvl = c->d32l[1]; a.fwl = c->d32l[2];
       a.pu = DFField{c->u32, c->u32l}; a.pv = DFField{c->v32, c->v32l}; a.pw = DFField{c->w32, c->w32l};
+      if (c->refine) { a.dvh = c->dv32h; a.dvl = c->dv32l; }
     } else {
       a.fu = (const T*)c->us; a.fv = (const T*)c->vs; a.fw = (const T*)c->ws;
       if (c->var_rho && !c->split) a.rho_c = c->rho;
@@ -1148,7 +1149,7 @@ int fen_ctx_destroy(fen_ctx* c) {
   for (double* b : bufs) if (b) cudaFree(b);
   float* fb[] = {c->u32, c->v32, c->w32, c->p32, c->u32l, c->v32l, c->w32l, c->p32l, c->phi32, c->d32[0],
                  c->d32[1], c->d32[2], c->dvo32[0], c->dvo32[1], c->dvo32[2], c->S32[0], c->S32[1], c->S32[2],
-                 c->dphi32, c->d32l[0], c->d32l[1], c->d32l[2], c->dvo32l[0], c->dvo32l[1], c->dvo32l[2]};
+                 c->dphi32, c->dv32h, c->dv32l, c->d32l[0], c->d32l[1], c->d32l[2], c->dvo32l[0], c->dvo32l[1], c->dvo32l[2]};
   for (float* b : fb) if (b) cudaFree(b);
   if (c->tmp64) cudaFree(c->tmp64);
   for (double* b : {c->rho, c->mu, c->p_o}) if (b) cudaFree(b);
@@ -1243,7 +1244,10 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
     for (float** f : fl)
       if ((r = alloc(f, L.total))) { fen_ctx_destroy(c); return r; }
     if ((r = alloc(&c->tmp64, L.total))) { fen_ctx_destroy(c); return r; }
-    if (c->refine && (r = alloc(&c->dphi32, L.total))) { fen_ctx_destroy(c); return r; }
+    if (c->refine && ((r = alloc(&c->dphi32, L.total)) || (r = alloc(&c->dv32h, L.total)) || (r = alloc(&c->dv32l, L.total)))) {
+      fen_ctx_destroy(c);
+      return r;
+    }
   } else {
     double** fl[] = {&c->phi, &c->us, &c->vs, &c->ws, &c->dvo[0], &c->dvo[1], &c->dvo[2]};
     for (double** f : fl)

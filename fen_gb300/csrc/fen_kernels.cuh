@@ -306,6 +306,7 @@ struct LineArgs {
   DFField pu, pv, pw;     // pair velocity of the mixed form (LD_DIVMIX)
   F2 idp[3];              // 1/delta per axis as float pairs (LD_DIVMIX, LD_RESID)
   F2 id2p[3];             // 1/delta^2 per axis as float pairs (LD_RESID)
+  float *dvh, *dvl;       // pair divergence D v*: written by LD_DIVMIX when set, read by LD_RESID
   const T* fsrc;          // LD_FIELD source
   T* fdst;                // ST_FIELD destination
   double* partial;        // ST_FIELD: per-CTA line sums (mean removal), may be null
@@ -394,14 +395,17 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
             const F2 dd = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
                                       a.ful, a.fvl, a.fwl,
                                       a.idp, i + 1, j, k);
+            if (a.dvh) {  // kept for the refinement's residual
+              const long long c = a.L.idx(i + 1, j, kst<DIM>(k));
+              a.dvh[c] = dd.hi;
+              a.dvl[c] = dd.lo;
+            }
             x = (T)(dd.hi + dd.lo) * (T)a.sc->rho_over_dt;
           } else {
-            // refinement right-hand side r = rho/dt D v* - L_h phi in double-float (phi = fsrc)
+            // refinement right-hand side r = rho/dt D v* - L_h phi in double-float (phi = fsrc;
+            // D v* as formed by this step's first transform)
             const long long c = a.L.idx(i + 1, j, kst<DIM>(k));
-            const F2 dd = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
-                                      a.ful, a.fvl, a.fwl,
-                                      a.idp, i + 1, j, k);
-            const F2 b = mul_pair(dd.hi, dd.lo, rod);
+            const F2 b = mul_pair(a.dvh[c], a.dvl[c], rod);
             const float* ph = (const float*)a.fsrc;
             F2 lap = add_pair(lap_term(ph, c, 1, a.id2p[0]), lap_term(ph, c, a.L.sx, a.id2p[1]));
             if (DIM == 3) lap = add_pair(lap, lap_term(ph, c, a.L.sp, a.id2p[2]));
