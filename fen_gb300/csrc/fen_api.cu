@@ -975,7 +975,11 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
       const size_t ns = c->stages.size();
       for (size_t q = 0; q < ns; ++q)
         if ((r = launch_stage(c, c->stages[q], q == 0 ? kFirstResidual : 0, c->phi32, c->dphi32))) return r;
-      if (c->needs_mean && (r = launch_mean(c, c->dphi32))) return r;
+      if (c->needs_mean) {  // mean of dphi only: k_correct_df removes it in the pressure update
+        k_mean_reduce<<<1, 1024, 0, c->stream>>>(c->partial, c->npartial, c->mean_div, c->sc);
+        c->launches++;
+        CK(cudaGetLastError());
+      }
       float* g[1] = {c->dphi32};
       if ((r = ghost<float>(c, 1, g, ids))) return r;
     }
@@ -984,6 +988,7 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
     ca.du = c->d32[0]; ca.dv = c->d32[1]; ca.dw = c->d32[2]; ca.phi = c->phi32;
     ca.dul = c->d32l[0]; ca.dvl = c->d32l[1]; ca.dwl = c->d32l[2];
     ca.dphi = c->refine ? c->dphi32 : nullptr;
+    ca.dphi_mean = c->refine && c->needs_mean;
     ca.u = DFFieldW{c->u32, c->u32l}; ca.v = DFFieldW{c->v32, c->v32l};
     ca.w = DFFieldW{c->w32, c->w32l}; ca.p = DFFieldW{c->p32, c->p32l};
     for (int q = 0; q < 3; ++q) ca.id[q] = 1.0 / c->d[q];

@@ -393,6 +393,7 @@ struct CorrDFArgs {
   const float *du, *dv, *dw, *phi;
   const float *dul, *dvl, *dwl;
   const float* dphi;  // refinement correction of phi (or null)
+  int dphi_mean;      // subtract the mean of dphi (sc->mean) in the pressure update
   DFFieldW u, v, w, p;
   double id[3];
   int iso;
@@ -406,6 +407,8 @@ __global__ void __launch_bounds__(256) k_correct_df(Layout L, const StepScalars*
   const float idx = (float)a.id[0];
   const float idy = a.iso ? idx : (float)a.id[1];
   const float idz = a.iso ? idx : (float)a.id[2];
+  // the mean of dphi leaves its gradient unchanged; it is removed only where dphi enters p
+  const float qm = a.dphi_mean ? (float)sc->mean : 0.0f;
   CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
   for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
     const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
@@ -434,7 +437,7 @@ __global__ void __launch_bounds__(256) k_correct_df(Layout L, const StepScalars*
     float hi, lo;
     hi = a.p.hi[c]; lo = a.p.lo[c];
     df_add(hi, lo, ph);
-    if (q) df_add(hi, lo, qh);
+    if (q) df_add(hi, lo, qh - qm);
     a.p.hi[c] = hi; a.p.lo[c] = lo;
   }
 }
