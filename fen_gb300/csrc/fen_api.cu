@@ -1186,6 +1186,11 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
   if (P->dim != 2 && P->dim != 3) return fail(FEN_ERR_ARG, "dim must be 2 or 3");
   if (P->nx < 2 || P->ny < 2 || (P->dim == 3 && P->nz < 2)) return fail(FEN_ERR_ARG, "grid sizes must be >= 2");
   if (P->precision != FEN_FP64 && P->precision != FEN_MIXED) return fail(FEN_ERR_ARG, "unknown precision form");
+  auto pos = [](double x) { return x > 0.0 && !std::isinf(x); };
+  if (!pos(P->lx) || !pos(P->ly) || (P->dim == 3 && !pos(P->lz))) return fail(FEN_ERR_ARG, "domain lengths must be positive");
+  if (!pos(P->density) || !(P->viscosity >= 0.0) || std::isinf(P->viscosity))
+    return fail(FEN_ERR_ARG, "density must be positive and viscosity non-negative");
+  if (P->constant_cfl && !pos(P->cfl)) return fail(FEN_ERR_ARG, "CFL must be positive");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(FEN_ERR_CUDA, "no CUDA device");
   fen_ctx* c = new fen_ctx();
@@ -1414,7 +1419,8 @@ int fen_set_bc_values(fen_ctx* c, int f, int face, const double* vals) {
 }
 
 int fen_set_bc_type(fen_ctx* c, int f, int face, int t) {
-  if (!c || f < FEN_U || f > FEN_PHI || face < 0 || face >= 6 || t < 0 || t > 2) return fail(FEN_ERR_ARG, "bad argument");
+  if (!c || f < FEN_U || f > FEN_PHI || face < 0 || face >= 2 * c->dim || t < 0 || t > 2)
+    return fail(FEN_ERR_ARG, "bad argument");
   c->ftype[f][face] = t;
   drop_graph(c);
   return 0;
@@ -1422,6 +1428,7 @@ int fen_set_bc_type(fen_ctx* c, int f, int face, int t) {
 
 int fen_set_timestep(fen_ctx* c, double U, double* dt) {
   if (!c || !dt) return fail(FEN_ERR_ARG, "null argument");
+  if (!(U >= 0.0)) return fail(FEN_ERR_ARG, "reference velocity U must be >= 0");
   // set_timestep (navier_stokes.f90:641-664)
   const double dl = c->dmin;
   const double dt_conv = c->prm.cfl * dl / U;
@@ -1440,6 +1447,7 @@ int fen_set_timestep(fen_ctx* c, double U, double* dt) {
 
 int fen_set_dt_o(fen_ctx* c, double dt_o) {
   if (!c) return fail(FEN_ERR_ARG, "null argument");
+  if (!(dt_o > 0.0) || std::isinf(dt_o)) return fail(FEN_ERR_ARG, "dt_o must be positive and finite");
   CK(cudaStreamSynchronize(c->stream));
   // keep dt_visc consistent with set_timestep's formula
   const double dl = c->dmin;
@@ -1456,6 +1464,7 @@ int fen_set_dt_o(fen_ctx* c, double dt_o) {
 int fen_advance_solution(fen_ctx* c, int step, double* dt) {
   (void)step;
   if (!c || !dt) return fail(FEN_ERR_ARG, "null argument");
+  if (!(*dt > 0.0) || std::isinf(*dt)) return fail(FEN_ERR_ARG, "dt must be positive and finite");
   int r;
   if ((r = pre_step(c, *dt))) return r;
   if ((r = capture_graph(c))) return r;
@@ -1469,6 +1478,7 @@ int fen_advance_solution(fen_ctx* c, int step, double* dt) {
 
 int fen_advance_n(fen_ctx* c, int nsteps, double* dt) {
   if (!c || !dt || nsteps < 0) return fail(FEN_ERR_ARG, "bad argument");
+  if (!(*dt > 0.0) || std::isinf(*dt)) return fail(FEN_ERR_ARG, "dt must be positive and finite");
   int r;
   if ((r = pre_step(c, *dt))) return r;
   if ((r = capture_graph(c))) return r;

@@ -43,3 +43,20 @@ def test_python_api_fails_loudly_when_library_missing(tmp_path):
 
     with pytest.raises(F.FenError):
         F.load_library(str(tmp_path / "missing.so"))
+
+
+@pytest.mark.parametrize("field,value,msg", [("lx", 0.0, b"domain lengths"), ("ly", -1.0, b"domain lengths"),
+                                             ("density", 0.0, b"density"), ("viscosity", -1.0, b"viscosity"),
+                                             ("cfl", 0.0, b"CFL")])
+def test_invalid_parameters_rejected_before_device_use(fen_lib, field, value, msg):
+    # parameter checks come before any CUDA call, so they run without a device
+    import fen_gb300 as F
+
+    p = F._Params()
+    p.dim, p.nx, p.ny, p.nz = 2, 8, 8, 1
+    p.lx = p.ly = p.lz = 1.0
+    p.density, p.viscosity, p.cfl, p.constant_cfl = 1.0, 0.01, 0.5, 1
+    setattr(p, field, value)
+    h = ctypes.c_void_p()
+    assert fen_lib.fen_ctx_create(ctypes.byref(p), ctypes.byref(h)) == -1
+    assert msg in fen_lib.fen_last_error()

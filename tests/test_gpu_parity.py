@@ -378,3 +378,22 @@ def test_get_field_into_caller_buffer(fen_lib):
     assert got is out and np.array_equal(out, s.get_field(F.U))
     with pytest.raises(ValueError):
         s.get_field(F.U, out=np.empty(g.shape, dtype=np.float32))
+
+
+def test_invalid_time_steps_rejected(fen_lib):
+    g = F.Grid(16, 16, 1, 1.0, 1.0, 1.0 / 16)
+    s = F.Solver(g)
+    for bad in (0.0, -1e-3, float("nan"), float("inf")):
+        with pytest.raises(F.FenError, match="dt_o"):
+            s.set_dt_o(bad)
+    s.set_dt_o(1e-3)
+    for bad in (0.0, -1e-3, float("nan")):
+        with pytest.raises(F.FenError, match="dt must be positive"):
+            s.advance_solution(1, bad)
+        with pytest.raises(F.FenError, match="dt must be positive"):
+            s.advance_n(2, bad)
+    with pytest.raises(F.FenError, match="U must be"):
+        s.set_timestep(-1.0)
+    # the context stays usable
+    s.advance_n(2, 1e-3)
+    assert not s.status()["nan"]
