@@ -197,7 +197,7 @@ def _compare_state(o, s, dim, tol):
 
 
 def test_step_tgv2d(fen_lib):
-    # BASELINE 2D TGV at reduced length: 128^2, nu = 0.01, dt = dt_o = 1e-3
+    # the 2D TGV workload at reduced length: 128^2, nu = 0.01, dt = dt_o = 1e-3
     N, L = 128, 2 * np.pi
     o, s = pair(2, (N, N, 1), (L, L, L / N), viscosity=0.01)
     _init_tgv2d(o, s, N, L)
@@ -213,7 +213,7 @@ def test_step_tgv2d(fen_lib):
 
 
 def test_step_tgv3d_constant_cfl(fen_lib):
-    # BASELINE 3D TGV at reduced size: Re = 1600, CFL = 0.5, dt from set_timestep(U = 1)
+    # the 3D TGV workload at reduced size: Re = 1600, CFL = 0.5, dt from set_timestep(U = 1)
     N, L = 32, 2 * np.pi
     o, s = pair(3, (N, N, N), (L, L, L), viscosity=1.0 / 1600, cfl=0.5, constant_cfl=True)
     u, v, w, p = C.tgv3d_fields(N, L)
