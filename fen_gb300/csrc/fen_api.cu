@@ -103,7 +103,7 @@ struct fen_ctx {
   double *us = nullptr, *vs = nullptr, *ws = nullptr;
   double* dvo[3] = {nullptr, nullptr, nullptr};
   double* S[3] = {nullptr, nullptr, nullptr};
-  // mixed-form FP32 fields: the state as hi/lo pairs, phi, the increment dt*rhs, dv_o, S
+  // mixed-form FP32 fields: the state as hi/lo pairs, phi, v* (pairs), dv_o, S
   float *u32 = nullptr, *v32 = nullptr, *w32 = nullptr, *p32 = nullptr, *phi32 = nullptr;
   float *u32l = nullptr, *v32l = nullptr, *w32l = nullptr, *p32l = nullptr;
   float* dphi32 = nullptr;  // refinement: correction of phi
@@ -111,7 +111,7 @@ struct fen_ctx {
   int refine = 0;
   float* d32[3] = {nullptr, nullptr, nullptr};
   float* dvo32[3] = {nullptr, nullptr, nullptr};
-  float* d32l[3] = {nullptr, nullptr, nullptr};    // increment lo (pairs with d32)
+  float* d32l[3] = {nullptr, nullptr, nullptr};    // v* lo (pairs with d32)
   float* dvo32l[3] = {nullptr, nullptr, nullptr};  // dv_o lo (pairs with dvo32)
   double* tmp64 = nullptr;                         // FP64 staging of dv_o pairs
   // variable-property path (FP64)
@@ -622,9 +622,7 @@ int launch_stage_t(fen_ctx* c, const Stage& s, int first_from_field, const void*
   } else if (s.ld == LD_DIV) {
     if (c->mixed) {
       ld = LD_DIVMIX;
-      a.fu = (const T*)c->d32[0]; a.fv = (const T*)c->d32[1]; a.fw = (const T*)c->d32[2];
-      a.ful = c->d32l[0]; a.fvl = c->d32l[1]; a.fwl = c->d32l[2];
-      a.pu = DFField{c->u32, c->u32l}; a.pv = DFField{c->v32, c->v32l}; a.pw = DFField{c->w32, c->w32l};
+      a.pu = DFField{c->d32[0], c->d32l[0]}; a.pv = DFField{c->d32[1], c->d32l[1]}; a.pw = DFField{c->d32[2], c->d32l[2]};
       if (c->refine) { a.dvh = c->dv32h; a.dvl = c->dv32l; }
     } else {
       a.fu = (const T*)c->us; a.fv = (const T*)c->vs; a.fw = (const T*)c->ws;
@@ -896,13 +894,20 @@ int pair_convert(fen_ctx* c, int f, int dir) {
 }
 
 // Ghost fill of up to four pair fields.
-int ghost_pairs(fen_ctx* c, int nf, const int* ids) {
+// Ghost fill of pair fields: the state pairs of `ids`, or the pairs (hi[q], lo[q]) with the
+// boundary rules of ids[q] when hi is given.
+int ghost_pairs(fen_ctx* c, int nf, const int* ids, float* const* hi = nullptr, float* const* lo = nullptr) {
   GhostDFBatch G;
   memset(&G, 0, sizeof(G));
   long long mx = 0;
   for (int q = 0; q < nf; ++q) {
-    double* d;
-    pair_of(c, ids[q], &G.hi[q], &G.lo[q], &d);
+    if (hi) {
+      G.hi[q] = hi[q];
+      G.lo[q] = lo[q];
+    } else {
+      double* d;
+      pair_of(c, ids[q], &G.hi[q], &G.lo[q], &d);
+    }
     G.bc[q] = field_bc(c, ids[q]);
     GhostCount g = (c->dim == 3) ? ghost_count<3>(c->L, G.bc[q]) : ghost_count<2>(c->L, G.bc[q]);
     G.n[q] = g.a + g.b + g.c;
@@ -930,11 +935,11 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
   if ((r = launch_predictor(c, c->sc))) return r;
   mark();  // 1: predictor
   if (c->mixed) {
+    // v* pairs take the velocity boundary rules (update_ghost_nodes on v*)
     float* f[3] = {c->d32[0], c->d32[1], c->d32[2]};
     float* fl[3] = {c->d32l[0], c->d32l[1], c->d32l[2]};
     int ids[3] = {FEN_U, FEN_V, FEN_W};
-    if ((r = ghost<float>(c, c->dim, f, ids, true))) return r;
-    if ((r = ghost<float>(c, c->dim, fl, ids, true))) return r;
+    if ((r = ghost_pairs(c, c->dim, ids, f, fl))) return r;
   } else {
     double* f[3] = {c->us, c->vs, c->ws};
     int ids[3] = {FEN_U, FEN_V, FEN_W};
@@ -954,7 +959,7 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
       if ((r = ghost<double>(c, c->dim, f, ids))) return r;
     }
   }
-  mark();  // 2: ghost v* (or its increment)
+  mark();  // 2: ghost v*
   {
     const size_t ns = c->stages.size();
     for (size_t q = 0; q < ns; ++q) {

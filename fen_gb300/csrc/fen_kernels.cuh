@@ -300,10 +300,10 @@ struct LineArgs {
   long long out_line, out_pos, out_outer;
   // fields (LD_FIELD / LD_DIV / ST_FIELD)
   Layout L;
-  const T *fu, *fv, *fw;  // predicted velocity for LD_DIV (the increment's hi part for LD_DIVMIX)
-  const float *ful, *fvl, *fwl;  // LD_DIVMIX: the increment's lo part
+  const T *fu, *fv, *fw;  // predicted velocity for LD_DIV
+  const float *ful, *fvl, *fwl;  // LD_DIVMIX: optional second pair added to pu, pv, pw
   const double* rho_c;           // LD_DIV with variable density: div * rho(i,j,k) * rho_over_dt (= 1/dt)
-  DFField pu, pv, pw;     // pair velocity of the mixed form (LD_DIVMIX)
+  DFField pu, pv, pw;     // pair v* of the mixed form (LD_DIVMIX)
   F2 idp[3];              // 1/delta per axis as float pairs (LD_DIVMIX, LD_RESID)
   F2 id2p[3];             // 1/delta^2 per axis as float pairs (LD_RESID)
   float *dvh, *dvl;       // pair divergence D v*: written by LD_DIVMIX when set, read by LD_RESID

@@ -123,16 +123,16 @@ __device__ __forceinline__ DF d2(DF p, DF c, DF m) {
 }
 
 // ------------------------------------------------------------------------------------
-// Predictor (mixed): the increment dt * rhs and dv_o, both as pairs.  Every term of
+// Predictor (mixed): v* = v + dt * rhs and dv_o, both as pairs.  Every term of
 // navier_stokes.f90:140-404 (advection in divergence form, diffusion, body force, pressure
-// gradient, AB2) is evaluated in double-float arithmetic, so the increments keep the
-// state's pair accuracy: FP32 rounding of the increments (about 0.5 |v| per step at
-// CFL 0.5) would otherwise random-walk into the solution.
+// gradient, AB2) is evaluated in double-float arithmetic and added to v as a pair, so v*
+// keeps the state's pair accuracy: FP32 rounding of the increments (about 0.5 |v| per step
+// at CFL 0.5) would otherwise random-walk into the solution.
 // ------------------------------------------------------------------------------------
 struct PredDFArgs {
   DFField u, v, w, p;
-  float *du, *dv, *dw;        // increment hi
-  float *dul, *dvl, *dwl;     // increment lo
+  float *du, *dv, *dw;        // v* hi
+  float *dul, *dvl, *dwl;     // v* lo
   float *dox, *doy, *doz;     // dv_o hi
   float *doxl, *doyl, *dozl;  // dv_o lo
   const float *Sx, *Sy, *Sz;
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(256) k_predictor_df(Layout L, const StepScalar
     DF ry = dsub(DF{a.g[1].hi, a.g[1].lo}, dmul(dsub(dfv(P, c + sy), pc), DF{a.gy.hi, a.gy.lo}));
     rx = dadd(rx, dadd(dmul(A, dx), dmul(B, DF{a.dox[c], a.doxl[c]})));
     ry = dadd(ry, dadd(dmul(A, dy), dmul(B, DF{a.doy[c], a.doyl[c]})));
-    const DF ix = dmul(DT, rx), iy = dmul(DT, ry);
+    const DF ix = dadd(uc, dmul(DT, rx)), iy = dadd(vc, dmul(DT, ry));  // v* pairs
     a.du[c] = ix.h; a.dul[c] = ix.l;
     a.dv[c] = iy.h; a.dvl[c] = iy.l;
     a.dox[c] = dx.h; a.doxl[c] = dx.l;
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(256) k_predictor_df(Layout L, const StepScalar
     if (DIM == 3) {
       DF rz = dsub(DF{a.g[2].hi, a.g[2].lo}, dmul(dsub(dfv(P, c + sz), pc), DF{a.gz.hi, a.gz.lo}));
       rz = dadd(rz, dadd(dmul(A, dz), dmul(B, DF{a.doz[c], a.dozl[c]})));
-      const DF iz = dmul(DT, rz);
+      const DF iz = dadd(wc, dmul(DT, rz));
       a.dw[c] = iz.h; a.dwl[c] = iz.l;
       a.doz[c] = dz.h; a.dozl[c] = dz.l;
     }
@@ -345,7 +345,8 @@ static __global__ void __launch_bounds__(kDTX * kDTY) k_predictor_df_tile(Layout
       rx = dadd(rx, dadd(dmul(A, dx), dmul(B, DF{a.dox[c], a.doxl[c]})));
       ry = dadd(ry, dadd(dmul(A, dy), dmul(B, DF{a.doy[c], a.doyl[c]})));
       rz = dadd(rz, dadd(dmul(A, dz), dmul(B, DF{a.doz[c], a.dozl[c]})));
-      const DF ix = dmul(DT, rx), iy = dmul(DT, ry), iz = dmul(DT, rz);
+      // v* = v + dt rhs as a pair
+      const DF ix = dadd(uc, dmul(DT, rx)), iy = dadd(vc, dmul(DT, ry)), iz = dadd(wc, dmul(DT, rz));
       a.du[c] = ix.h; a.dul[c] = ix.l;
       a.dv[c] = iy.h; a.dvl[c] = iy.l;
       a.dw[c] = iz.h; a.dwl[c] = iz.l;
@@ -375,7 +376,7 @@ __device__ __forceinline__ F2 div_term(const DFField& V, const float* d, const f
   return mul_pair(s, e, id);
 }
 
-// div(v*) at (i, j, k) as a pair, v* = v + (increment hi + lo) (null increments: div(v)).
+// div at (i, j, k) of the pair field V plus, when given, a second pair field (d, dl).
 template <int DIM>
 __device__ __forceinline__ F2 div_df(const Layout& L, const DFField& U, const DFField& V, const DFField& W,
                                      const float* du, const float* dv, const float* dw, const float* dul,
@@ -390,8 +391,8 @@ __device__ __forceinline__ F2 div_df(const Layout& L, const DFField& U, const DF
 // Correction (mixed): v = v + (dt*rhs - dt grad(phi)/rhof), p = p + phi, on the pairs.
 // ------------------------------------------------------------------------------------
 struct CorrDFArgs {
-  const float *du, *dv, *dw, *phi;
-  const float *dul, *dvl, *dwl;
+  const float *du, *dv, *dw, *phi;  // v* hi
+  const float *dul, *dvl, *dwl;     // v* lo
   const float* dphi;  // refinement correction of phi (or null)
   int dphi_mean;      // subtract the mean of dphi (sc->mean) in the pressure update
   DFFieldW u, v, w, p;
@@ -419,17 +420,17 @@ __global__ void __launch_bounds__(256) k_correct_df(Layout L, const StepScalars*
     // grad(phi + dphi) by differences of each part
     const float gx = (a.phi[c + 1] - ph) + (q ? q[c + 1] - qh : 0.0f);
     const float gy = (a.phi[c + L.sx] - ph) + (q ? q[c + L.sx] - qh : 0.0f);
-    // v += (increment pair) - dt grad(phi)/rhof, summed as pairs
+    // v = v* - dt grad(phi)/rhof, summed as pairs
     {
-      DF x = dadd(DF{a.u.hi[c], a.u.lo[c]}, DF{a.du[c], a.dul[c]});
+      DF x = DF{a.du[c], a.dul[c]};  // v*
       x = dadd(x, DF{-gx * idx * f, 0.f});
       a.u.hi[c] = x.h; a.u.lo[c] = x.l;
-      DF y = dadd(DF{a.v.hi[c], a.v.lo[c]}, DF{a.dv[c], a.dvl[c]});
+      DF y = DF{a.dv[c], a.dvl[c]};
       y = dadd(y, DF{-gy * idy * f, 0.f});
       a.v.hi[c] = y.h; a.v.lo[c] = y.l;
       if (DIM == 3) {
         const float gz = (a.phi[c + L.sp] - ph) + (q ? q[c + L.sp] - qh : 0.0f);
-        DF z = dadd(DF{a.w.hi[c], a.w.lo[c]}, DF{a.dw[c], a.dwl[c]});
+        DF z = DF{a.dw[c], a.dwl[c]};
         z = dadd(z, DF{-gz * idz * f, 0.f});
         a.w.hi[c] = z.h; a.w.lo[c] = z.l;
       }
