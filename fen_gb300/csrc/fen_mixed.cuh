@@ -270,7 +270,13 @@ __device__ __forceinline__ DF shfl_up_df(DF v) {
   return DF{__shfl_up_sync(0xffffffffu, v.h, 1), __shfl_up_sync(0xffffffffu, v.l, 1)};
 }
 
-static __global__ void __launch_bounds__(kDTX * kDTY) k_predictor_df_tile(Layout L, const StepScalars* __restrict__ sc,
+// Compiled for 3 resident 256-thread CTAs per SM (80 registers, no spills): 24 warps hide
+// the loads better than the 16 of the compiler's 128-register choice (channel: 2.82 ->
+// 2.36 ms); 4 CTAs (64 registers) spill.
+#ifndef FEN_DFTILE_MINB
+#define FEN_DFTILE_MINB 3
+#endif
+static __global__ void __launch_bounds__(kDTX * kDTY, FEN_DFTILE_MINB) k_predictor_df_tile(Layout L, const StepScalars* __restrict__ sc,
                                                                         PredDFArgs a) {
   __shared__ DF sh[2][3][kDTY][kDTX];
   const int tx = threadIdx.x, ty = threadIdx.y;
