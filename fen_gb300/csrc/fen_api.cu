@@ -297,8 +297,16 @@ Stage s_stage(fen_ctx* c, int op, int ld, int st, int ax, int ncol, int nouter, 
   const int n = c->n[ax];
   const bool cc = (op == OP_C2C_F || op == OP_C2C_I || op == OP_C2C_SOLVE);
   const int M = cc ? n : n / 2;
-  // tiles of 128-byte rows: 8 FP64 or 16 FP32 complex columns
-  int nl = c->mixed ? 16 : 8;
+  // columns per CTA (build-time knobs): 8 FP32 complex columns (64-byte row segments) or 4
+  // FP64 ones (64 bytes); measured against 16/8 and 4/8: FP32 column transforms 1.10 -> 0.90
+  // ms per mixed channel step, FP64 1.82 -> 1.77 ms per 256^3 TGV step
+#ifndef FEN_COL32_NL
+#define FEN_COL32_NL 8
+#endif
+#ifndef FEN_COL64_NL
+#define FEN_COL64_NL 4
+#endif
+  int nl = c->mixed ? FEN_COL32_NL : FEN_COL64_NL;
   while (nl > 2 && 2 * (size_t)nl * M * cplx_size(c) > 200 * 1024) nl /= 2;
   s.la.n = n;
   s.la.nl = nl;
