@@ -276,7 +276,12 @@ Stage x_stage(fen_ctx* c, int op, int ld, int st) {
   s.la = base_line(c);
   const int nx = c->n[0];
   const int M = nx / 2;
-  int nl = std::max(1, std::min(16, 1024 / M));
+// (measured: 2048 against 1024 and 512 complex elements per CTA; mixed channel inverse x
+// 0.44 -> 0.38 ms, the FP64 x transforms unchanged or slightly faster)
+#ifndef FEN_ROW_ELEMS
+#define FEN_ROW_ELEMS 2048
+#endif
+  int nl = std::max(1, std::min(16, FEN_ROW_ELEMS / M));  // lines per CTA: about FEN_ROW_ELEMS complex elements
   s.la.n = nx;
   s.la.nl = nl;
   s.la.nlines = c->n[1];
