@@ -282,6 +282,9 @@ Stage x_stage(fen_ctx* c, int op, int ld, int st) {
 #define FEN_ROW_ELEMS 2048
 #endif
   int nl = std::max(1, std::min(16, FEN_ROW_ELEMS / M));  // lines per CTA: about FEN_ROW_ELEMS complex elements
+  // small grids (2D): fewer lines per CTA so that the launch still spreads over the SMs
+  const long long rows = (long long)c->n[1] * (c->dim == 3 ? c->n[2] : 1);
+  while (nl > 1 && cdiv(rows, nl) < 2 * 152) nl /= 2;
   s.la.n = nx;
   s.la.nl = nl;
   s.la.nlines = c->n[1];
