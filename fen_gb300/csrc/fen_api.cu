@@ -708,14 +708,15 @@ int ghost(fen_ctx* c, int nf, T* const* ptr, const int* ids, bool homogeneous = 
   return 0;
 }
 
-int launch_mean(fen_ctx* c, float* target32 = nullptr) {
+// Remove the mean of phi (poisson.f90:491-503): reduce the inverse transform's partials, then
+// subtract.
+int launch_mean(fen_ctx* c) {
   const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
   const int grid = std::min(cdiv(ncell, 256), 152 * 8);
   k_mean_reduce<<<1, 1024, 0, c->stream>>>(c->partial, c->npartial, c->mean_div, c->sc);
   if (c->mixed) {
-    float* t = target32 ? target32 : c->phi32;
-    if (c->dim == 3) k_mean_subtract<float, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, t);
-    else k_mean_subtract<float, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, t);
+    if (c->dim == 3) k_mean_subtract<float, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, c->phi32);
+    else k_mean_subtract<float, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, c->phi32);
   } else {
     if (c->dim == 3) k_mean_subtract<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, c->phi);
     else k_mean_subtract<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, c->phi);
