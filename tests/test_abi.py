@@ -60,3 +60,11 @@ def test_invalid_parameters_rejected_before_device_use(fen_lib, field, value, ms
     h = ctypes.c_void_p()
     assert fen_lib.fen_ctx_create(ctypes.byref(p), ctypes.byref(h)) == -1
     assert msg in fen_lib.fen_last_error()
+
+
+def test_fortran_binding_covers_the_header():
+    # the iso_c_binding module a FEN maintainer adds binds every entry point
+    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    mod = txt[txt.index("module fen_gpu_mod"):txt.index("end module fen_gpu_mod")]
+    missing = [s for s in declared_symbols() if f"function {s}(" not in mod]
+    assert not missing, missing
