@@ -228,7 +228,13 @@ __global__ void __launch_bounds__(256) k_predictor_df(Layout L, const StepScalar
 // memory and from the previous k in registers), as in the FP64 k_predictor_tile.  Each sum
 // is formed upper + lower, so the sharing cell and the per-cell formula see the same pairs.
 // ------------------------------------------------------------------------------------
-constexpr int kDTX = 32, kDTY = 8, kDTZ = 16;
+#ifndef FEN_DFTILE_TY
+#define FEN_DFTILE_TY 4
+#endif
+#ifndef FEN_DFTILE_TZ
+#define FEN_DFTILE_TZ 16
+#endif
+constexpr int kDTX = 32, kDTY = FEN_DFTILE_TY, kDTZ = FEN_DFTILE_TZ;
 
 // Products on the + sides of cell c: fuu (i+1/2), fvv (j+1/2), fww (k+1/2), euv (i+1/2, j+1/2),
 // euw (i+1/2, k+1/2), evw (j+1/2, k+1/2) (the 1/4 is folded into q).
@@ -270,11 +276,12 @@ __device__ __forceinline__ DF shfl_up_df(DF v) {
   return DF{__shfl_up_sync(0xffffffffu, v.h, 1), __shfl_up_sync(0xffffffffu, v.l, 1)};
 }
 
-// Compiled for 3 resident 256-thread CTAs per SM (80 registers, no spills): 24 warps hide
-// the loads better than the 16 of the compiler's 128-register choice (channel: 2.82 ->
-// 2.36 ms); 4 CTAs (64 registers) spill.
+// Tiles of 32 x 4 cells compiled for 6 resident 128-thread CTAs per SM (80 registers, no
+// spills): 24 warps hide the loads better than the 16 of the compiler's 128-register choice
+// (channel: 2.82 -> 2.36 ms with 32 x 8 tiles at 3 CTAs, 2.30 ms with 32 x 4 at 6); 64
+// registers spill, and z-walks of 32 planes are slower.
 #ifndef FEN_DFTILE_MINB
-#define FEN_DFTILE_MINB 3
+#define FEN_DFTILE_MINB 6
 #endif
 static __global__ void __launch_bounds__(kDTX * kDTY, FEN_DFTILE_MINB) k_predictor_df_tile(Layout L, const StepScalars* __restrict__ sc,
                                                                         PredDFArgs a) {
