@@ -11,8 +11,11 @@ by FFT in all three directions.  A "step" is one navier_stokes_solver time step
 
 One JSON line on rank 0.  `value` is device time (CUDA events on the library's stream, K
 captured steps replayed back to back, inputs resident in HBM); `e2e` is the same metric
-through the C ABI with host buffers (pinned upload of u, v, w, p, K advance_solution calls
-each returning dt and the diagnostics to the host, download of u, v, w, p).
+through the C ABI with pinned host buffers (upload of u, v, w, p, K advance_solution calls
+each returning dt and the diagnostics to the host, download of u, v, w, p into pinned
+buffers).  Defaults: K = 100 timed steps after W = 3 warm-up steps; nvidia-smi clocks and
+throttle reasons are sampled every 50 ms during the timed region.  Inputs are larger than L2
+(137 MB per field at 256^3).
 Multi-GPU: the path does not shard (one grid per device); N ranks run N independent
 replicas (weak scaling) and `value` sums their cells over the slowest rank's time.
 `--impl reference` times the CPU restatement of the reference (the oracle port; the
