@@ -191,3 +191,36 @@ def test_unsupported_bc_rejected():
     # poisson.f90:91-95 aborts when no solver matches (here: walls in x only, 3D)
     with pytest.raises(ValueError):
         O.Oracle(3, (8, 8, 8), (1, 1, 1), bc=[O.WALL, O.WALL] + [O.PERIODIC] * 4)
+
+
+def test_abc_flow_decay_second_order():
+    # large_test/ABC (ABC.f90:40-166): the Arnold-Beltrami-Childress flow u = sin z + cos y,
+    # v = sin x + cos z, w = sin y + cos x is a Beltrami field (advection is a gradient the
+    # projection removes), so it decays as exp(-nu t); nu = 1 and dt = delta^2 / (16 nu) (the
+    # 3D viscous limit delta^2 / (6 nu) of set_timestep sits outside AB2's stability interval
+    # for the grid's highest Laplacian mode), errors at t = 0.1 converge at second order
+    nu, T = 1.0, 0.1
+    Ns, errs = [16, 32, 64], []
+    for N in Ns:
+        L = 2 * np.pi
+        d = L / N
+        g = C.mac_grids(3, (N, N, N), (d, d, d))
+        X, Y, Z = g["u"]
+        u = np.sin(Z) + np.cos(Y)
+        X, Y, Z = g["v"]
+        v = np.sin(X) + np.cos(Z)
+        X, Y, Z = g["w"]
+        w = np.sin(Y) + np.cos(X)
+        o = O.Oracle(3, (N, N, N), (L, L, L), viscosity=nu)
+        for f, a in ((O.U, u), (O.V, v), (O.W, w)):
+            o.field(f)[...] = a
+            o.update_ghost_nodes(f)
+        dt = d * d / (16 * nu)
+        o.dt_o = dt
+        nst = int(np.ceil(T / dt))
+        o.run(nst, dt)
+        decay = np.exp(-nu * nst * dt)
+        err = max(np.abs(C.interior(o.field(f), 3) - C.interior(a, 3) * decay).max()
+                  for f, a in ((O.U, u), (O.V, v), (O.W, w)))
+        errs.append(err)
+    assert C.convergence_slope(Ns, errs) > 1.8, errs
