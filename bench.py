@@ -116,20 +116,8 @@ def init_fields(name, cfg, n, shape):
         return {"u": u, "v": v, "p": p}
     # channel: laminar Poiseuille u = (1 - y^2)/(2 nu) plus seeded uniform noise of 5% of
     # the centreline velocity on u, v, w (PCG64 seed 1234, Fortran order)
-    rng = np.random.Generator(np.random.PCG64(1234))
-    dy = L[1] / n[1]
-    yc = -1.0 + (np.arange(n[1] + 2) - 0.5) * dy
-    Uc = 1.0 / (2 * cfg["nu"])
-    out = {}
-    for key in "uvw":
-        a = np.zeros(shape)
-        noise = rng.uniform(-1.0, 1.0, size=(n[2], n[1], n[0]))
-        a[1:-1, 1:-1, 1:-1] = 0.05 * Uc * noise
-        if key == "u":
-            a[1:-1, 1:-1, 1:-1] += ((1 - yc[1:-1] ** 2) / (2 * cfg["nu"]))[None, :, None]
-        out[key] = a
-    out["p"] = np.zeros(shape)
-    return out
+    assert shape == (n[2] + 2, n[1] + 2, n[0] + 2)
+    return dict(zip("uvwp", C.channel_fields(n, L, cfg["nu"])))
 
 
 def start_velocity(name, cfg):
@@ -293,7 +281,7 @@ def form_adjoint(F, ndir=16, nsteps=500, every=50):
 
     def load(s, u, v):
         for fid, a in ((F.U, u), (F.V, v), (F.P, None), (F.DVO_X, None), (F.DVO_Y, None)):
-            f = s.zeros()
+            f = s.zeros(fid)
             if a is not None:
                 f[1, 1:-1, 1:-1] = a
             s.set_field(fid, f)

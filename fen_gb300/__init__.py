@@ -9,10 +9,14 @@ FEN Fortran modules the C ABI replaces:
     navier_stokes_mod   set_timestep, module state v, p, phi, dv_o, S, maxdiv, maxCFL
                                                            (src/navier_stokes.f90:17-45, 623)
     poisson_mod         solve_poisson                      (src/poisson.f90:21-29)
-    fields_mod          divergence                         (src/fields.f90:120-153)
+    fields_mod          gradient, divergence, laplacian    (src/fields.f90:13-26)
+                        add_advection                      (src/navier_stokes.f90:261-353)
 
-Fields are exchanged as numpy arrays in FEN's layout f(0:nx+1, 0:ny+1, 0:nz+1) (x fastest),
-viewed in numpy as shape (nz+2, ny+2, nx+2); in 2D the z extent is 0:2 (3 planes).
+Fields are exchanged as numpy arrays in FEN's allocation of each field, x fastest: v, p, phi,
+rho, mu with one ghost layer, f(0:nx+1, 0:ny+1, 0:nz+1), viewed in numpy as shape
+(nz+2, ny+2, nx+2) (in 2D the z extent is 0:2, 3 planes); dv_o and S without ghosts,
+f(1:nx, 1:ny, 1:nz), shape (nz, ny, nx) (1 plane in 2D).  ``Solver.field_shape(fid)`` gives
+the shape.
 
 The CUDA library is required: there is no CPU fallback, and loading fails loudly when the
 shared library or a GPU is missing.
@@ -74,6 +78,7 @@ _EXPORTS = [
     "fen_ensemble_launches", "fen_ensemble_smem_bytes", "fen_ensemble_adjoint_setup", "fen_ensemble_adjoint_forward",
     "fen_ensemble_adjoint_seed", "fen_ensemble_adjoint_backward", "fen_ensemble_adjoint_gradient",
     "fen_ensemble_adjoint_dts", "fen_set_split_pressure", "fen_set_ibm_forcing", "fen_get_ibm_force",
+    "fen_upload_gl", "fen_download_gl", "fen_field_bounds", "fen_gradient", "fen_laplacian", "fen_add_advection",
 ]
 
 
@@ -92,6 +97,9 @@ def load_library(path=None):
     L.fen_last_error.restype = ctypes.c_char_p
     L.fen_upload.argtypes = [vp, ip, dp]
     L.fen_download.argtypes = [vp, ip, dp]
+    L.fen_upload_gl.argtypes = [vp, ip, dp, ip]
+    L.fen_download_gl.argtypes = [vp, ip, dp, ip]
+    L.fen_field_bounds.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.fen_update_ghost_nodes.argtypes = [vp, ip]
     L.fen_set_bc_values.argtypes = [vp, ip, ip, dp]
     L.fen_set_bc_type.argtypes = [vp, ip, ip, ip]
@@ -103,6 +111,9 @@ def load_library(path=None):
     L.fen_solve_poisson.argtypes = [vp]
     L.fen_divergence.argtypes = [vp, dp]
     L.fen_explicit_terms.argtypes = [vp, dp]
+    L.fen_gradient.argtypes = [vp, ip, dp, dp, dp]
+    L.fen_laplacian.argtypes = [vp, ip, dp]
+    L.fen_add_advection.argtypes = [vp, dp, dp, dp]
     L.fen_sync.argtypes = [vp]
     L.fen_kernel_launches.argtypes = [vp]
     L.fen_kernel_launches.restype = ctypes.c_longlong
@@ -177,6 +188,17 @@ class Grid:
         """numpy shape (k, j, i) of a ghosted field."""
         return ((self.Nz + 2) if self.dim == 3 else 3, self.Ny + 2, self.Nx + 2)
 
+    @property
+    def interior_shape(self):
+        """numpy shape (k, j, i) of a field without ghosts (FEN's default gl = 0)."""
+        return (self.Nz if self.dim == 3 else 1, self.Ny, self.Nx)
+
+
+# Ghost level of FEN's allocation of each field (navier_stokes.f90:759-768): dv_o and S have
+# none (scalar.f90:76-81), the others one.
+def field_gl(fid):
+    return 0 if DVO_X <= fid <= S_Z else 1
+
 
 class Solver:
     """One solver instance: init_solver + the navier_stokes_mod/poisson_mod module state.
@@ -225,25 +247,43 @@ class Solver:
             pass
 
     # -- fields ----------------------------------------------------------------------------
-    def zeros(self):
-        return np.zeros(self.grid.shape)
+    def zeros(self, fid=None):
+        """A zero host array shaped like field `fid` (a ghosted field when omitted)."""
+        return np.zeros(self.field_shape(fid if fid is not None else U))
 
-    def set_field(self, fid, arr):
+    def field_shape(self, fid, gl=None):
+        """numpy shape of field `fid` with ghost level `gl` (FEN's allocation when None)."""
+        gl = field_gl(fid) if gl is None else gl
+        return self.grid.shape if gl == 1 else self.grid.interior_shape
+
+    def field_bounds(self, fid):
+        """Fortran (lbound, ubound) of FEN's allocation of field `fid`."""
+        lo, hi = (ctypes.c_int * 3)(), (ctypes.c_int * 3)()
+        self._check(self._L.fen_field_bounds(self._h, fid, lo, hi))
+        return tuple(lo), tuple(hi)
+
+    def set_field(self, fid, arr, gl=None):
+        """Upload field `fid` from a host array in FEN's allocation of it (or with ghost level
+        `gl`: 0 interior only, 1 with one ghost layer)."""
         a = np.ascontiguousarray(arr, dtype=np.float64)
-        if a.shape != self.grid.shape:
-            raise ValueError(f"field shape {a.shape} != {self.grid.shape}")
-        self._check(self._L.fen_upload(self._h, fid, _dp(a)))
+        shape = self.field_shape(fid, gl)
+        if a.shape != shape:
+            raise ValueError(f"field {fid}: shape {a.shape} != {shape}")
+        g = field_gl(fid) if gl is None else int(gl)
+        self._check(self._L.fen_upload_gl(self._h, fid, _dp(a), g))
 
-    def get_field(self, fid, out=None):
-        """Download field `fid`; into `out` (a C-contiguous float64 array of the grid's shape,
+    def get_field(self, fid, out=None, gl=None):
+        """Download field `fid`; into `out` (a C-contiguous float64 array of the field's shape,
         e.g. a pinned host buffer) when given, else into a new array."""
+        shape = self.field_shape(fid, gl)
         if out is None:
-            a = self.zeros()
+            a = np.zeros(shape)
         else:
             a = out
-            if a.shape != self.grid.shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
-                raise ValueError(f"out must be a C-contiguous float64 array of shape {self.grid.shape}")
-        self._check(self._L.fen_download(self._h, fid, _dp(a)))
+            if a.shape != shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"out must be a C-contiguous float64 array of shape {shape}")
+        g = field_gl(fid) if gl is None else int(gl)
+        self._check(self._L.fen_download_gl(self._h, fid, _dp(a), g))
         return a
 
     def update_ghost_nodes(self, fid):
@@ -304,6 +344,39 @@ class Solver:
         out = np.zeros(g.Nx * g.Ny * g.Nz)
         self._check(self._L.fen_divergence(self._h, _dp(out)))
         return out.reshape(g.Nz, g.Ny, g.Nx)
+
+    def gradient(self, fid):
+        """gradient_of_scalar of field `fid` (p, phi, rho, mu, p_o): interior arrays
+        (gx, gy[, gz]) at the faces (fields.f90:31-64)."""
+        g = self.grid
+        out = [np.zeros(g.interior_shape) for _ in range(3)]
+        self._check(self._L.fen_gradient(self._h, fid, _dp(out[0]), _dp(out[1]), _dp(out[2])))
+        return tuple(out[: g.dim])
+
+    def laplacian(self, fid):
+        """laplacian of field `fid` over the interior: laplacian_of_scalar for p, phi, rho, mu,
+        p_o; the laplacian_of_vector component formula for u, v, w (fields.f90:256-343)."""
+        out = np.zeros(self.grid.interior_shape)
+        self._check(self._L.fen_laplacian(self._h, fid, _dp(out)))
+        return out
+
+    def add_advection(self, rhs=None):
+        """add_advection(comp_grid, RHS) (navier_stokes.f90:261-353): RHS += the advection
+        terms of the current velocity; rhs is a list of interior arrays (zeros if None),
+        updated in place and returned."""
+        g = self.grid
+        if rhs is None:
+            rhs = [np.zeros(g.interior_shape) for _ in range(g.dim)]
+        rr = [np.ascontiguousarray(a, dtype=np.float64) for a in rhs]
+        for a in rr:
+            if a.shape != g.interior_shape:
+                raise ValueError(f"rhs shape {a.shape} != {g.interior_shape}")
+        z = rr[2] if g.dim == 3 else np.zeros(1)
+        self._check(self._L.fen_add_advection(self._h, _dp(rr[0]), _dp(rr[1]), _dp(z)))
+        for a, b in zip(rhs, rr):
+            if a is not b:
+                a[...] = b
+        return rhs
 
     def explicit_terms(self):
         g = self.grid

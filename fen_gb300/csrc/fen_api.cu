@@ -25,6 +25,7 @@
 
 #include "../../include/fen_gpu.h"
 #include "fen_adjoint.cuh"
+#include "fen_fields.cuh"
 #include "fen_kernels.cuh"
 #include "fen_varprop.cuh"
 #include "fen_types.cuh"
@@ -158,6 +159,7 @@ struct fen_ctx {
   long long launches = 0;
   long long launches_per_step = 0;
   double* stage_scratch = nullptr;  // host-layout staging for upload/download (one field)
+  double* util = nullptr;           // fields_mod operators: 3 interior arrays + one FP64 field
   // discrete adjoint (2D periodic FP64): checkpoints, recomputed step inputs, adjoint fields
   struct Adjoint {
     int nsteps = 0, every = 0, nckpt = 0;
@@ -1082,32 +1084,45 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
 
 int host_planes(fen_ctx* c) { return c->dim == 3 ? c->n[2] + 2 : 3; }
 
-// Copy one field between FEN's host layout and the padded HBM layout through a contiguous
-// staging buffer (one memcpy + one relayout kernel).  dir 0: host -> device, 1: back.
+// Copy one field between FEN's host layout (gl ghost layers, see k_relayout) and the padded
+// HBM layout through a contiguous staging buffer (one memcpy + one relayout kernel).  dir 0:
+// host -> device, 1: back.
 template <typename T>
-int relayout(fen_ctx* c, T* dfield, double* host_rw, int dir) {
-  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
-  const int planes = (c->dim == 3) ? c->n[2] + 2 : 1;
-  const size_t cnt = (size_t)nxg * nyg * planes;
-  double* h = host_rw + (c->dim == 2 ? (size_t)nxg * nyg : 0);  // 2D: plane k = 1
+int relayout(fen_ctx* c, T* dfield, double* host_rw, int dir, int gl) {
+  const int nxh = c->n[0] + 2 * gl, nyh = c->n[1] + 2 * gl;
+  const int planes = (c->dim == 3) ? c->n[2] + 2 * gl : 1;
+  const size_t cnt = (size_t)nxh * nyh * planes;
+  double* h = host_rw + ((c->dim == 2 && gl == 1) ? (size_t)nxh * nyh : 0);  // 2D, gl = 1: plane k = 1
   if (!c->stage_scratch) {
     int r;
-    if ((r = alloc(&c->stage_scratch, (long long)cnt))) return r;
+    const long long full = (long long)(c->n[0] + 2) * (c->n[1] + 2) * ((c->dim == 3) ? c->n[2] + 2 : 1);
+    if ((r = alloc(&c->stage_scratch, full))) return r;
   }
   const int grid = std::min(cdiv((long long)cnt, 256), 152 * 16);
   if (dir == 0) {
     CK(cudaMemcpyAsync(c->stage_scratch, h, cnt * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    k_relayout<T><<<grid, 256, 0, c->stream>>>(c->L, planes, c->stage_scratch, dfield, nullptr, nullptr, 0);
+    k_relayout<T><<<grid, 256, 0, c->stream>>>(c->L, planes, gl, c->stage_scratch, dfield, nullptr, nullptr, 0);
     c->launches++;
     CK(cudaGetLastError());
   } else {
-    k_relayout<T><<<grid, 256, 0, c->stream>>>(c->L, planes, nullptr, nullptr, dfield, c->stage_scratch, 1);
+    k_relayout<T><<<grid, 256, 0, c->stream>>>(c->L, planes, gl, nullptr, nullptr, dfield, c->stage_scratch, 1);
     c->launches++;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h, c->stage_scratch, cnt * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
   return 0;
+}
+
+// Ghost level of FEN's allocation of each field (navier_stokes.f90:759-768): p, phi, rho,
+// mu and v with one layer; dv_o and S with none (scalar.f90:76-81, default gl = 0); p_o with
+// one (multiphase.f90:55).
+int fen_gl(int f) { return (f >= FEN_DVO_X && f <= FEN_S_Z) ? 0 : 1; }
+
+// Host elements of a field array with gl ghost layers (2D: gl = 1 arrays have 3 planes).
+size_t host_count(fen_ctx* c, int gl) {
+  const size_t pl = (c->dim == 3) ? (size_t)c->n[2] + 2 * gl : (size_t)(1 + 2 * gl);
+  return (size_t)(c->n[0] + 2 * gl) * (c->n[1] + 2 * gl) * pl;
 }
 
 int pre_step(fen_ctx* c, double dt) {
@@ -1172,7 +1187,7 @@ int fen_ctx_destroy(fen_ctx* c) {
   drop_graph(c);
   double* bufs[] = {c->u, c->v, c->w, c->p, c->phi, c->us, c->vs, c->ws, c->dvo[0], c->dvo[1], c->dvo[2],
                     c->S[0], c->S[1], c->S[2], c->mwn[0], c->mwn[1], c->mwn[2], c->ta, c->tb, c->tc, c->c1,
-                    c->fac, c->partial, c->pdiv, c->pvel, c->stage_scratch};
+                    c->fac, c->partial, c->pdiv, c->pvel, c->stage_scratch, c->util};
   for (double* b : bufs) if (b) cudaFree(b);
   float* fb[] = {c->u32, c->v32, c->w32, c->p32, c->u32l, c->v32l, c->w32l, c->p32l, c->phi32, c->d32[0],
                  c->d32[1], c->d32[2], c->dvo32[0], c->dvo32[1], c->dvo32[2], c->S32[0], c->S32[1], c->S32[2],
@@ -1320,9 +1335,10 @@ int prop_field(fen_ctx* c, int f, double** out) {
   return 0;
 }
 
-int fen_upload(fen_ctx* c, int f, const double* host) {
+int fen_upload_gl(fen_ctx* c, int f, const double* host, int gl) {
   if (!c || !host) return fail(FEN_ERR_ARG, "null argument");
   if (f < FEN_U || f > FEN_P_O || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
+  if (gl != 0 && gl != 1) return fail(FEN_ERR_ARG, "ghost level must be 0 or 1");
   double* hrw = const_cast<double*>(host);
   int r;
   if (f >= FEN_RHO) {
@@ -1330,7 +1346,7 @@ int fen_upload(fen_ctx* c, int f, const double* host) {
     if ((r = prop_field(c, f, &d))) return r;
     if (f == FEN_RHO && !c->var_rho) { c->var_rho = 1; drop_graph(c); }
     if (f == FEN_MU && !c->var_mu) { c->var_mu = 1; drop_graph(c); }
-    return relayout<double>(c, d, hrw, 0);
+    return relayout<double>(c, d, hrw, 0, gl);
   }
   if (f >= FEN_S_X && f <= FEN_S_Z) {
     // S is used in every component once any is set (dv += S/rhof, navier_stokes.f90:245-255)
@@ -1338,14 +1354,13 @@ int fen_upload(fen_ctx* c, int f, const double* host) {
       if (c->mixed && !c->S32[q] && (r = alloc(&c->S32[q], c->L.total))) return r;
       if (!c->mixed && !c->S[q] && (r = alloc(&c->S[q], c->L.total))) return r;
     }
-    c->has_S = 1;
-    drop_graph(c);
-    return c->mixed ? relayout<float>(c, c->S32[f - FEN_S_X], hrw, 0) : relayout<double>(c, c->S[f - FEN_S_X], hrw, 0);
+    if (!c->has_S) { c->has_S = 1; drop_graph(c); }
+    return c->mixed ? relayout<float>(c, c->S32[f - FEN_S_X], hrw, 0, gl) : relayout<double>(c, c->S[f - FEN_S_X], hrw, 0, gl);
   }
   if (f >= FEN_DVO_X && f <= FEN_DVO_Z) {
-    if (!c->mixed) return relayout<double>(c, c->dvo[f - FEN_DVO_X], hrw, 0);
+    if (!c->mixed) return relayout<double>(c, c->dvo[f - FEN_DVO_X], hrw, 0, gl);
     // dv_o is a pair in the mixed form: FP64 staging, then split
-    if ((r = relayout<double>(c, c->tmp64, hrw, 0))) return r;
+    if ((r = relayout<double>(c, c->tmp64, hrw, 0, gl))) return r;
     const int grid = std::min(cdiv(c->L.total, 256), 152 * 16);
     k_split<<<grid, 256, 0, c->stream>>>(c->L.total, c->tmp64, c->dvo32[f - FEN_DVO_X], c->dvo32l[f - FEN_DVO_X]);
     c->launches++;
@@ -1353,45 +1368,60 @@ int fen_upload(fen_ctx* c, int f, const double* host) {
     CK(cudaStreamSynchronize(c->stream));
     return 0;
   }
-  if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, hrw, 0) : relayout<double>(c, c->phi, hrw, 0);
+  if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, hrw, 0, gl) : relayout<double>(c, c->phi, hrw, 0, gl);
   double* d = (f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p;
-  if ((r = relayout<double>(c, d, hrw, 0))) return r;
+  if (c->mixed && gl == 0 && (r = pair_convert(c, f, 1))) return r;  // keep the device ghosts
+  if ((r = relayout<double>(c, d, hrw, 0, gl))) return r;
   if (c->mixed && (r = pair_convert(c, f, 0))) return r;
   if (f == FEN_U || f == FEN_V || f == FEN_W) c->vel_dirty = 1;
   CK(cudaStreamSynchronize(c->stream));
   return 0;
 }
 
-int fen_download(fen_ctx* c, int f, double* host) {
+int fen_download_gl(fen_ctx* c, int f, double* host, int gl) {
   if (!c || !host) return fail(FEN_ERR_ARG, "null argument");
   if (f < FEN_U || f > FEN_P_O || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
+  if (gl != 0 && gl != 1) return fail(FEN_ERR_ARG, "ghost level must be 0 or 1");
   if (f >= FEN_RHO) {
     double* d;
     int r;
     if ((r = prop_field(c, f, &d))) return r;
-    return relayout<double>(c, d, host, 1);
+    return relayout<double>(c, d, host, 1, gl);
   }
   if (f >= FEN_S_X && f <= FEN_S_Z) {
     if (!c->has_S) {
-      const size_t nh = (size_t)(c->n[0] + 2) * (c->n[1] + 2) * host_planes(c);
-      memset(host, 0, nh * sizeof(double));
+      memset(host, 0, host_count(c, gl) * sizeof(double));
       return 0;
     }
-    return c->mixed ? relayout<float>(c, c->S32[f - FEN_S_X], host, 1) : relayout<double>(c, c->S[f - FEN_S_X], host, 1);
+    return c->mixed ? relayout<float>(c, c->S32[f - FEN_S_X], host, 1, gl) : relayout<double>(c, c->S[f - FEN_S_X], host, 1, gl);
   }
   if (f >= FEN_DVO_X && f <= FEN_DVO_Z) {
-    if (!c->mixed) return relayout<double>(c, c->dvo[f - FEN_DVO_X], host, 1);
+    if (!c->mixed) return relayout<double>(c, c->dvo[f - FEN_DVO_X], host, 1, gl);
     const int grid = std::min(cdiv(c->L.total, 256), 152 * 16);
     k_join<<<grid, 256, 0, c->stream>>>(c->L.total, c->dvo32[f - FEN_DVO_X], c->dvo32l[f - FEN_DVO_X], c->tmp64);
     c->launches++;
     CK(cudaGetLastError());
-    return relayout<double>(c, c->tmp64, host, 1);
+    return relayout<double>(c, c->tmp64, host, 1, gl);
   }
-  if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, host, 1) : relayout<double>(c, c->phi, host, 1);
+  if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, host, 1, gl) : relayout<double>(c, c->phi, host, 1, gl);
   double* d = (f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p;
   int r;
   if (c->mixed && (r = pair_convert(c, f, 1))) return r;
-  return relayout<double>(c, d, host, 1);
+  return relayout<double>(c, d, host, 1, gl);
+}
+
+int fen_upload(fen_ctx* c, int f, const double* host) { return fen_upload_gl(c, f, host, fen_gl(f)); }
+int fen_download(fen_ctx* c, int f, double* host) { return fen_download_gl(c, f, host, fen_gl(f)); }
+
+int fen_field_bounds(fen_ctx* c, int f, int* lo, int* hi) {
+  if (!c || !lo || !hi) return fail(FEN_ERR_ARG, "null argument");
+  if (f < FEN_U || f > FEN_P_O || (f == FEN_W && c->dim == 2)) return fail(FEN_ERR_ARG, "bad field id");
+  const int gl = fen_gl(f);
+  for (int q = 0; q < 3; ++q) {
+    lo[q] = 1 - gl;
+    hi[q] = c->n[q] + gl;
+  }
+  return 0;
 }
 
 int fen_update_ghost_nodes(fen_ctx* c, int f) {
@@ -1432,11 +1462,14 @@ int fen_set_bc_values(fen_ctx* c, int f, int face, const double* vals) {
   const int nbd = (c->dim == 3 || face >= 4) ? nb : 1;
   const double* src = vals + ((c->dim == 2 && face < 4) ? (size_t)na : 0);
   if (!c->bcval[f][face]) {
+    // a new device array: the captured step must be rebuilt to read it
     int r;
     if ((r = alloc(&c->bcval[f][face], (long long)na * nbd))) return r;
+    drop_graph(c);
   }
-  CK(cudaMemcpy(c->bcval[f][face], src, (size_t)na * nbd * sizeof(double), cudaMemcpyHostToDevice));
-  drop_graph(c);
+  // stream-ordered after the previous step (the graph reads these values in place)
+  CK(cudaMemcpyAsync(c->bcval[f][face], src, (size_t)na * nbd * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   return 0;
 }
 
@@ -1587,17 +1620,9 @@ int fen_explicit_terms(fen_ctx* c, double* out) {
   CK(cudaMalloc((void**)&dsc, sizeof(StepScalars)));
   CK(cudaMemcpyAsync(dsc, &s, sizeof(s), cudaMemcpyHostToDevice, c->stream));
   if ((r = launch_predictor(c, dsc))) return r;
-  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
   const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
-  std::vector<double> h((size_t)nxg * nyg * host_planes(c));
   for (int q = 0; q < c->dim; ++q) {
-    if ((r = fen_download(c, FEN_DVO_X + q, h.data()))) return r;
-    size_t t = 0;
-    const int K = (c->dim == 3) ? c->n[2] : 1;
-    for (int k = 1; k <= K; ++k)
-      for (int j = 1; j <= c->n[1]; ++j)
-        for (int i = 1; i <= c->n[0]; ++i)
-          out[(size_t)q * ncell + t++] = h[(size_t)i + (size_t)nxg * ((size_t)j + (size_t)nyg * k)];
+    if ((r = fen_download_gl(c, FEN_DVO_X + q, out + (size_t)q * ncell, 0))) return r;
     void* dst = c->mixed ? (void*)c->dvo32[q] : (void*)c->dvo[q];
     CK(cudaMemcpyAsync(dst, save[q], tot * es, cudaMemcpyDeviceToDevice, c->stream));
     if (c->mixed)
@@ -1609,33 +1634,137 @@ int fen_explicit_terms(fen_ctx* c, double* out) {
   return 0;
 }
 
-// ---- checkpoint / restart (solver.f90:103-329) ----------------------------------------
+// ---- fields_mod generics and add_advection (fields.f90:13-26; navier_stokes.f90:261-353) ----
 namespace {
-// Interior of one field (x fastest) through a ghosted host download.
-int interior_get(fen_ctx* c, int f, std::vector<double>& out) {
-  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
-  std::vector<double> h((size_t)nxg * nyg * host_planes(c));
-  int r;
-  if ((r = fen_download(c, f, h.data()))) return r;
-  const int K = (c->dim == 3) ? c->n[2] : 1;
-  out.resize((size_t)c->n[0] * c->n[1] * K);
-  size_t t = 0;
-  for (int k = 1; k <= K; ++k)
-    for (int j = 1; j <= c->n[1]; ++j)
-      for (int i = 1; i <= c->n[0]; ++i) out[t++] = h[(size_t)i + (size_t)nxg * ((size_t)j + (size_t)nyg * k)];
+// Scratch of the field operators: three interior arrays and one ghosted FP64 field.
+int util_scratch(fen_ctx* c, double** out3, double** field) {
+  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+  if (!c->util) {
+    int r;
+    if ((r = alloc(&c->util, 3 * ncell + c->L.total))) return r;
+  }
+  *out3 = c->util;
+  *field = c->util + 3 * ncell;
   return 0;
 }
 
-int interior_set(fen_ctx* c, int f, const double* in) {
-  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
-  std::vector<double> h((size_t)nxg * nyg * host_planes(c), 0.0);
-  const int K = (c->dim == 3) ? c->n[2] : 1;
-  size_t t = 0;
-  for (int k = 1; k <= K; ++k)
-    for (int j = 1; j <= c->n[1]; ++j)
-      for (int i = 1; i <= c->n[0]; ++i) h[(size_t)i + (size_t)nxg * ((size_t)j + (size_t)nyg * k)] = in[t++];
-  return fen_upload(c, f, h.data());
+// Device FP64 copy of a ghosted scalar or velocity field (pairs joined in the mixed form).
+int fp64_field(fen_ctx* c, int f, double* spare, const double** out) {
+  int r;
+  switch (f) {
+    case FEN_U: case FEN_V: case FEN_W: case FEN_P:
+      if (c->mixed && (r = pair_convert(c, f, 1))) return r;
+      *out = (f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p;
+      return 0;
+    case FEN_PHI:
+      if (!c->mixed) { *out = c->phi; return 0; }
+      k_widen_field<<<std::min(cdiv(c->L.total, 256), 152 * 16), 256, 0, c->stream>>>(c->L.total, c->phi32, spare);
+      c->launches++;
+      CK(cudaGetLastError());
+      *out = spare;
+      return 0;
+    case FEN_RHO: case FEN_MU: case FEN_P_O: {
+      double* d;
+      if ((r = prop_field(c, f, &d))) return r;
+      *out = d;
+      return 0;
+    }
+  }
+  return fail(FEN_ERR_ARG, "field has no ghost nodes (gradient and laplacian need a ghosted field)");
 }
+
+FieldOpArgs field_args(fen_ctx* c) {
+  FieldOpArgs a;
+  memset(&a, 0, sizeof(a));
+  for (int q = 0; q < 3; ++q) {
+    a.id[q] = 1.0 / c->d[q];
+    a.id2[q] = 1.0 / (c->d[q] * c->d[q]);
+  }
+  a.iso = c->iso;
+  return a;
+}
+
+int launch_field_op(fen_ctx* c, const FieldOpArgs& a) {
+  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+  const int grid = std::min(cdiv(ncell, 256), 152 * 16);
+  if (c->dim == 3) k_field_op<3><<<grid, 256, 0, c->stream>>>(c->L, a);
+  else k_field_op<2><<<grid, 256, 0, c->stream>>>(c->L, a);
+  c->launches++;
+  CK(cudaGetLastError());
+  return 0;
+}
+}  // namespace
+
+int fen_gradient(fen_ctx* c, int f, double* gx, double* gy, double* gz) {
+  if (!c || !gx || !gy || (c->dim == 3 && !gz)) return fail(FEN_ERR_ARG, "null argument");
+  if (f == FEN_U || f == FEN_V || f == FEN_W) return fail(FEN_ERR_ARG, "gradient of a scalar field (p, phi, rho, mu, p_o)");
+  double *o, *spare;
+  const double* s;
+  int r;
+  if ((r = util_scratch(c, &o, &spare)) || (r = fp64_field(c, f, spare, &s))) return r;
+  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+  FieldOpArgs a = field_args(c);
+  a.op = FOP_GRADIENT;
+  a.s = s;
+  a.o0 = o; a.o1 = o + ncell; a.o2 = o + 2 * ncell;
+  if ((r = launch_field_op(c, a))) return r;
+  double* dst[3] = {gx, gy, gz};
+  for (int q = 0; q < c->dim; ++q)
+    CK(cudaMemcpyAsync(dst[q], o + q * ncell, ncell * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int fen_laplacian(fen_ctx* c, int f, double* out) {
+  if (!c || !out) return fail(FEN_ERR_ARG, "null argument");
+  double *o, *spare;
+  const double* s;
+  int r;
+  if ((r = util_scratch(c, &o, &spare)) || (r = fp64_field(c, f, spare, &s))) return r;
+  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+  FieldOpArgs a = field_args(c);
+  a.op = FOP_LAPLACIAN;
+  a.s = s;
+  a.comp = (f == FEN_W) ? 2 : 0;
+  a.o0 = o;
+  if ((r = launch_field_op(c, a))) return r;
+  CK(cudaMemcpyAsync(out, o, ncell * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int fen_add_advection(fen_ctx* c, double* rx, double* ry, double* rz) {
+  if (!c || !rx || !ry || (c->dim == 3 && !rz)) return fail(FEN_ERR_ARG, "null argument");
+  double *o, *spare;
+  const double *u, *v, *w = nullptr;
+  int r;
+  if ((r = util_scratch(c, &o, &spare)) || (r = fp64_field(c, FEN_U, spare, &u)) || (r = fp64_field(c, FEN_V, spare, &v)))
+    return r;
+  if (c->dim == 3 && (r = fp64_field(c, FEN_W, spare, &w))) return r;
+  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+  double* rr[3] = {rx, ry, rz};
+  for (int q = 0; q < c->dim; ++q)
+    CK(cudaMemcpyAsync(o + q * ncell, rr[q], ncell * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  FieldOpArgs a = field_args(c);
+  a.op = FOP_ADVECTION;
+  a.u = u; a.v = v; a.w = w;
+  a.o0 = o; a.o1 = o + ncell; a.o2 = o + 2 * ncell;
+  if ((r = launch_field_op(c, a))) return r;
+  for (int q = 0; q < c->dim; ++q)
+    CK(cudaMemcpyAsync(rr[q], o + q * ncell, ncell * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+// ---- checkpoint / restart (solver.f90:103-329) ----------------------------------------
+namespace {
+// Interior of one field (x fastest), FEN's f(lo(1):hi(1), lo(2):hi(2), lo(3):hi(3)).
+int interior_get(fen_ctx* c, int f, std::vector<double>& out) {
+  out.resize(host_count(c, 0));
+  return fen_download_gl(c, f, out.data(), 0);
+}
+
+int interior_set(fen_ctx* c, int f, const double* in) { return fen_upload_gl(c, f, in, 0); }
 
 // save_state / load_state field order (solver.f90:195-208, 277-292).
 std::vector<int> state_order(fen_ctx* c) {
@@ -1852,7 +1981,7 @@ int fen_adjoint_backward(fen_ctx* c, const double* lam_u, const double* lam_v, d
   if (!A.ready) return fail(FEN_ERR_STATE, "fen_adjoint_forward first");
   int r;
   // adjoint of the final state: (lam_u, lam_v), p^ = 0, dv_o^ = 0
-  if ((r = relayout<double>(c, A.uh, const_cast<double*>(lam_u), 0)) || (r = relayout<double>(c, A.vh, const_cast<double*>(lam_v), 0)))
+  if ((r = relayout<double>(c, A.uh, const_cast<double*>(lam_u), 0, 1)) || (r = relayout<double>(c, A.vh, const_cast<double*>(lam_v), 0, 1)))
     return r;
   CK(cudaMemsetAsync(A.ph, 0, c->L.total * sizeof(double), c->stream));
   CK(cudaMemsetAsync(A.dou, 0, c->L.total * sizeof(double), c->stream));
@@ -1884,7 +2013,7 @@ int fen_adjoint_backward(fen_ctx* c, const double* lam_u, const double* lam_v, d
   if ((r = adj_restore(c, A.nckpt))) return r;
   // gradient: interior of v^ at step 0 (ghost entries zero)
   const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
-  if ((r = relayout<double>(c, A.uh, g_u, 1)) || (r = relayout<double>(c, A.vh, g_v, 1))) return r;
+  if ((r = relayout<double>(c, A.uh, g_u, 1, 1)) || (r = relayout<double>(c, A.vh, g_v, 1, 1))) return r;
   for (double* g : {g_u, g_v}) {
     double* h = g + (size_t)nxg * nyg;  // plane k = 1
     for (int j = 0; j < nyg; ++j)

@@ -1602,7 +1602,7 @@ int fen_ensemble_tune(fen_ensemble* e, int steps, const char* cache_path) {
   const std::string key = device_key(e->dev);
   std::map<int, int> cached_g;
   int cached_t = 0;
-  if (cache_path) {
+  if (cache_path && cache_path[0]) {
     std::ifstream f(cache_path);
     std::string line;
     while (std::getline(f, line)) {
@@ -1688,7 +1688,7 @@ int fen_ensemble_tune(fen_ensemble* e, int steps, const char* cache_path) {
   cudaFree(backup);
   if (r) return r;
   if ((r = build_packs(e, {}))) return r;
-  if (cache_path) {
+  if (cache_path && cache_path[0]) {
     std::ofstream f(cache_path, std::ios::app);
     for (size_t c = 0; c < e->cls_n.size(); ++c) f << key << " N " << e->cls_n[c] << " " << e->cls_g[c] << "\n";
     f << key << " threads " << e->threads << "\n";

@@ -1001,18 +1001,25 @@ __global__ void k_inv_lam_table(int ncol, int n, int nouter, const double* lamA,
   }
 }
 
-// Host-layout <-> HBM-layout copies.  The host array is FEN's contiguous f(0:nx+1, 0:ny+1,
-// planes) (x fastest); one contiguous copy moves it to a staging buffer and this kernel
-// scatters rows into the padded layout (dir = 0) or gathers them back (dir = 1).
+// Host-layout <-> HBM-layout copies.  The host array is FEN's contiguous Fortran array with
+// gl ghost layers (x fastest): gl = 1 is f(0:nx+1, 0:ny+1, planes) as FEN allocates p, phi,
+// v, rho and mu (scalar.f90:79-81 with l = 1); gl = 0 is the interior f(1:nx, 1:ny, 1:nz)
+// that FEN allocates for dv, dv_o, grad_p, rhof and S (navier_stokes.f90:759-768, default
+// gl = 0).  One contiguous copy moves it to a staging buffer and this kernel scatters rows
+// into the padded layout (dir = 0) or gathers them back (dir = 1); with gl = 0 the device
+// ghosts are left as they are.  `planes` counts the host array's planes (1 in 2D).
 template <typename T>
-__global__ void __launch_bounds__(256) k_relayout(Layout L, int planes, const double* __restrict__ src, T* dst_field,
+__global__ void __launch_bounds__(256) k_relayout(Layout L, int planes, int gl, const double* __restrict__ src, T* dst_field,
                                                   const T* __restrict__ src_field, double* dst, int dir) {
-  const int nxg = L.n0 + 2;
-  const long long total = (long long)nxg * (L.n1 + 2) * planes;
+  const int nxh = L.n0 + 2 * gl, nyh = L.n1 + 2 * gl;
+  const int k0 = (L.dim == 3) ? 1 - gl : 0;  // storage plane of the host array's first plane
+  const long long total = (long long)nxh * nyh * planes;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % nxg);
-    const long long row = t / nxg;  // j + (ny+2) * plane
-    const long long d = (long long)L.off + i + (long long)L.sx * row;
+    const long long row = t / nxh;  // j + nyh * plane
+    const int i = (int)(t - row * nxh) + 1 - gl;
+    const int pl = (int)(row / nyh);
+    const int j = (int)(row - (long long)pl * nyh) + 1 - gl;
+    const long long d = L.idx(i, j, pl + k0);
     if (dir == 0) dst_field[d] = (T)src[t];
     else dst[t] = (double)src_field[d];
   }

@@ -1,19 +1,20 @@
 // Allocation-free 2D periodic Poisson solve (FEN's pp solver, src/poisson.f90:416-505).
 //
 // Some callers cannot allocate device memory: host codes that run inside a framework which
-// owns every device allocation through its own pool, code running while a CUDA graph is
-// being captured by someone else, or embedded solvers whose memory budget is fixed up front.
-// They already hold their input and output arrays, but cannot give the solver the scratch it
-// needs.  fen_poisson_pp2d_noalloc therefore keeps its scratch (half spectrum, twiddles,
+// owns every device allocation through its own pool, or embedded solvers whose memory budget
+// is fixed up front.  They already hold their input and output arrays, but cannot give the
+// solver the scratch it needs.  fen_poisson_pp2d_noalloc therefore keeps its scratch (half spectrum, twiddles,
 // eigenvalues, mean-removal partial sums) in one file-scope static device array of a fixed
 // maximum size, which every GPU that loads this library holds until the process exits.
 //
 // The array name is only a host-side stand-in in host code; its device address is fetched
-// with cudaGetSymbolAddress once per device (with that device current) and passed to the
-// kernels.  Every call shares the array and leaves its contents behind, so calls that
-// overlap on the GPU (different streams, or different host threads on the same device)
-// race; serialise them.  Nothing in the array needs to start at zero: each call rewrites the
-// tables it uses and every partial-sum slot it reads.
+// with cudaGetSymbolAddress on the first call on each device (with that device current) and
+// passed to the kernels.  Later calls fetch it again (no allocation) and redo the set-up
+// when it changed, which happens after cudaDeviceReset reloads the module.  Every call
+// shares the array and leaves its contents behind, so calls that overlap on the GPU
+// (different streams, or different host threads on the same device) race; serialise them.
+// Nothing in the array needs to start at zero: each call rewrites the tables it uses and
+// every partial-sum slot it reads.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,14 +53,15 @@ std::mutex g_mu;
 double2* g_addr[256] = {nullptr};
 
 // Per-device set-up: the device address of the static array and the shared-memory limits of
-// the transform kernels used here.  Runs on the first call on each device.
+// the transform kernels used here.  Runs on the first call on each device, and again when
+// the array's address changed (a device reset reloads the module and drops the limits).
 int setup_device(int dev, double2** out) {
   std::lock_guard<std::mutex> lk(g_mu);
   if (dev < 0 || dev >= 256) return fen_internal_fail(FEN_ERR_ARG, "fen_poisson_pp2d_noalloc: device index out of range");
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return fen_internal_fail(FEN_ERR_CUDA, (std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)).c_str());
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return fen_internal_fail(FEN_ERR_CUDA, (std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)).c_str());
+  if (g_addr[dev] != (double2*)p) {
     const int lim = 200 * 1024;
     e = cudaFuncSetAttribute(k_line<double, 2, true, OP_R2C, LD_FIELD, ST_CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e == cudaSuccess)

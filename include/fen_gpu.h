@@ -8,9 +8,13 @@
  * Conventions
  *   - Every entry point returns 0 on success or a negative FEN_ERR_* code; the message of
  *     the last failure on the calling thread is returned by fen_last_error().
- *   - Host field arrays use FEN's Fortran layout with one ghost layer:
- *       f(0:nx+1, 0:ny+1, 0:nz+1), x fastest (src/scalar.f90:79-81);
- *     in 2D the z extent is 0:2 and only plane k = 1 is read or written.
+ *   - Host field arrays use FEN's Fortran layout, x fastest, with the ghost level FEN
+ *     allocates for that field (src/navier_stokes.f90:759-768, src/scalar.f90:76-81):
+ *       gl = 1: f(0:nx+1, 0:ny+1, 0:nz+1) for v (u, v, w), p, phi, rho, mu, p_o;
+ *       gl = 0: f(1:nx, 1:ny, 1:nz) for dv_o and S (FEN's default, no ghosts).
+ *     In 2D the z extent is 0:2 (gl = 1; only plane k = 1 is read or written) or 1:1
+ *     (gl = 0).  fen_field_bounds returns the bounds; fen_upload_gl/fen_download_gl take
+ *     an explicit ghost level for callers whose host copy is laid out otherwise.
  *   - One context = one grid + one solver instance on the current CUDA device, with one
  *     stream.  Calls on one context must be serialised by the caller; distinct contexts are
  *     independent.  Device state persists between calls; host arrays are never retained.
@@ -82,10 +86,19 @@ int fen_ctx_create(const fen_params* params, fen_ctx** out);
 int fen_ctx_destroy(fen_ctx* ctx);
 const char* fen_last_error(void);
 
-/* Host <-> device transfer of one field (Fortran layout above).  fen_upload copies the
- * whole ghosted array (interior and ghosts) like a Fortran assignment to v%x%f. */
+/* Host <-> device transfer of one field in FEN's allocation of it (layout above), like a
+ * Fortran assignment to v%x%f or S%x%f: the host array is c_loc(f%f) of the FEN field.
+ * fen_upload of a gl = 1 field copies interior and ghosts; a gl = 0 field (dv_o, S) has no
+ * ghosts to copy. */
 int fen_upload(fen_ctx* ctx, int field, const double* host);
 int fen_download(fen_ctx* ctx, int field, double* host);
+/* The same with the host array's ghost level given explicitly (0: interior f(1:nx, 1:ny,
+ * 1:nz) only, the device ghosts are left as they are; 1: f(0:nx+1, 0:ny+1, 0:nz+1)). */
+int fen_upload_gl(fen_ctx* ctx, int field, const double* host, int gl);
+int fen_download_gl(fen_ctx* ctx, int field, double* host, int gl);
+/* Fortran bounds lbound(f%f) / ubound(f%f) of FEN's allocation of `field` (scalar.f90:
+ * 76-81): lo = 1 - gl, hi = n + gl per axis (in 2D the z bounds are 0:2 or 1:1). */
+int fen_field_bounds(fen_ctx* ctx, int field, int lo[3], int hi[3]);
 /* scalar%update_ghost_nodes (src/scalar.f90:223-396) on the device copy. */
 int fen_update_ghost_nodes(fen_ctx* ctx, int field);
 /* Dirichlet values of one face of one field: field%bc%left ... (scalar.f90:28-36).  The
@@ -114,6 +127,18 @@ int fen_divergence(fen_ctx* ctx, double* out);
 /* compute_explicit_terms(dv) with the current v, p (src/navier_stokes.f90:217-257); the
  * three components go to out (3 * nx*ny*nz, x fastest). */
 int fen_explicit_terms(fen_ctx* ctx, double* out);
+
+/* fields_mod generics on the device copy of a field (src/fields.f90:13-26), FP64 results in
+ * interior arrays f(1:nx, 1:ny, 1:nz), the shape FEN allocates for grad_p and lap_v (gl = 0).
+ * fen_gradient: gradient_of_scalar (fields.f90:31-64) of p, phi, rho, mu or p_o, forward
+ * differences to the faces (gz unused in 2D).  fen_laplacian: laplacian_of_scalar (:256-290)
+ * of a scalar field, or the component formula of laplacian_of_vector (:294-343) for u, v, w.
+ * fen_add_advection: add_advection(comp_grid, RHS) (navier_stokes.f90:261-353, called by
+ * test/small_test/navier_stokes/advection/advection.f90:50): adds the advection terms of the
+ * current velocity to the caller's RHS arrays (in/out). */
+int fen_gradient(fen_ctx* ctx, int field, double* gx, double* gy, double* gz);
+int fen_laplacian(fen_ctx* ctx, int field, double* out);
+int fen_add_advection(fen_ctx* ctx, double* rhs_x, double* rhs_y, double* rhs_z);
 
 /* save_state / load_state (src/solver.f90:160-329): raw FP64 global interiors, x fastest,
  * no header, in the order p, u, v, dv_o%x, dv_o%y[, w, dv_o%z]; load_state refreshes the
@@ -171,17 +196,20 @@ int fen_profile_step(fen_ctx* ctx, int reps, double dt, double* out);
 
 /* Allocation-free 2D periodic Poisson solve.  No counterpart in the reference: it serves
  * callers that cannot allocate device memory (a host framework that owns every device
- * allocation through its own pool, code running inside someone else's stream capture, or a
- * solver embedded under a fixed memory budget).  It solves lap(phi) = rhs exactly as FEN's
- * pp solver does (FFT in x and y, zero mode set to 0, mean removed) with grid spacing
- * lx/nx on both axes.  rhs and phi are caller-owned device-accessible arrays of nx*ny
- * doubles (interior only, x fastest); they may alias.  The call allocates nothing: its
- * scratch lives in a static device array of about 8.5 MB that every GPU loading this library
- * holds until exit, sized for nx, ny <= FEN_NOALLOC_MAX_N; larger sizes are rejected with
- * FEN_ERR_ARG.  The first call on each device fetches that array's device address (make it
- * before any stream capture).  All calls share the array, so calls that overlap on the GPU
- * race and must be serialised.  Work is queued on `stream` (NULL = default stream) and the
- * call returns after synchronising it. */
+ * allocation through its own pool, or a solver embedded under a fixed memory budget).  It
+ * solves lap(phi) = rhs as FEN's pp solver does (FFT in x and y, zero mode set to 0, mean
+ * removed) with grid spacing lx/nx on both axes.  rhs and phi are caller-owned
+ * device-accessible arrays of nx*ny doubles (interior only, x fastest); they may alias.  The
+ * call allocates nothing: its scratch lives in a static device array of about 8.5 MB that
+ * every GPU loading this library holds until exit, sized for nx, ny <= FEN_NOALLOC_MAX_N;
+ * larger sizes are rejected with FEN_ERR_ARG.  The first call on each device fetches that
+ * array's device address (the set-up); every later call checks the address again and
+ * repeats the set-up if it changed (after cudaDeviceReset).  All calls share the array, so
+ * calls that overlap on the GPU race and must be serialised.  Work is queued on `stream`
+ * (NULL = default stream) and the call returns after synchronising it.  The eigenvalues
+ * come from device sincospi here, not from the host cosine table of the context path, so
+ * the result matches fen_solve_poisson on the same grid to rounding (1e-13 relative L2), not
+ * bit for bit. */
 #define FEN_NOALLOC_MAX_N 1024
 int fen_poisson_pp2d_noalloc(const double* rhs, double* phi, int nx, int ny, double lx, void* stream);
 
@@ -213,7 +241,7 @@ int fen_ensemble_config(fen_ensemble* ens, int* threads, int* sizes, int* groups
 int fen_ensemble_set_config(fen_ensemble* ens, int threads, const int* groups);
 /* Autotuner: times each feasible CTAs-per-run choice per grid size, then the CTA size, on
  * the ensemble's own runs (state restored afterwards); caches results in cache_path (may be
- * NULL) and reuses them when present. */
+ * NULL or empty: no cache) and reuses them when present. */
 int fen_ensemble_tune(fen_ensemble* ens, int steps, const char* cache_path);
 long long fen_ensemble_launches(fen_ensemble* ens);
 /* Forward/adjoint pair of every run: the discrete adjoint of the ensemble step (FP32, the

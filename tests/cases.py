@@ -59,6 +59,27 @@ def tgv3d_fields(n, L):
     return u, v, w, p
 
 
+def channel_fields(n, L, nu, seed=1234, noise=0.05):
+    """Channel workload start (walls at y = -1, 1): laminar Poiseuille u = (1 - y^2)/(2 nu)
+    at the u points plus seeded uniform noise of `noise` times the centreline velocity on the
+    interiors of u, v, w (PCG64(seed), drawn per component in Fortran order, x fastest);
+    p = 0.  Returns ghosted arrays (u, v, w, p)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shape = (n[2] + 2, n[1] + 2, n[0] + 2)
+    dy = L[1] / n[1]
+    yc = -1.0 + (np.arange(n[1] + 2) - 0.5) * dy
+    Uc = 1.0 / (2 * nu)
+    out = []
+    for key in "uvw":
+        a = np.zeros(shape)
+        a[1:-1, 1:-1, 1:-1] = noise * Uc * rng.uniform(-1.0, 1.0, size=(n[2], n[1], n[0]))
+        if key == "u":
+            a[1:-1, 1:-1, 1:-1] += ((1 - yc[1:-1] ** 2) / (2 * nu))[None, :, None]
+        out.append(a)
+    out.append(np.zeros(shape))
+    return tuple(out)
+
+
 def random_interior(shape, rng, dim):
     a = np.zeros(shape)
     if dim == 3:

@@ -62,9 +62,47 @@ def test_invalid_parameters_rejected_before_device_use(fen_lib, field, value, ms
     assert msg in fen_lib.fen_last_error()
 
 
+def declared_prototypes():
+    """{name: number of arguments} of every entry point in include/fen_gpu.h."""
+    txt = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for name, args in re.findall(r"\b(fen_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt, flags=re.S):
+        a = args.strip()
+        out[name] = 0 if a in ("", "void") else a.count(",") + 1
+    return out
+
+
+FORTRAN = os.path.join(ROOT, "fen_gb300", "fortran")
+
+
 def test_fortran_binding_covers_the_header():
-    # the iso_c_binding module a FEN maintainer adds binds every entry point
-    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    mod = txt[txt.index("module fen_gpu_mod"):txt.index("end module fen_gpu_mod")]
-    missing = [s for s in declared_symbols() if f"function {s}(" not in mod]
+    # the iso_c_binding module (fen_gb300/fortran/fen_gpu_mod.f90) binds every entry point
+    # with the C prototype's number of arguments and its C name
+    txt = open(os.path.join(FORTRAN, "fen_gpu_mod.f90")).read()
+    body = txt[txt.index("module fen_gpu_mod"):txt.index("end module fen_gpu_mod")]
+    bound = {}
+    for name, args, cname in re.findall(
+            r"function\s+(fen_[a-z0-9_]+)\s*\(([^)]*)\)\s*(?:&\s*)?bind\s*\(\s*C\s*,\s*name\s*=\s*'([a-z0-9_]+)'",
+            body):
+        bound[name] = (0 if not args.strip() else args.count(",") + 1, cname)
+    protos = declared_prototypes()
+    assert len(protos) >= 50
+    missing = [s for s in protos if s not in bound]
     assert not missing, missing
+    wrong = {s: (bound[s], protos[s]) for s in protos if bound[s][0] != protos[s] or bound[s][1] != s}
+    assert not wrong, wrong
+
+
+def test_fortran_routing_uses_only_bound_entry_points():
+    # the FEN-side routing module calls entry points that fen_gpu_mod binds, and re-points
+    # FEN's two procedure pointers
+    route = open(os.path.join(FORTRAN, "fen_gpu_route.f90")).read()
+    mod = open(os.path.join(FORTRAN, "fen_gpu_mod.f90")).read()
+    called = set(re.findall(r"\b(fen_[a-z0-9_]+)\s*\(", route))
+    for s in called - {"fen_check"}:
+        assert f"function {s}(" in mod, s
+    assert "advance_solution => gpu_advance_solution" in route
+    assert "solve_poisson => gpu_solve_poisson" in route
+    # every module and program unit is closed
+    for f in (route, mod):
+        assert f.count("module fen_gpu") == 2 * len(re.findall(r"^module ", f, flags=re.M))

@@ -25,9 +25,12 @@ def _smooth(rng, n, kmax=6):
     return f / np.sqrt(np.mean(f ** 2))
 
 
-def _full(s, interior):
-    a = s.zeros()
-    a[1, 1:-1, 1:-1] = interior
+def _full(s, interior, fid=0):
+    a = s.zeros(fid)
+    if a.shape[0] == 1:  # a field without ghosts (dv_o)
+        a[0] = interior
+    else:
+        a[1, 1:-1, 1:-1] = interior
     return a
 
 
@@ -38,7 +41,7 @@ def _solver(n, nu):
 
 def _state(s, u0, v0, p0):
     for fid, a in ((F.U, u0), (F.V, v0), (F.P, p0), (F.DVO_X, 0 * u0), (F.DVO_Y, 0 * u0)):
-        s.set_field(fid, _full(s, a))
+        s.set_field(fid, _full(s, a, fid))
         if fid in (F.U, F.V, F.P):
             s.update_ghost_nodes(fid)
 

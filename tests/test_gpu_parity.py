@@ -340,7 +340,7 @@ def test_nan_is_reported_not_faulted(fen_lib):
     # the context stays usable once the state (including the AB2 history dv_o, which
     # carries the NaN as it would in the reference) is re-initialised
     for fid in (F.U, F.V, F.P, F.DVO_X, F.DVO_Y):
-        s.set_field(fid, s.zeros())
+        s.set_field(fid, s.zeros(fid))
     s.advance_solution(2, 1e-3)
 
 
