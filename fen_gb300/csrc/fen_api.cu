@@ -133,6 +133,8 @@ struct fen_ctx {
   double* mwn[3] = {nullptr, nullptr, nullptr};
   double *ta = nullptr, *tb = nullptr, *tc = nullptr;  // tridiagonal a, b, c (device)
   double *c1 = nullptr, *fac = nullptr;
+  int* conv = nullptr;        // first row of the pivots' fixed point per system
+  double tri_a = 0.0;         // sub-diagonal of the interior rows
   void* specC = nullptr;
   void* specR = nullptr;
   void* inv_lam = nullptr;
@@ -342,6 +344,8 @@ Stage t_stage(fen_ctx* c, void* x, long long s_col, long long s_row, long long s
   s.ta.a = c->ta;
   s.ta.c1 = c->c1;
   s.ta.fac = c->fac;
+  s.ta.conv = c->conv;
+  s.ta.aval = c->tri_a;
   s.ta.form3 = form3;
   s.tgrid = dim3(cdiv(ncol, 128), nouter);
   return s;
@@ -369,8 +373,10 @@ int init_tridiag(fen_ctx* c, int ax, int ncol, int nouter, const double* lamA, c
   CK(cudaMemcpy(c->tb, b.data(), n * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(c->tc, cc.data(), n * sizeof(double), cudaMemcpyHostToDevice));
   const long long nt = (long long)n * ncol * nouter;
-  if ((r = alloc(&c->c1, nt)) || (r = alloc(&c->fac, nt))) return r;
-  k_thomas_tables<<<dim3(cdiv(ncol, 128), nouter), 128>>>(ncol, nouter, n, c->ta, c->tb, c->tc, lamA, lamB, form3, c->c1, c->fac);
+  if ((r = alloc(&c->c1, nt)) || (r = alloc(&c->fac, nt)) || (r = alloc(&c->conv, (long long)ncol * nouter))) return r;
+  c->tri_a = a[n - 1];  // rows 1 .. n-1 share a = 1/delta^2
+  k_thomas_tables<<<dim3(cdiv(ncol, 128), nouter), 128>>>(ncol, nouter, n, c->ta, c->tb, c->tc, lamA, lamB, form3, c->c1, c->fac,
+                                                        c->conv);
   CK(cudaGetLastError());
   CK(cudaDeviceSynchronize());
   return 0;
@@ -1195,6 +1201,7 @@ int fen_ctx_destroy(fen_ctx* c) {
   for (float* b : fb) if (b) cudaFree(b);
   if (c->tmp64) cudaFree(c->tmp64);
   for (double* b : {c->rho, c->mu, c->p_o}) if (b) cudaFree(b);
+  if (c->conv) cudaFree(c->conv);
   for (auto& I : c->ibm) {
     void* bs[] = {I.idx, I.nidx, I.nn, I.w, I.c0, I.vs, I.fe};
     for (void* b : bs) if (b) cudaFree(b);

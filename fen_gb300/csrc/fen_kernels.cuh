@@ -607,14 +607,24 @@ __global__ void __launch_bounds__(256, 6) k_line_row32(LineArgs<float> a) {
 // right-hand-side recurrences.  FORM3 = the 3D solvers' reciprocal `factor` form, else the
 // 2D solvers' division form.  Arithmetic uses explicitly rounded operations (no FMA
 // contraction) so the zero-mode pivot cancels to exactly zero as in the reference.
+//
+// The interior rows share a, b and c, so each pivot is a function of the previous c1 alone;
+// in FP64 that recurrence reaches an exact fixed point after a few rows for all but the
+// lowest wavenumbers (channel 512 x 256 x 384: 11 rows on average, 43 at the 99th
+// percentile, 12 of 98688 systems never).  conv[sys] is the first row whose (c1, factor)
+// repeat the previous row's bit for bit; every later interior row then holds the same pair,
+// so a sweep reads the tables for rows below conv only and keeps the fixed point in
+// registers: the values used are the tabulated ones, and the results are unchanged.
 // ------------------------------------------------------------------------------------
 struct ThomasArgs {
   void* x;                    // spectral data (complex or real), in place
   long long s_col, s_row, s_outer;
   int ncol, nouter, n;
   const double* a;            // sub-diagonal a(row)
+  double aval;                // a(row) of rows 1 .. n-1 (all equal: 1/delta^2)
   const double* c1;           // [sys][row] forward coefficients
   const double* fac;          // [sys][row] reciprocal factor (FORM3) or divisor (2D form); last row: raw pivot
+  const int* conv;            // [sys] first interior row of the fixed point (n - 1: none)
   int form3;
   int split2;                 // complex data swept as two real systems: thread 2c + part, part 0 re / 1 im
 };
@@ -677,9 +687,9 @@ template <> __device__ __forceinline__ float tback<double, float>(double v) { re
 template <> __device__ __forceinline__ float2 tback<double2, float2>(double2 v) { return make_float2(narrow(v.x), narrow(v.y)); }
 
 // One system per thread.  The rows are swept in batches of kTB: the batch's right-hand
-// sides and table values are loaded first (independent loads, their latencies overlap),
-// then the batch's dependent elimination steps run in registers.  The arithmetic and its
-// order are the plain Thomas recurrence.
+// sides (and, below conv, its table values) are loaded first (independent loads, their
+// latencies overlap), then the batch's dependent elimination steps run in registers.  The
+// arithmetic and its order are the plain Thomas recurrence.
 constexpr int kTB = 8;
 
 template <typename VS, typename VC>
@@ -699,6 +709,11 @@ __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
   const double* f = a.fac + sys;
   const int n = a.n;
   const long long sr = a.s_row * w;
+  const double av = a.aval;
+  // the fixed point of the interior rows: rows >= T hold row T - 1's (c1, factor)
+  const int T = a.conv[sys];
+  const double ffix = f[(long long)(T - 1) * ns];
+  const double cfix = c1[(long long)(T - 1) * ns];
   // forward sweep: d1 overwrites the right-hand side
   VC d = tconv<VS, VC>(X[0]);
   d = a.form3 ? O::mul(d, f[0]) : O::div(d, f[0]);
@@ -706,16 +721,15 @@ __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
   int t = 1;
   for (; t + kTB <= n - 1; t += kTB) {
     VS xb[kTB];
-    double fb[kTB], ab[kTB];
+    double fb[kTB];
 #pragma unroll
     for (int q = 0; q < kTB; ++q) {
       xb[q] = X[(long long)(t + q) * sr];
-      fb[q] = f[(long long)(t + q) * ns];
-      ab[q] = a.a[t + q];
+      fb[q] = (t + q < T) ? f[(long long)(t + q) * ns] : ffix;
     }
 #pragma unroll
     for (int q = 0; q < kTB; ++q) {
-      VC r = O::sub_amul(tconv<VS, VC>(xb[q]), ab[q], d);
+      VC r = O::sub_amul(tconv<VS, VC>(xb[q]), av, d);
       d = a.form3 ? O::mul(r, fb[q]) : O::div(r, fb[q]);
       xb[q] = tback<VC, VS>(d);
     }
@@ -724,12 +738,13 @@ __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
   }
   for (; t < n - 1; ++t) {
     VC r = tconv<VS, VC>(X[(long long)t * sr]);
-    r = O::sub_amul(r, a.a[t], d);
-    d = a.form3 ? O::mul(r, f[t * ns]) : O::div(r, f[t * ns]);
+    r = O::sub_amul(r, av, d);
+    const double ft = (t < T) ? f[(long long)t * ns] : ffix;
+    d = a.form3 ? O::mul(r, ft) : O::div(r, ft);
     X[(long long)t * sr] = tback<VC, VS>(d);
   }
   {
-    const double piv = f[(n - 1) * ns];
+    const double piv = f[(long long)(n - 1) * ns];
     VC r = tconv<VS, VC>(X[(long long)(n - 1) * sr]);
     if (piv != 0.0) d = O::div(O::sub_amul(r, a.a[n - 1], d), piv);
     else d = O::zero();
@@ -744,7 +759,7 @@ __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
 #pragma unroll
     for (int q = 0; q < kTB; ++q) {
       xb[q] = X[(long long)(t - q) * sr];
-      cb[q] = c1[(long long)(t - q) * ns];
+      cb[q] = (t - q < T) ? c1[(long long)(t - q) * ns] : cfix;
     }
 #pragma unroll
     for (int q = 0; q < kTB; ++q) {
@@ -756,15 +771,16 @@ __global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
   }
   for (; t >= 0; --t) {
     VC dt = tconv<VS, VC>(X[(long long)t * sr]);
-    xn = O::sub_amul(dt, c1[t * ns], xn);
+    xn = O::sub_amul(dt, (t < T) ? c1[(long long)t * ns] : cfix, xn);
     X[(long long)t * sr] = tback<VC, VS>(xn);
   }
 }
 
 // Tabulate c1 and the row factors for every (col, outer) system with the reference's
-// operation order.  lamA indexed by col, lamB by outer (nullptr in 2D).
+// operation order, and the first interior row of their fixed point (conv, see k_thomas).
+// lamA indexed by col, lamB by outer (nullptr in 2D).
 static __global__ void k_thomas_tables(int ncol, int nouter, int n, const double* a, const double* b, const double* c,
-                                const double* lamA, const double* lamB, int form3, double* c1, double* fac) {
+                                const double* lamA, const double* lamB, int form3, double* c1, double* fac, int* conv) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   const int outer = blockIdx.y;
   if (col >= ncol) return;
@@ -774,6 +790,7 @@ static __global__ void k_thomas_tables(int ncol, int nouter, int n, const double
   double* F = fac + sys;
   const double mA = lamA[col];
   const double mB = lamB ? lamB[outer] : 0.0;
+  int T = n - 1;
   if (form3) {
     // factor = 1/(b + mwn_x + mwn_y - a*c1)   (poisson.f90:1096, 1105, 1114)
     double fct = __ddiv_rn(1.0, __dadd_rn(__dadd_rn(b[0], mA), mB));
@@ -783,6 +800,7 @@ static __global__ void k_thomas_tables(int ncol, int nouter, int n, const double
       fct = __ddiv_rn(1.0, __dsub_rn(__dadd_rn(__dadd_rn(b[t], mA), mB), __dmul_rn(a[t], C1[(t - 1) * ns])));
       C1[(t) * ns] = __dmul_rn(c[t], fct);
       F[(t) * ns] = fct;
+      if (T == n - 1 && C1[t * ns] == C1[(t - 1) * ns] && F[t * ns] == F[(t - 1) * ns]) T = t;
     }
     F[(n - 1) * ns] = __dsub_rn(__dadd_rn(__dadd_rn(b[n - 1], mA), mB), __dmul_rn(a[n - 1], C1[(n - 2) * ns]));
     C1[(n - 1) * ns] = 0.0;
@@ -793,10 +811,12 @@ static __global__ void k_thomas_tables(int ncol, int nouter, int n, const double
     for (int t = 1; t < n - 1; ++t) {
       C1[(t) * ns] = __ddiv_rn(c[t], __dadd_rn(__dsub_rn(b[t], __dmul_rn(a[t], C1[(t - 1) * ns])), mA));
       F[(t) * ns] = __dsub_rn(__dadd_rn(b[t], mA), __dmul_rn(a[t], C1[(t - 1) * ns]));
+      if (T == n - 1 && C1[t * ns] == C1[(t - 1) * ns] && F[t * ns] == F[(t - 1) * ns]) T = t;
     }
     F[(n - 1) * ns] = __dsub_rn(__dadd_rn(b[n - 1], mA), __dmul_rn(a[n - 1], C1[(n - 2) * ns]));
     C1[(n - 1) * ns] = 0.0;
   }
+  conv[sys] = T;
 }
 
 // ------------------------------------------------------------------------------------

@@ -13,8 +13,9 @@ from tests import cases as C
 
 pytestmark = pytest.mark.gpu
 
-# FP32 transforms: a single Poisson solve agrees with FP64 to about 1e-6 relative L2.
-RTOL_POISSON = 1e-5
+# FP32 transforms: a single Poisson solve agrees with the FP64 oracle to 1e-7 to 2e-7
+# relative L2 (measured on every solver); the form's bar is 1e-6.
+RTOL_POISSON = 1e-6
 
 
 def _solver(dim, n, L, bc, prec, **kw):
@@ -98,7 +99,7 @@ def test_mixed_channel_matches_fp64(fen_lib):
     e = _errors(s64, s32, 3)
     for fid in (F.U, F.V, F.W):
         assert e[fid] < 1e-6, e
-    assert e[F.P] < 1e-5, e
+    assert e[F.P] < 1e-6, e
 
 
 def test_mixed_partial_tiles_match_fp64(fen_lib):
@@ -125,7 +126,7 @@ def test_mixed_partial_tiles_match_fp64(fen_lib):
     e = _errors(s64, s32, 3)
     for fid in (F.U, F.V, F.W):
         assert e[fid] < 1e-6, e
-    assert e[F.P] < 1e-5, e
+    assert e[F.P] < 1e-6, e
 
 
 def test_mixed_2d_and_refinement(fen_lib):
