@@ -42,34 +42,86 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-# Algorithmic words per cell-step (FP64 words; 3D / 2D), the compulsory reads and writes of
-# each stage counted once, complex half-spectra as one real word per cell.
-WORDS_3D = {"predictor": 13, "forward": 4, "spectral": 6, "inverse": 9 - 7, "correct": 7, "ghost": 0, "checks": 0}
+# Algorithmic bytes per cell of each stage of one step: the compulsory reads and writes of
+# the stage counted once, a complex half-spectrum as one real word per cell; the Poisson
+# correction phi between the inverse transform and the correction is an intermediate of this
+# implementation and is not counted.  FP64 words: 13 + 4 + 6 + 1 + 8 = 32 (3D) and
+# 9 + 3 + 2 + 1 + 6 = 21 (2D).
 STAGES = ["predictor", "ghost_vstar", "forward_x", "spectral", "inverse_x", "correct", "ghost", "checks"]
-# bytes moved by each stage of this implementation per cell (FP64), used for the roofline
-STAGE_BYTES_3D = {
-    "predictor": 8 * 13,      # read u,v,w,p,dv_o(3); write v*(3), dv_o(3)
-    "forward_x": 8 * 4,       # read v*(3); write half-spectrum (16 B x 1/2 per cell)
-    "spectral": 8 * 6,        # y fwd, z fwd+solve+inv, y inv: 3 x (read + write) half-spectrum
-    "inverse_x": 8 * 2,       # read half-spectrum; write phi
-    "correct": 8 * 9,         # read v*(3), phi; read+write p; write v(3)
+STAGE_WORDS = {
+    3: {"predictor": 13,   # read u, v, w, p, dv_o(3); write v*(3), dv_o(3)
+        "forward_x": 4,    # read v*(3); write the half spectrum
+        "spectral": 6,     # y forward, z forward + solve + inverse, y inverse: 3 x (read + write)
+        "inverse_x": 1,    # read the half spectrum
+        "correct": 8},     # read v*(3), p; write v(3), p
+    2: {"predictor": 9, "forward_x": 3, "spectral": 2, "inverse_x": 1, "correct": 6},
+}
+# The mixed form keeps u, v, w, p, v* and dv_o as double-float pairs (8 B per value): its
+# predictor reads u, v, w, p, dv_o and writes v*, dv_o as pairs, 13 pair words = 104 B/cell.
+MIXED_PREDICTOR_BYTES = {3: 104, 2: 72}
+# ncu figures of one launch of the dominant kernel (the predictor), per cell: DRAM bytes read +
+# written and FP64 thread instructions, from `--set full` captures of the named case.
+NCU_PREDICTOR = {
+    "fp64": {"dram_bytes_per_cell": 99.6, "fp64_instr_per_cell": 72.0,
+             "source": "ncu --set full, k_predictor_tile, 3D TGV 192^3 FP64, one launch"},
+    "mixed": {"dram_bytes_per_cell": 100.4, "fp64_instr_per_cell": 0.0,
+              "source": "ncu --set full, k_predictor_df_tile, channel 256x128x192 mixed, one launch"},
 }
 
-# DRAM bytes per cell of one launch, measured with ncu (profiles/k_predictor_tile_tgv3d_192_fp64.md)
-TRAFFIC_BYTES_PER_CELL = {"predictor": 99.6}
-# FP64 thread instructions per cell of one launch (same capture: DADD + DMUL + DFMA)
-FP64_INSTR_PER_CELL = {"predictor": 72.0}
+
+def device_sms_and_clock():
+    """SM count of device 0 and its maximum SM clock in GHz (nvidia-smi; 2.07 if unreadable)."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    ghz = 2.07
+    try:
+        out = subprocess.run(["nvidia-smi", "-i", "0", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits"],
+                             capture_output=True, text=True, timeout=10)
+        ghz = float(out.stdout.strip().splitlines()[0]) / 1e3
+    except Exception:
+        pass
+    return sms, ghz
 
 
-def fp64_issue(kernel, cells, ms):
-    """Achieved FP64 instruction rate of `kernel` against the GB300 issue peak (2 FP64 thread
-    instructions per SM per cycle x 152 SMs x the maximum SM clock)."""
-    if kernel not in FP64_INSTR_PER_CELL or not ms:
+def fp64_issue(instr_per_cell, cells, ms, sms=152, ghz=2.07):
+    """Achieved FP64 instruction rate of a kernel with `instr_per_cell` FP64 thread
+    instructions per cell against the issue peak of 2 FP64 thread instructions per SM per
+    cycle (`sms` SMs at `ghz`)."""
+    if not instr_per_cell or not ms:
         return None
-    peak = 2 * 152 * 2.07e9 / 1e9
-    got = FP64_INSTR_PER_CELL[kernel] * cells / (ms / 1e3) / 1e9
+    peak = 2 * sms * ghz
+    got = instr_per_cell * cells / (ms / 1e3) / 1e9
     return {"achieved": round(got, 1), "peak": round(peak, 1), "unit": "G FP64 instr/s", "frac": round(got / peak, 4),
-            "instr_per_cell": FP64_INSTR_PER_CELL[kernel]}
+            "instr_per_cell": instr_per_cell}
+
+
+def roofline_block(dim, form, cells, stage_ms, peak, peak_kind, sms=152, ghz=2.07):
+    """Roofline of the dominant kernel, the predictor (the largest single kernel of the step in
+    both forms): algorithmic bytes per cell x cells / its CUDA-event time against the measured
+    HBM copy bandwidth; the whole step's algorithmic bytes beside it."""
+    words = STAGE_WORDS[dim]
+    bpc = 8 * words["predictor"] if form == "fp64" else MIXED_PREDICTOR_BYTES[dim]
+    ms = stage_ms["predictor"]
+    achieved = bpc * cells / (ms / 1e3) / 1e9
+    ncu = NCU_PREDICTOR[form]
+    tr = ncu["dram_bytes_per_cell"]
+    step_w = sum(words.values())
+    step_ms = sum(stage_ms.values())
+    out = {"bound": "hbm", "kernel": "k_predictor_tile" if form == "fp64" else "k_predictor_df_tile",
+           "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+           "traffic": int(tr * cells) if tr and dim == 3 else None, "peak_source": peak_kind,
+           "bytes_per_cell": bpc, "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
+           "step_algorithmic_bytes_per_cell": 8 * step_w if form == "fp64" else None,
+           "step_achieved_gbs": round(8 * step_w * cells / (step_ms / 1e3) / 1e9, 1) if form == "fp64" else None}
+    if tr:
+        out["traffic_source"] = ncu["source"] + f" ({tr} B/cell), scaled by cells"
+    if form == "fp64" and dim == 3:
+        out["fp64_issue"] = fp64_issue(ncu["fp64_instr_per_cell"], cells, ms, sms, ghz)
+        out["fp64_issue_source"] = ncu["source"]
+        out["note"] = "FP64 kernels are bound by FP64 issue on GB300, not by HBM"
+    return out
+
 
 CONFIGS = {
     "tgv3d": dict(dim=3, n=(256, 256, 256), L=(2 * np.pi,) * 3, nu=1.0 / 1600, cfl=0.5, constant_cfl=True,
@@ -248,6 +300,10 @@ def form_mixed(F, steps, scale=1):
         dt = s.set_timestep(start_velocity("channel", cfg))
         ms = s.time_steps(steps, dt)
         out[name] = round(cells * steps / (ms / 1e3) / 1e6, 3)
+        if name == "mixed":
+            peak, peak_kind = measured_peaks()
+            stage = dict(zip(STAGES, s.profile_step(3, s.status()["dt"])))
+            out["roofline"] = roofline_block(3, "mixed", cells, stage, peak, peak_kind)
         res = {k: s.get_field(fid)[1:-1, 1:-1, 1:-1] for k, fid in (("u", F.U), ("v", F.V), ("w", F.W), ("p", F.P))}
         if name == "fp64":
             ref = res
@@ -409,6 +465,9 @@ def main():
     ap.add_argument("--ensemble-runs", type=int, default=512)
     ap.add_argument("--ensemble-steps", type=int, default=2000)
     ap.add_argument("--ensemble-sizes", default="64,96,128,192,256")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="arithmetic form of the headline run (mixed: FP32 stencils/transforms, FP64 "
+                         "tridiagonal, zero mode, refinement residual and reductions)")
     args = ap.parse_args()
     cfg_name = args.config
     cfg = dict(CONFIGS[cfg_name])
@@ -449,7 +508,7 @@ def main():
     n, L = cfg["n"], cfg["L"]
     g = F.Grid(n[0], n[1], n[2], L[0], L[1], L[2], bc=cfg["bc"], dim=cfg["dim"], aniso=cfg.get("aniso", False))
     s = F.Solver(g, viscosity=cfg["nu"], g=cfg.get("g", (0, 0, 0)), CFL=cfg.get("cfl", 1.0),
-                 constant_CFL=cfg.get("constant_cfl", False))
+                 constant_CFL=cfg.get("constant_cfl", False), precision=F.MIXED if args.precision == "mixed" else F.FP64)
     fields = init_fields(cfg_name, cfg, n, g.shape)
     fid = {"u": F.U, "v": F.V, "w": F.W, "p": F.P}
     keys = [k for k in "uvwp" if k in fields]
@@ -491,20 +550,8 @@ def main():
     st = s.profile_step(3, s.status()["dt"])
     stage = dict(zip(STAGES, st))
     peak, peak_kind = measured_peaks()
-    dom = max(STAGE_BYTES_3D, key=lambda k: stage.get(k, 0) if k in stage else 0)
-    bpc = STAGE_BYTES_3D[dom] if cfg["dim"] == 3 else STAGE_BYTES_3D[dom] * 0.7
-    achieved = bpc * cells / (stage[dom] / 1e3) / 1e9
-    # DRAM bytes per launch of the predictor from ncu (110 B/cell at 192^3, scaled by cells)
-    traffic = TRAFFIC_BYTES_PER_CELL.get(dom)
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": int(traffic * cells) if traffic and cfg["dim"] == 3 else None,
-                "traffic_source": "ncu dram__bytes_read+write of one predictor launch at 192^3 (99.6 B/cell), scaled by cells",
-                "fp64_pipe_pct": 85.7, "peak_source": peak_kind,
-                # FP64 issue bound: instructions per cell of the tiled predictor (ncu, 192^3)
-                # against 2 FP64 thread instructions per SM per cycle (ncu peak_sustained)
-                "fp64_issue": fp64_issue(dom, cells, stage.get(dom)) if cfg["dim"] == 3 else None,
-                "bytes_per_cell": bpc, "stage_ms": {k: round(v, 4) for k, v in stage.items()},
-                "note": "FP64 kernels are FP64-issue-bound on GB300 (1.19 TFLOP/s FP64 measured)"}
+    sms, ghz = device_sms_and_clock()
+    roofline = roofline_block(cfg["dim"], args.precision, cells, stage, peak, peak_kind, sms, ghz)
 
     # ---- end to end through the C ABI with pinned host buffers ----
     host = {k: torch.from_numpy(np.ascontiguousarray(fields[k])).pin_memory() for k in keys}
@@ -533,10 +580,13 @@ def main():
     if rank == 0:
         line = {"metric": "Mcell-steps/s", "value": round(value, 3), "unit": "Mcell-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.precision == "fp64" else "f32 stencils/transforms + f64 solve/reductions",
                 "data": "synthetic",
-                "config": {"workload": cfg["desc"], "cells": cells, "grid": list(n),
-                           "flush": "inputs larger than L2 (fields 137 MB each)" if cells > 1e6 else "L2-resident",
+                "config": {"workload": cfg["desc"] if args.precision == "fp64" else cfg["desc"].replace("FP64", "mixed"),
+                           "cells": cells, "grid": list(n), "form": args.precision,
+                           "flush": f"inputs larger than L2 (fields {8 * int(np.prod(g.shape)) / 1e6:.0f} MB each)"
+                           if cells > 1e6 else "L2-resident",
                            "parallelism": f"replicas{world}"},
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "clocks": clk.summary()}
         if world == 1 and not args.no_cpu_baseline:

@@ -8,13 +8,12 @@ from the values already in the solver.
 import numpy as np
 import torch
 
-from . import FP64, P, U, V
+from . import U, V
 
 
 class Rollout(torch.autograd.Function):
     @staticmethod
     def forward(ctx, u0, v0, solver, nsteps, dt, every=50):
-        p0 = solver.get_field(P)
         solver.set_field(U, u0.detach().cpu().numpy())
         solver.set_field(V, v0.detach().cpu().numpy())
         solver.update_ghost_nodes(U)
@@ -23,7 +22,6 @@ class Rollout(torch.autograd.Function):
         solver.adjoint_setup(nsteps, every)
         solver.adjoint_forward(dt)
         ctx.solver = solver
-        ctx.p0 = p0
         uT = torch.from_numpy(solver.get_field(U))
         vT = torch.from_numpy(solver.get_field(V))
         return uT, vT
