@@ -79,6 +79,7 @@ _EXPORTS = [
     "fen_ensemble_adjoint_seed", "fen_ensemble_adjoint_backward", "fen_ensemble_adjoint_gradient",
     "fen_ensemble_adjoint_dts", "fen_set_split_pressure", "fen_set_ibm_forcing", "fen_get_ibm_force",
     "fen_upload_gl", "fen_download_gl", "fen_field_bounds", "fen_gradient", "fen_laplacian", "fen_add_advection",
+    "fen_save_state_mf", "fen_load_state_mf",
 ]
 
 
@@ -122,6 +123,8 @@ def load_library(path=None):
     L.fen_save_state.argtypes = [vp, ctypes.c_char_p]
     L.fen_load_state.argtypes = [vp, ctypes.c_char_p]
     L.fen_save_fields.argtypes = [vp, ctypes.c_char_p, ip]
+    L.fen_save_state_mf.argtypes = [vp, ctypes.c_char_p, dp]
+    L.fen_load_state_mf.argtypes = [vp, ctypes.c_char_p, dp]
     L.fen_adjoint_setup.argtypes = [vp, ip, ip]
     L.fen_set_split_pressure.argtypes = [vp, ctypes.c_double]
     cip_ = ctypes.POINTER(ctypes.c_int)
@@ -395,6 +398,23 @@ class Solver:
         path = path or os.path.join(directory, "state_%07d.raw" % step)
         self._check(self._L.fen_load_state(self._h, path.encode()))
         return path
+
+    def save_state_mf(self, step, vof, directory="data", path=None):
+        """save_state of FEN's multiphase build: the state file plus vof (the caller's interior
+        array), rho, mu and p_o; returns the path."""
+        path = path or os.path.join(directory, "state_%07d.raw" % step)
+        a = np.ascontiguousarray(vof, dtype=np.float64)
+        if a.shape != self.grid.interior_shape:
+            raise ValueError(f"vof shape {a.shape} != {self.grid.interior_shape}")
+        self._check(self._L.fen_save_state_mf(self._h, path.encode(), _dp(a)))
+        return path
+
+    def load_state_mf(self, step, directory="data", path=None):
+        """load_state of FEN's multiphase build; returns the volume fraction read."""
+        path = path or os.path.join(directory, "state_%07d.raw" % step)
+        vof = np.zeros(self.grid.interior_shape)
+        self._check(self._L.fen_load_state_mf(self._h, path.encode(), _dp(vof)))
+        return vof
 
     def save_fields(self, step, directory="data"):
         self._check(self._L.fen_save_fields(self._h, directory.encode(), int(step)))

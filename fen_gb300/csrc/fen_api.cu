@@ -438,7 +438,10 @@ int init_poisson(fen_ctx* c) {
   }
   const int nx = c->n[0], ny = c->n[1], nz = (c->dim == 3) ? c->n[2] : 1;
   const int h = nx / 2 + 1;
-  const long long hp = h;  // complex pitch along x
+  // complex pitch along x: the h = nx/2 + 1 half-spectrum columns padded to 64 bytes, so the
+  // column transforms and tridiagonal sweeps move whole 64-byte segments of every row
+  const int padc = c->mixed ? 8 : 4;
+  const long long hp = (h + padc - 1) / padc * padc;
   c->stages.clear();
   c->needs_mean = (s == S_PP || s == S_PN || s == S_PPN || s == S_PNP);
   c->mean_div = ffloat((long long)nx * ny * nz);
@@ -1814,6 +1817,57 @@ int fen_load_state(fen_ctx* c, const char* path) {
     return r;
   if (c->dim == 3 && (r = fen_update_ghost_nodes(c, FEN_W))) return r;
   return 0;
+}
+
+// save_state / load_state of FEN's multiphase build (solver.f90:203-208, 296-304): after the
+// fields above come vof (the caller's array), rho, mu and p_o.
+int fen_save_state_mf(fen_ctx* c, const char* path, const double* vof) {
+  if (!c || !path || !vof) return fail(FEN_ERR_ARG, "null argument");
+  if (c->mixed) return fail(FEN_ERR_ARG, "the variable-property path runs in FP64 contexts only");
+  int r;
+  if ((r = fen_save_state(c, path))) return r;
+  FILE* fp = fopen(path, "ab");
+  if (!fp) return fail(FEN_ERR_ARG, std::string("cannot open ") + path + ": " + strerror(errno));
+  const size_t cnt = host_count(c, 0);
+  std::vector<double> buf(cnt);
+  bool ok = fwrite(vof, sizeof(double), cnt, fp) == cnt;
+  for (int f : {FEN_RHO, FEN_MU, FEN_P_O}) {
+    if (!ok) break;
+    if (f == FEN_MU && c->dim == 3) {
+      // FEN's 3D step has no variable-viscosity branch: mu is the constant viscosity
+      std::fill(buf.begin(), buf.end(), c->prm.viscosity);
+    } else if ((r = interior_get(c, f, buf))) {
+      fclose(fp);
+      return r;
+    }
+    ok = fwrite(buf.data(), sizeof(double), cnt, fp) == cnt;
+  }
+  fclose(fp);
+  return ok ? 0 : fail(FEN_ERR_ARG, "short write");
+}
+
+int fen_load_state_mf(fen_ctx* c, const char* path, double* vof) {
+  if (!c || !path || !vof) return fail(FEN_ERR_ARG, "null argument");
+  if (c->mixed) return fail(FEN_ERR_ARG, "the variable-property path runs in FP64 contexts only");
+  int r;
+  if ((r = fen_load_state(c, path))) return r;
+  FILE* fp = fopen(path, "rb");
+  if (!fp) return fail(FEN_ERR_ARG, std::string("cannot open ") + path + ": " + strerror(errno));
+  const size_t cnt = host_count(c, 0);
+  const long skip = (long)(cnt * sizeof(double) * state_order(c).size());
+  std::vector<double> buf(cnt);
+  bool ok = fseek(fp, skip, SEEK_SET) == 0 && fread(vof, sizeof(double), cnt, fp) == cnt;
+  for (int f : {FEN_RHO, FEN_MU, FEN_P_O}) {
+    if (!ok) break;
+    ok = fread(buf.data(), sizeof(double), cnt, fp) == cnt;
+    if (!ok || (f == FEN_MU && c->dim == 3)) continue;
+    if ((r = interior_set(c, f, buf.data())) || (r = fen_update_ghost_nodes(c, f))) {
+      fclose(fp);
+      return r;
+    }
+  }
+  fclose(fp);
+  return ok ? 0 : fail(FEN_ERR_ARG, "state file too short for the multiphase fields");
 }
 
 int fen_save_fields(fen_ctx* c, const char* dir, int step) {

@@ -346,6 +346,13 @@ __device__ __forceinline__ T div_at(const LineArgs<T>& a, int i, int j, int k) {
   return d;
 }
 
+// Elements loaded per thread before the first of them is stored to shared memory in the
+// FP32 spectral loaders (memory-level parallelism of the load phase).
+#ifndef FEN_LINE_LB
+#define FEN_LINE_LB 4
+#endif
+constexpr int kLB = FEN_LINE_LB;
+
 template <typename T, int DIM, bool CONTIG, int OP, int LD, int ST>
 __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   typedef typename cpx<T>::t T2;
@@ -421,6 +428,38 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
       if (OP == OP_DCT2) r = (i & 1) ? (n - 1 - (i >> 1)) : (i >> 1);
       RS(l, r) = x;
     }
+  } else if (OP == OP_C2R && sizeof(T) == 4) {
+    // FP32 c2r: the same pre-processing with kLB elements (2 kLB loads) in flight per thread,
+    // all loads of a batch issued before the first use (the kernel is bound by load latency)
+    const int work = nl * M;
+    for (int t0 = tid; t0 < work; t0 += nth * kLB) {
+      T2 xk[kLB], xm[kLB];
+#pragma unroll
+      for (int b = 0; b < kLB; ++b) {
+        const int t = t0 + b * nth;
+        int l = 0, kk = 0;
+        if (t < work) {
+          if (CONTIG) divmod(t, fM, l, kk); else divmod(t, fL, kk, l);
+        }
+        if (t < work && l < nlv) {
+          const long long base = (long long)(line0 + l) * a.in_line + (long long)outer * a.in_outer;
+          xk[b] = inC[base + (long long)kk * a.in_pos];
+          xm[b] = inC[base + (long long)(M - kk) * a.in_pos];
+        } else {
+          xk[b] = mk<T2>(0, 0);
+          xm[b] = xk[b];
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < kLB; ++b) {
+        const int t = t0 + b * nth;
+        if (t < work) {
+          int l, kk;
+          if (CONTIG) divmod(t, fM, l, kk); else divmod(t, fL, kk, l);
+          S(l, kk) = (l < nlv) ? c2r_pre(xk[b], xm[b], M, kk, a.tw.wN) : mk<T2>(0, 0);
+        }
+      }
+    }
   } else if (OP == OP_C2R || OP == OP_DCT3) {
     // Hermitian half-spectrum X_0..X_M -> c2r pre-processed Z'_0..Z'_{M-1}
     const int work = nl * M;
@@ -448,14 +487,31 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
       }
       S(l, kk) = z;
     }
-  } else {  // complex in
+  } else {  // complex in: kLB loads in flight per thread (FP32; one in the FP64 kernels)
     const int work = nl * M;
-    for (int t = tid; t < work; t += nth) {
-      int l, p;
-      if (CONTIG) divmod(t, fM, l, p); else divmod(t, fL, p, l);
-      T2 z = mk<T2>(0, 0);
-      if (l < nlv) z = inC[(long long)(line0 + l) * a.in_line + (long long)p * a.in_pos + (long long)outer * a.in_outer];
-      S(l, p) = z;
+    constexpr int B = (sizeof(T) == 4) ? kLB : 1;
+    for (int t0 = tid; t0 < work; t0 += nth * B) {
+      T2 zb[B];
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int t = t0 + b * nth;
+        int l = 0, p = 0;
+        if (t < work) {
+          if (CONTIG) divmod(t, fM, l, p); else divmod(t, fL, p, l);
+        }
+        zb[b] = (t < work && l < nlv)
+                    ? inC[(long long)(line0 + l) * a.in_line + (long long)p * a.in_pos + (long long)outer * a.in_outer]
+                    : mk<T2>(0, 0);
+      }
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int t = t0 + b * nth;
+        if (t < work) {
+          int l, p;
+          if (CONTIG) divmod(t, fM, l, p); else divmod(t, fL, p, l);
+          S(l, p) = zb[b];
+        }
+      }
     }
   }
   __syncthreads();
@@ -692,8 +748,11 @@ template <> __device__ __forceinline__ float2 tback<double2, float2>(double2 v) 
 // arithmetic and its order are the plain Thomas recurrence.
 constexpr int kTB = 8;
 
+#ifndef FEN_THOMAS_MINB
+#define FEN_THOMAS_MINB 1
+#endif
 template <typename VS, typename VC>
-__global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
+__global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas(ThomasArgs a) {
   typedef ThomasOps<VC> O;
   const int tcol = blockIdx.x * blockDim.x + threadIdx.x;
   const int col = a.split2 ? (tcol >> 1) : tcol;

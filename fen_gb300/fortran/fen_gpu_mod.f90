@@ -174,6 +174,18 @@ module fen_gpu_mod
             type(c_ptr), value :: ctx
             character(kind=c_char), intent(in) :: path(*)
         end function fen_load_state
+        integer(c_int) function fen_save_state_mf(ctx, path, vof) bind(C, name='fen_save_state_mf')
+            import :: c_int, c_ptr, c_char, c_double
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)
+            real(c_double), intent(in) :: vof(*)
+        end function fen_save_state_mf
+        integer(c_int) function fen_load_state_mf(ctx, path, vof) bind(C, name='fen_load_state_mf')
+            import :: c_int, c_ptr, c_char, c_double
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)
+            real(c_double), intent(out) :: vof(*)
+        end function fen_load_state_mf
         integer(c_int) function fen_save_fields(ctx, dir, step) bind(C, name='fen_save_fields')
             import :: c_int, c_ptr, c_char
             type(c_ptr), value :: ctx

@@ -145,6 +145,15 @@ int fen_add_advection(fen_ctx* ctx, double* rhs_x, double* rhs_y, double* rhs_z)
  * ghost nodes of p and v.  FEN names the file data/state_<step:7>.raw. */
 int fen_save_state(fen_ctx* ctx, const char* path);
 int fen_load_state(fen_ctx* ctx, const char* path);
+/* The same files of FEN's multiphase build (-DMF, solver.f90:203-208, 296-304): the fields
+ * above followed by vof, rho, mu and p_o (FP64 contexts).  The volume fraction belongs to the
+ * caller (VoF advection stays with FEN): vof is its interior array f(1:nx, 1:ny, 1:nz),
+ * written as given and filled by the load.  rho, mu and p_o come from the device (their
+ * initial values density, viscosity and 0 when never uploaded); the load uploads them, which
+ * puts the context on the variable-property path, and refreshes their ghosts.  In 3D FEN has
+ * no variable-viscosity branch: mu is written as the constant viscosity and not read back. */
+int fen_save_state_mf(fen_ctx* ctx, const char* path, const double* vof);
+int fen_load_state_mf(fen_ctx* ctx, const char* path, double* vof);
 /* save_fields (src/solver.f90:103-156): <dir>/vx_<step:7>.raw, vy_, [vz_], p_ with the
  * velocity interpolated to cell centres (face_to_center, src/fields.f90:210-252). */
 int fen_save_fields(fen_ctx* ctx, const char* dir, int step);

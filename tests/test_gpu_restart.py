@@ -74,3 +74,53 @@ def test_save_fields_layout(fen_lib, tmp_path):
     assert np.allclose(vx, 0.5 * (ufull[1:-1, 1:-1] + ufull[1:-1, :-2]), rtol=0, atol=1e-15)
     pr = np.fromfile(tmp_path / "p_0000003.raw").reshape(N, N)
     assert np.array_equal(pr, s.get_field(F.P)[1, 1:-1, 1:-1])
+
+
+def test_multiphase_state_file(fen_lib, tmp_path):
+    # FEN's -DMF state file (solver.f90:203-208, 296-304): p, u, v, dv_o%x, dv_o%y, vof, rho,
+    # mu, p_o; a restart with variable density and viscosity and the split pressure is
+    # bitwise, and vof (the caller's array) comes back as written
+    N, L = 32, 2 * np.pi
+    g = F.Grid(N, N, 1, L, L, L / N)
+    rng = np.random.Generator(np.random.PCG64(12))
+    u, v, p = C.tgv2d_fields(N, L)
+    x = (np.arange(N + 2) - 0.5) * L / N
+    X, Y = np.meshgrid(x, x)
+    rho = np.zeros((3, N + 2, N + 2))
+    mu = np.zeros((3, N + 2, N + 2))
+    rho[1] = 1.0 + 0.4 * (1 + np.sin(X) * np.cos(2 * Y))
+    mu[1] = 0.02 * (1.0 + 0.3 * np.cos(X + Y) ** 2)
+    vof = rng.uniform(0, 1, g.interior_shape)
+
+    def make():
+        s = F.Solver(g, viscosity=0.02)
+        for fid, a in ((F.U, u), (F.V, v), (F.P, p), (F.RHO, rho), (F.MU, mu)):
+            s.set_field(fid, a)
+            s.update_ghost_nodes(fid)
+        s.set_split_pressure(1.0)
+        s.set_dt_o(1e-3)
+        return s
+
+    s = make()
+    for step in range(1, 11):
+        s.advance_solution(step, 1e-3)
+        if step == 5:
+            s.save_state_mf(step, vof, str(tmp_path))
+    full = s.save_state_mf(10, vof, str(tmp_path))
+    data = np.fromfile(full)
+    assert data.size == 9 * N * N
+    seg = lambda q: data[q * N * N:(q + 1) * N * N].reshape(N, N)
+    assert np.array_equal(seg(0), s.get_field(F.P)[1, 1:-1, 1:-1])
+    assert np.array_equal(seg(5), vof[0])
+    assert np.array_equal(seg(6), rho[1, 1:-1, 1:-1])
+    assert np.array_equal(seg(7), mu[1, 1:-1, 1:-1])
+    assert np.array_equal(seg(8), s.get_field(F.P_O)[1, 1:-1, 1:-1])
+    r = F.Solver(g, viscosity=0.02)
+    r.set_split_pressure(1.0)
+    r.set_dt_o(1e-3)
+    back = r.load_state_mf(5, str(tmp_path))
+    assert np.array_equal(back, vof)
+    for step in range(6, 11):
+        r.advance_solution(step, 1e-3)
+    again = np.fromfile(r.save_state_mf(20, vof, str(tmp_path)))
+    assert np.array_equal(data, again)
