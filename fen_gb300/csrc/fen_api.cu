@@ -110,6 +110,7 @@ struct fen_ctx {
   float* dphi32 = nullptr;  // refinement: correction of phi
   float *dv32h = nullptr, *dv32l = nullptr;  // refinement: pair divergence of v* from the first transform
   int refine = 0;
+  int phi_offset = 0;  // phi32 still holds its mean (deferred_mean) until the next download
   float* d32[3] = {nullptr, nullptr, nullptr};
   float* dvo32[3] = {nullptr, nullptr, nullptr};
   float* d32l[3] = {nullptr, nullptr, nullptr};    // v* lo (pairs with d32)
@@ -752,6 +753,10 @@ double rhof_of(fen_ctx* c) { return 0.5 * (c->prm.density + c->prm.density); }
 // uploaded or the split pressure is on.
 bool var_path(const fen_ctx* c) { return c->var_rho || c->var_mu || c->split; }
 
+// Mixed form with refinement: the step keeps the mean of phi (removed in the correction's
+// pressure update instead of by a separate pass over phi).
+bool deferred_mean(const fen_ctx* c) { return c->mixed && c->refine && c->needs_mean; }
+
 // Density of the Poisson scaling rho_over_dt: 1 with a density field (the loader multiplies
 // by rho(i,j,k)), rhomin with the split, else the constant density.
 double rho_scale(const fen_ctx* c) { return c->split ? c->rhomin : (c->var_rho ? 1.0 : c->prm.density); }
@@ -995,7 +1000,16 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
       if (q == 0) mark();       // 3: first (fused divergence) transform
       if (q + 2 == ns) mark();  // 4: spectral middle stages
     }
-    if (c->needs_mean && (r = launch_mean(c))) return r;
+    if (deferred_mean(c)) {
+      // the mean of phi is removed where phi enters p (k_correct_df); the gradient and the
+      // refinement's residual do not see it
+      k_mean_reduce<<<1, 1024, 0, c->stream>>>(c->partial, c->npartial, c->mean_div, c->sc);
+      k_keep_mean<<<1, 1, 0, c->stream>>>(c->sc, 0);
+      c->launches += 2;
+      CK(cudaGetLastError());
+    } else if (c->needs_mean && (r = launch_mean(c))) {
+      return r;
+    }
   }
   mark();  // 5: inverse x transform (+ mean)
   if (c->mixed) {
@@ -1022,6 +1036,7 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
     ca.dul = c->d32l[0]; ca.dvl = c->d32l[1]; ca.dwl = c->d32l[2];
     ca.dphi = c->refine ? c->dphi32 : nullptr;
     ca.dphi_mean = c->refine && c->needs_mean;
+    ca.phi_mean = deferred_mean(c);
     ca.u = DFFieldW{c->u32, c->u32l}; ca.v = DFFieldW{c->v32, c->v32l};
     ca.w = DFFieldW{c->w32, c->w32l}; ca.p = DFFieldW{c->p32, c->p32l};
     for (int q = 0; q < 3; ++q) ca.id[q] = 1.0 / c->d[q];
@@ -1147,6 +1162,7 @@ int pre_step(fen_ctx* c, double dt) {
     if ((r = launch_checks(c, 0))) return r;
   }
   c->vel_dirty = 0;
+  if (deferred_mean(c)) c->phi_offset = 1;
   return 0;
 }
 
@@ -1378,7 +1394,10 @@ int fen_upload_gl(fen_ctx* c, int f, const double* host, int gl) {
     CK(cudaStreamSynchronize(c->stream));
     return 0;
   }
-  if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, hrw, 0, gl) : relayout<double>(c, c->phi, hrw, 0, gl);
+  if (f == FEN_PHI) {
+    c->phi_offset = 0;
+    return c->mixed ? relayout<float>(c, c->phi32, hrw, 0, gl) : relayout<double>(c, c->phi, hrw, 0, gl);
+  }
   double* d = (f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p;
   if (c->mixed && gl == 0 && (r = pair_convert(c, f, 1))) return r;  // keep the device ghosts
   if ((r = relayout<double>(c, d, hrw, 0, gl))) return r;
@@ -1412,6 +1431,21 @@ int fen_download_gl(fen_ctx* c, int f, double* host, int gl) {
     c->launches++;
     CK(cudaGetLastError());
     return relayout<double>(c, c->tmp64, host, 1, gl);
+  }
+  if (f == FEN_PHI && c->mixed && c->phi_offset) {
+    // the last step left the mean of phi in place: remove it and refill the ghosts
+    const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+    const int grid = std::min(cdiv(ncell, 256), 152 * 8);
+    k_keep_mean<<<1, 1, 0, c->stream>>>(c->sc, 1);
+    if (c->dim == 3) k_mean_subtract<float, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, c->phi32);
+    else k_mean_subtract<float, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, c->phi32);
+    c->launches += 2;
+    CK(cudaGetLastError());
+    float* pf[1] = {c->phi32};
+    int ids[1] = {FEN_PHI};
+    int r;
+    if ((r = ghost<float>(c, 1, pf, ids))) return r;
+    c->phi_offset = 0;
   }
   if (f == FEN_PHI) return c->mixed ? relayout<float>(c, c->phi32, host, 1, gl) : relayout<double>(c, c->phi, host, 1, gl);
   double* d = (f == FEN_U) ? c->u : (f == FEN_V) ? c->v : (f == FEN_W) ? c->w : c->p;
@@ -1574,6 +1608,7 @@ int fen_solve_poisson(fen_ctx* c) {
   if (!c) return fail(FEN_ERR_ARG, "null argument");
   int r;
   if ((r = run_poisson(c, true))) return r;
+  c->phi_offset = 0;  // the solve removes the mean itself
   CK(cudaStreamSynchronize(c->stream));
   return 0;
 }

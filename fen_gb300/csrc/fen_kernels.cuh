@@ -748,8 +748,11 @@ template <> __device__ __forceinline__ float2 tback<double2, float2>(double2 v) 
 // arithmetic and its order are the plain Thomas recurrence.
 constexpr int kTB = 8;
 
+// Resident 128-thread CTAs per SM the sweep is compiled for: 8 (64 registers) keeps more
+// systems in flight than the compiler's 116-register choice (mixed channel 512x256x384:
+// spectral stage 0.77 -> 0.75 ms; 6 CTAs 0.76 ms).
 #ifndef FEN_THOMAS_MINB
-#define FEN_THOMAS_MINB 1
+#define FEN_THOMAS_MINB 8
 #endif
 template <typename VS, typename VC>
 __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas(ThomasArgs a) {
@@ -929,6 +932,13 @@ static __global__ void __launch_bounds__(1024) k_mean_reduce(const double* __res
     __syncthreads();
   }
   if (threadIdx.x == 0) sc->mean = red[0] / ncell_f;
+}
+
+// Keep the mean of phi for the mixed form's correction (dir 0: mean_phi = mean), or bring it
+// back for an explicit removal (dir 1: mean = mean_phi).
+static __global__ void k_keep_mean(StepScalars* sc, int dir) {
+  if (dir == 0) sc->mean_phi = sc->mean;
+  else sc->mean = sc->mean_phi;
 }
 
 template <typename T, int DIM>

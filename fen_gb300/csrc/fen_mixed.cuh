@@ -408,6 +408,7 @@ struct CorrDFArgs {
   const float *dul, *dvl, *dwl;     // v* lo
   const float* dphi;  // refinement correction of phi (or null)
   int dphi_mean;      // subtract the mean of dphi (sc->mean) in the pressure update
+  int phi_mean;       // subtract the mean of phi (sc->mean_phi) in the pressure update
   DFFieldW u, v, w, p;
   double id[3];
   int iso;
@@ -421,8 +422,10 @@ __global__ void __launch_bounds__(256) k_correct_df(Layout L, const StepScalars*
   const float idx = (float)a.id[0];
   const float idy = a.iso ? idx : (float)a.id[1];
   const float idz = a.iso ? idx : (float)a.id[2];
-  // the mean of dphi leaves its gradient unchanged; it is removed only where dphi enters p
+  // the means of phi and dphi leave their gradients unchanged; they are removed only where
+  // they enter p (the mean removal of the Poisson solve, poisson.f90:491-503, fused here)
   const float qm = a.dphi_mean ? (float)sc->mean : 0.0f;
+  const float pm = a.phi_mean ? (float)sc->mean_phi : 0.0f;
   CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
   for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
     const int i = 1 + cw.i, j = 1 + cw.j, k = 1 + cw.k;
@@ -450,7 +453,7 @@ __global__ void __launch_bounds__(256) k_correct_df(Layout L, const StepScalars*
     }
     float hi, lo;
     hi = a.p.hi[c]; lo = a.p.lo[c];
-    df_add(hi, lo, ph);
+    df_add(hi, lo, a.phi_mean ? ph - pm : ph);
     if (q) df_add(hi, lo, qh - qm);
     a.p.hi[c] = hi; a.p.lo[c] = lo;
   }

@@ -97,6 +97,7 @@ struct StepScalars {
   double maxvel;            // max(|u|+|v|+|w|) of the current velocity (:599-611)
   double maxdiv, maxCFL;    // checks (:570-619)
   double mean;              // Poisson mean removal (poisson.f90:491-503)
+  double mean_phi;          // mixed form with refinement: mean of phi, removed where phi enters p
   double dt_visc, dt_conv;
   int err;                  // NaN detected in the reductions
   int pad;
