@@ -79,7 +79,7 @@ _EXPORTS = [
     "fen_ensemble_adjoint_seed", "fen_ensemble_adjoint_backward", "fen_ensemble_adjoint_gradient",
     "fen_ensemble_adjoint_dts", "fen_set_split_pressure", "fen_set_ibm_forcing", "fen_get_ibm_force",
     "fen_upload_gl", "fen_download_gl", "fen_field_bounds", "fen_gradient", "fen_laplacian", "fen_add_advection",
-    "fen_save_state_mf", "fen_load_state_mf",
+    "fen_save_state_mf", "fen_load_state_mf", "fen_adjoint_backward3",
 ]
 
 
@@ -132,6 +132,7 @@ def load_library(path=None):
     L.fen_get_ibm_force.argtypes = [vp, ip, dp]
     L.fen_adjoint_forward.argtypes = [vp, ctypes.c_double]
     L.fen_adjoint_backward.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.fen_adjoint_backward3.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp]
     cip = ctypes.POINTER(ctypes.c_int)
     L.fen_ensemble_create.argtypes = [ctypes.c_int, cip, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_int, ctypes.POINTER(vp)]
@@ -449,7 +450,7 @@ class Solver:
             self._check(self._L.fen_get_ibm_force(self._h, int(comp), _dp(out)))
         return out
 
-    # -- discrete adjoint (2D periodic FP64) ------------------------------------------------
+    # -- discrete adjoint (FP64; periodic, or walls in y) ------------------------------------
     def adjoint_setup(self, nsteps, every):
         self._check(self._L.fen_adjoint_setup(self._h, int(nsteps), int(every)))
 
@@ -457,14 +458,17 @@ class Solver:
         """Run the configured rollout from the current state, keeping checkpoints."""
         self._check(self._L.fen_adjoint_forward(self._h, float(dt)))
 
-    def adjoint_backward(self, lam_u, lam_v):
-        """Gradient w.r.t. the initial (u, v) of a loss with sensitivity (lam_u, lam_v) to
-        the final (u, v).  Returns (g_u, g_v, times_ms) with times = (backward, forward)."""
+    def adjoint_backward(self, lam_u, lam_v, lam_w=None):
+        """Gradient w.r.t. the initial velocity of a loss with sensitivity (lam_u, lam_v[,
+        lam_w]) to the final velocity (ghosted arrays).  Returns (g_u, g_v, times_ms) in 2D and
+        (g_u, g_v, g_w, times_ms) in 3D, times = (backward, forward) in ms."""
         lu = np.ascontiguousarray(lam_u, dtype=np.float64)
         lv = np.ascontiguousarray(lam_v, dtype=np.float64)
-        gu, gv, ms = self.zeros(), self.zeros(), np.zeros(2)
-        self._check(self._L.fen_adjoint_backward(self._h, _dp(lu), _dp(lv), _dp(gu), _dp(gv), _dp(ms)))
-        return gu, gv, ms
+        d3 = self.grid.dim == 3
+        lw = np.ascontiguousarray(lam_w if lam_w is not None else self.zeros(), dtype=np.float64)
+        gu, gv, gw, ms = self.zeros(), self.zeros(), self.zeros(), np.zeros(2)
+        self._check(self._L.fen_adjoint_backward3(self._h, _dp(lu), _dp(lv), _dp(lw), _dp(gu), _dp(gv), _dp(gw), _dp(ms)))
+        return (gu, gv, gw, ms) if d3 else (gu, gv, ms)
 
     # -- measurement -------------------------------------------------------------------------
     def kernel_launches(self):

@@ -165,12 +165,13 @@ struct fen_ctx {
   double* util = nullptr;           // fields_mod operators: 3 interior arrays + one FP64 field
   // discrete adjoint (2D periodic FP64): checkpoints, recomputed step inputs, adjoint fields
   struct Adjoint {
-    int nsteps = 0, every = 0, nckpt = 0;
+    int nsteps = 0, every = 0, nckpt = 0, nf = 0, nv = 0;
     double dt = 0;
-    std::vector<double*> ckpt;    // nckpt+1 checkpoints x 5 fields (u, v, p, dv_o x, dv_o y)
-    std::vector<double*> inputs;  // every x 2 fields (u, v at the start of each step)
-    double *uh = nullptr, *vh = nullptr, *ph = nullptr, *dou = nullptr, *dov = nullptr;
-    double *fh = nullptr, *bh = nullptr, *ush = nullptr, *vsh = nullptr, *dhu = nullptr, *dhv = nullptr;
+    std::vector<double*> ckpt;    // nckpt+1 checkpoints x nf fields (u, v, [w,] p, dv_o x, y[, z])
+    std::vector<double*> inputs;  // every x nv fields (the velocity at the start of each step)
+    double *uh = nullptr, *vh = nullptr, *wh = nullptr, *ph = nullptr, *dou = nullptr, *dov = nullptr, *dow = nullptr;
+    double *fh = nullptr, *bh = nullptr, *ush = nullptr, *vsh = nullptr, *wsh = nullptr;
+    double *dhu = nullptr, *dhv = nullptr, *dhw = nullptr, *part = nullptr;
     double fwd_ms = 0, bwd_ms = 0;
     bool ready = false;
   } adj;
@@ -665,15 +666,20 @@ int launch_thomas(fen_ctx* c, const Stage& s) {
   ThomasArgs ta = s.ta;
   ta.split2 = 0;
   constexpr int kTh = 128;  // (64-thread CTAs measured no faster)
+  // the mixed form's reciprocal-factor (3D) solves take the two-FMA sweep above the pivots'
+  // fixed point; the FP64 form keeps the reference's operation order
+  const bool fast = c->mixed && ta.form3;
   if (real) {
     const dim3 g(cdiv(ta.ncol, kTh), s.tgrid.y, s.tgrid.z);
-    if (c->mixed) k_thomas<float, double><<<g, kTh, 0, c->stream>>>(ta);
+    if (fast) k_thomas_mixed<0><<<g, kTh, 0, c->stream>>>(ta);
+    else if (c->mixed) k_thomas<float, double><<<g, kTh, 0, c->stream>>>(ta);
     else k_thomas<double, double><<<g, kTh, 0, c->stream>>>(ta);
   } else {
     // complex right-hand sides: real and imaginary parts as two real systems per column
     ta.split2 = 1;
     const dim3 g(cdiv(2LL * ta.ncol, kTh), s.tgrid.y, s.tgrid.z);
-    if (c->mixed) k_thomas<float, double><<<g, kTh, 0, c->stream>>>(ta);
+    if (fast) k_thomas_mixed<1><<<g, kTh, 0, c->stream>>>(ta);
+    else if (c->mixed) k_thomas<float, double><<<g, kTh, 0, c->stream>>>(ta);
     else k_thomas<double, double><<<g, kTh, 0, c->stream>>>(ta);
   }
   c->launches++;
@@ -1235,8 +1241,8 @@ int fen_ctx_destroy(fen_ctx* c) {
   if (c->sc_host) cudaFreeHost(c->sc_host);
   for (double* b : c->adj.ckpt) if (b) cudaFree(b);
   for (double* b : c->adj.inputs) if (b) cudaFree(b);
-  double* ab[] = {c->adj.uh, c->adj.vh, c->adj.ph, c->adj.dou, c->adj.dov, c->adj.fh, c->adj.bh, c->adj.ush,
-                  c->adj.vsh, c->adj.dhu, c->adj.dhv};
+  double* ab[] = {c->adj.uh, c->adj.vh, c->adj.wh, c->adj.ph, c->adj.dou, c->adj.dov, c->adj.dow, c->adj.fh,
+                  c->adj.bh, c->adj.ush, c->adj.vsh, c->adj.wsh, c->adj.dhu, c->adj.dhv, c->adj.dhw, c->adj.part};
   for (double* b : ab) if (b) cudaFree(b);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -1939,77 +1945,116 @@ int fen_save_fields(fen_ctx* c, const char* dir, int step) {
 
 // ---- discrete adjoint (fen_adjoint.cuh) ------------------------------------------------
 namespace {
+constexpr int kAdjParts = 152 * 4;  // CTAs of the adjoint mean reduction
+
 int adj_copy(fen_ctx* c, double* dst, const double* src) {
   CK(cudaMemcpyAsync(dst, src, c->L.total * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
   return 0;
 }
 
+// The state a checkpoint holds: u, v, [w,] p, dv_o.
+std::vector<double*> adj_state(fen_ctx* c) {
+  if (c->dim == 3) return {c->u, c->v, c->w, c->p, c->dvo[0], c->dvo[1], c->dvo[2]};
+  return {c->u, c->v, c->p, c->dvo[0], c->dvo[1]};
+}
+
 int adj_save(fen_ctx* c, int q) {
-  double* src[5] = {c->u, c->v, c->p, c->dvo[0], c->dvo[1]};
-  for (int f = 0; f < 5; ++f) {
+  const auto src = adj_state(c);
+  for (size_t f = 0; f < src.size(); ++f) {
     int r;
-    if ((r = adj_copy(c, c->adj.ckpt[5 * q + f], src[f]))) return r;
+    if ((r = adj_copy(c, c->adj.ckpt[c->adj.nf * q + f], src[f]))) return r;
   }
   return 0;
 }
 
 int adj_restore(fen_ctx* c, int q) {
-  double* dst[5] = {c->u, c->v, c->p, c->dvo[0], c->dvo[1]};
-  for (int f = 0; f < 5; ++f) {
+  const auto dst = adj_state(c);
+  for (size_t f = 0; f < dst.size(); ++f) {
     int r;
-    if ((r = adj_copy(c, dst[f], c->adj.ckpt[5 * q + f]))) return r;
+    if ((r = adj_copy(c, dst[f], c->adj.ckpt[c->adj.nf * q + f]))) return r;
   }
   return 0;
 }
 
-// Periodic ghost fill of adjoint fields (copies, so the stencils gather wrapped values).
-int adj_ghost(fen_ctx* c, double* a, double* b) {
-  double* f[2] = {a, b};
-  int ids[2] = {FEN_U, FEN_V};
-  return b ? ghost<double>(c, 2, f, ids) : ghost<double>(c, 1, f, ids + 0);
+// Walls in y (pn, pnp), else periodic on every axis.
+bool adj_walls(const fen_ctx* c) { return c->solver == S_PN || c->solver == S_PNP; }
+
+// Ghosts of adjoint fields: periodic copies, zeros across the walls.
+int adj_ghost(fen_ctx* c, std::initializer_list<double*> fs) {
+  const int wall = adj_walls(c) ? 1 : 0;
+  for (double* f : fs) {
+    if (!f) continue;
+    for (int ax = 0; ax < c->dim; ++ax) {
+      const long long n = 2LL * ((ax == 0) ? c->n[1] + 2 : c->n[0] + 2) * (c->dim == 3 ? ((ax == 2) ? c->n[1] + 2 : c->n[2] + 2) : 1);
+      const int g = std::min(cdiv(n, 256), 152 * 8);
+      const int zero = (ax == 1) ? wall : 0;
+      if (c->dim == 3) k_adj_ghost<3><<<g, 256, 0, c->stream>>>(c->L, f, ax, zero);
+      else k_adj_ghost<2><<<g, 256, 0, c->stream>>>(c->L, f, ax, zero);
+      c->launches++;
+    }
+  }
+  CK(cudaGetLastError());
+  return 0;
 }
 
-// One adjoint step with the stored forward input (u, v) of that step.
-int adj_step(fen_ctx* c, const double* u, const double* v) {
+AdjScales adj_scales(const fen_ctx* c) {
+  AdjScales q;
+  for (int a = 0; a < 3; ++a) {
+    q.id[a] = 1.0 / c->d[a];
+    q.id2[a] = 1.0 / (c->d[a] * c->d[a]);
+  }
+  return q;
+}
+
+// One adjoint step with the stored forward input velocity (u, v, w) of that step.
+int adj_step(fen_ctx* c, const double* u, const double* v, const double* w) {
   auto& A = c->adj;
   int r;
-  const int grid = std::min(cdiv((long long)c->n[0] * c->n[1], 256), 152 * 16);
-  const double idx = 1.0 / c->d[0], idy = 1.0 / c->d[1];
+  const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
+  const int grid = std::min(cdiv(ncell, 256), 152 * 16);
+  const AdjScales q = adj_scales(c);
   const double rhof = rhof_of(c), rho = c->prm.density, dt = A.dt;
   const double Acoef = 1.0 + 0.5 * dt / c->sc_host->dt_o, Bcoef = -0.5 * dt / c->sc_host->dt_o;
+  const int wall = adj_walls(c) ? 1 : 0;
+  const bool d3 = (c->dim == 3);
+#define ADJ_LAUNCH(kern, ...) \
+  do { if (d3) kern<3><<<grid, 256, 0, c->stream>>>(__VA_ARGS__); else kern<2><<<grid, 256, 0, c->stream>>>(__VA_ARGS__); c->launches++; } while (0)
   // phi^ = p'^ + dt/rhof D v'^
-  if ((r = adj_ghost(c, A.uh, A.vh))) return r;
-  k_adj_div2<<<grid, 256, 0, c->stream>>>(c->L, A.ph, A.uh, A.vh, dt / rhof, idx, idy, A.fh);
-  c->launches++;
+  if ((r = adj_ghost(c, {A.uh, A.vh, d3 ? A.wh : nullptr}))) return r;
+  ADJ_LAUNCH(k_adj_div, c->L, A.ph, A.uh, A.vh, A.wh, dt / rhof, q, A.fh);
+  if (wall) {
+    // b^ = P (phi^ - <phi^>): the walls' solve is symmetric on mean-free right-hand sides
+    const int gp = kAdjParts;
+    if (d3) k_adj_sum<3><<<gp, 256, 0, c->stream>>>(c->L, A.fh, A.part);
+    else k_adj_sum<2><<<gp, 256, 0, c->stream>>>(c->L, A.fh, A.part);
+    k_mean_reduce<<<1, 1024, 0, c->stream>>>(A.part, gp, (double)ncell, c->sc);
+    if (d3) k_mean_subtract<double, 3><<<grid, 256, 0, c->stream>>>(c->L, c->sc, A.fh);
+    else k_mean_subtract<double, 2><<<grid, 256, 0, c->stream>>>(c->L, c->sc, A.fh);
+    c->launches += 3;
+  }
   // b^ = P phi^ (the forward's Poisson plan, loaded from phi^, written to b^)
-  for (size_t q = 0; q < c->stages.size(); ++q)
-    if ((r = launch_stage(c, c->stages[q], q == 0, A.fh, A.bh))) return r;
+  for (size_t s = 0; s < c->stages.size(); ++s)
+    if ((r = launch_stage(c, c->stages[s], s == 0, A.fh, A.bh))) return r;
   if (c->needs_mean) {
-    const int g2 = std::min(cdiv((long long)c->n[0] * c->n[1], 256), 152 * 8);
+    const int g2 = std::min(cdiv(ncell, 256), 152 * 8);
     k_mean_reduce<<<1, 1024, 0, c->stream>>>(c->partial, c->npartial, c->mean_div, c->sc);
-    k_mean_subtract<double, 2><<<g2, 256, 0, c->stream>>>(c->L, c->sc, A.bh);
+    if (d3) k_mean_subtract<double, 3><<<g2, 256, 0, c->stream>>>(c->L, c->sc, A.bh);
+    else k_mean_subtract<double, 2><<<g2, 256, 0, c->stream>>>(c->L, c->sc, A.bh);
     c->launches += 2;
   }
-  {
-    double* f[1] = {A.bh};
-    int ids[1] = {FEN_PHI};
-    if ((r = ghost<double>(c, 1, f, ids))) return r;
-  }
-  // v*^ = v'^ - rho/dt G b^
-  k_adj_grad2<<<grid, 256, 0, c->stream>>>(c->L, A.uh, A.vh, A.bh, rho / dt, idx, idy, A.ush, A.vsh);
-  c->launches++;
+  if ((r = adj_ghost(c, {A.bh}))) return r;
+  // v*^ = E^T (v'^ - rho/dt G b^)
+  ADJ_LAUNCH(k_adj_grad, c->L, A.uh, A.vh, A.wh, A.bh, rho / dt, q, wall, A.ush, A.vsh, A.wsh);
   // p^ = p'^ + dt/rhof D v*^
-  if ((r = adj_ghost(c, A.ush, A.vsh))) return r;
-  k_adj_div2<<<grid, 256, 0, c->stream>>>(c->L, A.ph, A.ush, A.vsh, dt / rhof, idx, idy, A.ph);
-  c->launches++;
+  if ((r = adj_ghost(c, {A.ush, A.vsh, d3 ? A.wsh : nullptr}))) return r;
+  ADJ_LAUNCH(k_adj_div, c->L, A.ph, A.ush, A.vsh, A.wsh, dt / rhof, q, A.ph);
   // dv^ = dv_o'^ + dt A v*^, dv_o^ = dt B v*^
-  k_adj_dv2<<<grid, 256, 0, c->stream>>>(c->L, A.ush, A.vsh, A.dou, A.dov, dt * Acoef, dt * Bcoef, A.dhu, A.dhv);
-  c->launches++;
-  // v^ = v*^ + N'^T dv^ + mu/rhof L dv^
-  if ((r = adj_ghost(c, A.dhu, A.dhv))) return r;
-  k_adj_state2<<<grid, 256, 0, c->stream>>>(c->L, u, v, A.ush, A.vsh, A.dhu, A.dhv, idx, idy, idx * idx, idy * idy,
-                                           c->prm.viscosity / rhof, A.uh, A.vh);
-  c->launches++;
+  ADJ_LAUNCH(k_adj_dv, c->L, A.ush, A.vsh, A.wsh, A.dou, A.dov, A.dow, dt * Acoef, dt * Bcoef, A.dhu, A.dhv, A.dhw);
+  // v^ = v*^ + E^T (N'^T dv^ + mu/rhof L dv^)
+  if ((r = adj_ghost(c, {A.dhu, A.dhv, d3 ? A.dhw : nullptr}))) return r;
+  ADJ_LAUNCH(k_adj_state, c->L, u, v, w, A.ush, A.vsh, A.wsh, A.dhu, A.dhv, A.dhw, q, c->prm.viscosity / rhof, wall,
+             A.uh, A.vh, A.wh);
+#undef ADJ_LAUNCH
   CK(cudaGetLastError());
   return 0;
 }
@@ -2017,8 +2062,14 @@ int adj_step(fen_ctx* c, const double* u, const double* v) {
 
 int fen_adjoint_setup(fen_ctx* c, int nsteps, int every) {
   if (!c || nsteps < 1 || every < 1) return fail(FEN_ERR_ARG, "bad argument");
-  if (c->dim != 2 || c->mixed || c->solver != S_PP || c->prm.constant_cfl || c->has_S || var_path(c))
-    return fail(FEN_ERR_ARG, "the adjoint covers 2D periodic FP64 runs with fixed dt and no source field");
+  const bool solver_ok = c->solver == S_PP || c->solver == S_PPP || c->solver == S_PN || c->solver == S_PNP;
+  if (c->mixed || !solver_ok || c->prm.constant_cfl || c->has_S || var_path(c))
+    return fail(FEN_ERR_ARG,
+                "the adjoint covers FP64 runs with fixed dt and no source field, periodic or with walls in y only "
+                "(solvers pp, ppp, pn, pnp)");
+  // the adjoint folds the ghosts of 'Wall' faces (reflected tangential, overwritten normal)
+  if (adj_walls(c) && (c->pbc[FEN_BOTTOM] != FEN_BC_WALL || c->pbc[FEN_TOP] != FEN_BC_WALL))
+    return fail(FEN_ERR_ARG, "the adjoint's walls in y must be 'Wall' faces");
   auto& A = c->adj;
   for (double* b : A.ckpt) if (b) cudaFree(b);
   for (double* b : A.inputs) if (b) cudaFree(b);
@@ -2027,14 +2078,18 @@ int fen_adjoint_setup(fen_ctx* c, int nsteps, int every) {
   A.nsteps = nsteps;
   A.every = std::min(every, nsteps);
   A.nckpt = (nsteps + A.every - 1) / A.every;
+  A.nf = (c->dim == 3) ? 7 : 5;
+  A.nv = c->dim;
   int r;
-  A.ckpt.assign(5 * (A.nckpt + 1), nullptr);
+  A.ckpt.assign((size_t)A.nf * (A.nckpt + 1), nullptr);
   for (auto& b : A.ckpt) if ((r = alloc(&b, c->L.total))) return r;
-  A.inputs.assign(2 * A.every, nullptr);
+  A.inputs.assign((size_t)A.nv * A.every, nullptr);
   for (auto& b : A.inputs) if ((r = alloc(&b, c->L.total))) return r;
-  double** ab[] = {&A.uh, &A.vh, &A.ph, &A.dou, &A.dov, &A.fh, &A.bh, &A.ush, &A.vsh, &A.dhu, &A.dhv};
+  double** ab[] = {&A.uh, &A.vh, &A.wh, &A.ph, &A.dou, &A.dov, &A.dow, &A.fh, &A.bh, &A.ush, &A.vsh, &A.wsh,
+                   &A.dhu, &A.dhv, &A.dhw};
   for (double** b : ab)
     if (!*b && (r = alloc(b, c->L.total))) return r;
+  if (!A.part && (r = alloc(&A.part, kAdjParts))) return r;
   A.ready = false;
   return 0;
 }
@@ -2071,19 +2126,27 @@ int fen_adjoint_forward(fen_ctx* c, double dt) {
   return 0;
 }
 
-int fen_adjoint_backward(fen_ctx* c, const double* lam_u, const double* lam_v, double* g_u, double* g_v, double* ms) {
-  if (!c || !lam_u || !lam_v || !g_u || !g_v) return fail(FEN_ERR_ARG, "null argument");
+int fen_adjoint_backward3(fen_ctx* c, const double* lam_u, const double* lam_v, const double* lam_w, double* g_u,
+                          double* g_v, double* g_w, double* ms) {
+  if (!c || !lam_u || !lam_v || !g_u || !g_v || (c->dim == 3 && (!lam_w || !g_w))) return fail(FEN_ERR_ARG, "null argument");
   auto& A = c->adj;
   if (!A.ready) return fail(FEN_ERR_STATE, "fen_adjoint_forward first");
   int r;
-  // adjoint of the final state: (lam_u, lam_v), p^ = 0, dv_o^ = 0
-  if ((r = relayout<double>(c, A.uh, const_cast<double*>(lam_u), 0, 1)) || (r = relayout<double>(c, A.vh, const_cast<double*>(lam_v), 0, 1)))
+  const bool d3 = (c->dim == 3);
+  // adjoint of the final state: (lam_u, lam_v, lam_w), p^ = 0, dv_o^ = 0
+  if ((r = relayout<double>(c, A.uh, const_cast<double*>(lam_u), 0, 1)) ||
+      (r = relayout<double>(c, A.vh, const_cast<double*>(lam_v), 0, 1)) ||
+      (d3 && (r = relayout<double>(c, A.wh, const_cast<double*>(lam_w), 0, 1))))
     return r;
-  CK(cudaMemsetAsync(A.ph, 0, c->L.total * sizeof(double), c->stream));
-  CK(cudaMemsetAsync(A.dou, 0, c->L.total * sizeof(double), c->stream));
-  CK(cudaMemsetAsync(A.dov, 0, c->L.total * sizeof(double), c->stream));
+  for (double* f : {A.ph, A.dou, A.dov, A.dow}) CK(cudaMemsetAsync(f, 0, c->L.total * sizeof(double), c->stream));
+  if (adj_walls(c)) {
+    // the upper wall face of v is overwritten by the boundary value: no sensitivity
+    const long long nf = (long long)c->n[0] * (d3 ? c->n[2] : 1);
+    if (d3) k_adj_wall_face<3><<<cdiv(nf, 256), 256, 0, c->stream>>>(c->L, A.vh);
+    else k_adj_wall_face<2><<<cdiv(nf, 256), 256, 0, c->stream>>>(c->L, A.vh);
+    c->launches++;
+  }
   // ghost entries of the seed carry no sensitivity: the first adjoint step overwrites them
-  // with periodic copies of the interior
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -2092,12 +2155,16 @@ int fen_adjoint_backward(fen_ctx* c, const double* lam_u, const double* lam_v, d
     const int s0 = seg * A.every, s1 = std::min(A.nsteps, s0 + A.every);
     if ((r = adj_restore(c, seg))) return r;
     for (int s = s0; s < s1; ++s) {
-      if ((r = adj_copy(c, A.inputs[2 * (s - s0)], c->u)) || (r = adj_copy(c, A.inputs[2 * (s - s0) + 1], c->v))) return r;
+      const double* cur[3] = {c->u, c->v, c->w};  // the step's input velocity, kept for its adjoint
+      for (int q = 0; q < A.nv; ++q)
+        if ((r = adj_copy(c, A.inputs[(size_t)A.nv * (s - s0) + q], cur[q]))) return r;
       CK(cudaGraphLaunch(c->graph, c->stream));
     }
     c->launches += c->launches_per_step * (s1 - s0);
-    for (int s = s1 - 1; s >= s0; --s)
-      if ((r = adj_step(c, A.inputs[2 * (s - s0)], A.inputs[2 * (s - s0) + 1]))) return r;
+    for (int s = s1 - 1; s >= s0; --s) {
+      double* const* in = &A.inputs[(size_t)A.nv * (s - s0)];
+      if ((r = adj_step(c, in[0], in[1], d3 ? in[2] : nullptr))) return r;
+    }
   }
   CK(cudaEventRecord(e1, c->stream));
   CK(cudaEventSynchronize(e1));
@@ -2107,20 +2174,30 @@ int fen_adjoint_backward(fen_ctx* c, const double* lam_u, const double* lam_v, d
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if ((r = adj_restore(c, A.nckpt))) return r;
-  // gradient: interior of v^ at step 0 (ghost entries zero)
-  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2;
-  if ((r = relayout<double>(c, A.uh, g_u, 1, 1)) || (r = relayout<double>(c, A.vh, g_v, 1, 1))) return r;
-  for (double* g : {g_u, g_v}) {
-    double* h = g + (size_t)nxg * nyg;  // plane k = 1
-    for (int j = 0; j < nyg; ++j)
-      for (int i = 0; i < nxg; ++i)
-        if (i == 0 || j == 0 || i == nxg - 1 || j == nyg - 1) h[i + (size_t)nxg * j] = 0.0;
+  // gradient: interior of v^ at step 0, ghost entries zero
+  double* gout[3] = {g_u, g_v, g_w};
+  double* gdev[3] = {A.uh, A.vh, A.wh};
+  const int nxg = c->n[0] + 2, nyg = c->n[1] + 2, nzg = d3 ? c->n[2] + 2 : 3;
+  for (int q = 0; q < c->dim; ++q) {
+    if ((r = relayout<double>(c, gdev[q], gout[q], 1, 1))) return r;
+    double* g = gout[q];
+    for (int k = 0; k < nzg; ++k)
+      for (int j = 0; j < nyg; ++j)
+        for (int i = 0; i < nxg; ++i) {
+          const bool in_k = d3 ? (k >= 1 && k <= c->n[2]) : (k == 1);
+          if (!in_k || i == 0 || j == 0 || i == nxg - 1 || j == nyg - 1) g[i + (size_t)nxg * (j + (size_t)nyg * k)] = 0.0;
+        }
   }
   if (ms) {
     ms[0] = A.bwd_ms;
     ms[1] = A.fwd_ms;
   }
   return 0;
+}
+
+int fen_adjoint_backward(fen_ctx* c, const double* lam_u, const double* lam_v, double* g_u, double* g_v, double* ms) {
+  if (c && c->dim == 3) return fail(FEN_ERR_ARG, "3D contexts take fen_adjoint_backward3 (three components)");
+  return fen_adjoint_backward3(c, lam_u, lam_v, nullptr, g_u, g_v, nullptr, ms);
 }
 
 int fen_set_ibm_forcing(fen_ctx* c, int comp, int npoints, const int* ijk, const int* nnbr, const int* nbr_ijk,

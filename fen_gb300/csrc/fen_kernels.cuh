@@ -748,14 +748,15 @@ template <> __device__ __forceinline__ float2 tback<double2, float2>(double2 v) 
 // arithmetic and its order are the plain Thomas recurrence.
 constexpr int kTB = 8;
 
-// Resident 128-thread CTAs per SM the sweep is compiled for: 8 (64 registers) keeps more
-// systems in flight than the compiler's 116-register choice (mixed channel 512x256x384:
-// spectral stage 0.77 -> 0.75 ms; 6 CTAs 0.76 ms).
+// Resident 128-thread CTAs per SM the mixed-form 3D sweep (k_thomas_mixed) is compiled for:
+// more systems in flight than the compiler's register choice (with the three-instruction
+// sweep on the mixed channel 512x256x384: spectral stage 0.77 -> 0.75 ms at 8 CTAs, 0.76 ms
+// at 6; 8 spills here, 6 does not).
 #ifndef FEN_THOMAS_MINB
-#define FEN_THOMAS_MINB 8
+#define FEN_THOMAS_MINB 6
 #endif
 template <typename VS, typename VC>
-__global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas(ThomasArgs a) {
+__global__ void __launch_bounds__(128) k_thomas(ThomasArgs a) {
   typedef ThomasOps<VC> O;
   const int tcol = blockIdx.x * blockDim.x + threadIdx.x;
   const int col = a.split2 ? (tcol >> 1) : tcol;
@@ -835,6 +836,135 @@ __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas(ThomasArgs a) {
     VC dt = tconv<VS, VC>(X[(long long)t * sr]);
     xn = O::sub_amul(dt, (t < T) ? c1[(long long)t * ns] : cfix, xn);
     X[(long long)t * sr] = tback<VC, VS>(xn);
+  }
+}
+
+// Mixed-form sweep (FP32 spectrum, FP64 elimination).  Above the fixed point (rows
+// t0 = conv - 1 .. n - 2, where the factor f and c1 are the constants f*, c*) the forward
+// sweep keeps the unscaled e_t = r_t - a d_(t-1), d_t = f* e_t, as one FMA per row,
+// e_t = r_t - (a f*) e_(t-1); the backward sweep runs on y_t = x_t / f*, y_t = e_t - c* y_(t+1),
+// again one FMA, and the stored result x_t = f* y_t is formed by an FP32 multiply of the
+// narrowed y_t (an extra rounding of the order of the narrowing itself).  Rows below t0 and the
+// last row take the tabulated recurrence of k_thomas.  Two FP64 instructions per row instead
+// of three; FORM3 (the reciprocal factor form) only.
+template <int SPLIT2>
+__global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_mixed(ThomasArgs a) {
+  const int tcol = blockIdx.x * blockDim.x + threadIdx.x;
+  const int col = SPLIT2 ? (tcol >> 1) : tcol;
+  const int outer = blockIdx.y;
+  if (col >= a.ncol) return;
+  const int w = SPLIT2 ? 2 : 1;
+  float* X = reinterpret_cast<float*>(a.x) + ((long long)col * a.s_col + (long long)outer * a.s_outer) * w + (tcol & (w - 1));
+  const long long sys = (long long)outer * a.ncol + col;
+  const long long ns = (long long)a.ncol * a.nouter;
+  const double* c1 = a.c1 + sys;
+  const double* f = a.fac + sys;
+  const int n = a.n;
+  const long long sr = a.s_row * w;
+  const double av = a.aval;
+  const int T = a.conv[sys];
+  const int t0 = (T < n - 1) ? T - 1 : n - 1;  // first row of the fixed point (n - 1: none)
+  // forward sweep, tabulated rows [0, t0): d_t = (r_t - a d_(t-1)) f_t
+  double d = 0.0;
+  int t = 0;
+  for (; t + kTB <= t0; t += kTB) {
+    float xb[kTB];
+    double fb[kTB];
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      xb[q] = X[(long long)(t + q) * sr];
+      fb[q] = f[(long long)(t + q) * ns];
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      const double r = (t + q == 0) ? widen(xb[q]) : fma(-av, d, widen(xb[q]));
+      d = __dmul_rn(r, fb[q]);
+      xb[q] = narrow(d);
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) X[(long long)(t + q) * sr] = xb[q];
+  }
+  for (; t < t0; ++t) {
+    const double r = (t == 0) ? widen(X[0]) : fma(-av, d, widen(X[(long long)t * sr]));
+    d = __dmul_rn(r, f[(long long)t * ns]);
+    X[(long long)t * sr] = narrow(d);
+  }
+  const double piv = f[(long long)(n - 1) * ns];
+  double xn;
+  if (t0 < n - 1) {
+    const double fs = f[(long long)t0 * ns], cs = c1[(long long)t0 * ns];
+    const double g = __dmul_rn(av, fs);
+    // converged rows [t0, n - 1): e_t, stored in place of d_t
+    double e = (t0 == 0) ? widen(X[0]) : fma(-av, d, widen(X[(long long)t0 * sr]));
+    X[(long long)t0 * sr] = narrow(e);
+    t = t0 + 1;
+    for (; t + kTB <= n - 1; t += kTB) {
+      float xb[kTB];
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) xb[q] = X[(long long)(t + q) * sr];
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) {
+        e = fma(-g, e, widen(xb[q]));
+        xb[q] = narrow(e);
+      }
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) X[(long long)(t + q) * sr] = xb[q];
+    }
+    for (; t < n - 1; ++t) {
+      e = fma(-g, e, widen(X[(long long)t * sr]));
+      X[(long long)t * sr] = narrow(e);
+    }
+    // last row: a d_(n-2) = (a f*) e_(n-2); the zero mode's pivot cancels to exactly zero
+    const double r = widen(X[(long long)(n - 1) * sr]);
+    xn = (piv != 0.0) ? __ddiv_rn(fma(-g, e, r), piv) : 0.0;
+    X[(long long)(n - 1) * sr] = narrow(xn);
+    // backward sweep on y = x / f*: y_t = e_t - c* y_(t+1); x_t = f* y_t in FP32
+    const float fs32 = narrow(fs);
+    double y = __ddiv_rn(xn, fs);
+    t = n - 2;
+    for (; t - kTB + 1 >= t0; t -= kTB) {
+      float xb[kTB];
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) xb[q] = X[(long long)(t - q) * sr];
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) {
+        y = fma(-cs, y, widen(xb[q]));
+        xb[q] = narrow(y) * fs32;
+      }
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) X[(long long)(t - q) * sr] = xb[q];
+    }
+    for (; t >= t0; --t) {
+      y = fma(-cs, y, widen(X[(long long)t * sr]));
+      X[(long long)t * sr] = narrow(y) * fs32;
+    }
+    xn = __dmul_rn(fs, y);  // x_(t0), the start of the tabulated rows below
+  } else {
+    const double r = widen(X[(long long)(n - 1) * sr]);
+    xn = (piv != 0.0) ? __ddiv_rn(fma(-av, d, r), piv) : 0.0;
+    X[(long long)(n - 1) * sr] = narrow(xn);
+    t = n - 2;
+  }
+  // backward sweep, tabulated rows below t0: x_t = d_t - c1_t x_(t+1)
+  for (t = t0 - 1; t - kTB + 1 >= 0; t -= kTB) {
+    float xb[kTB];
+    double cb[kTB];
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      xb[q] = X[(long long)(t - q) * sr];
+      cb[q] = c1[(long long)(t - q) * ns];
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      xn = fma(-cb[q], xn, widen(xb[q]));
+      xb[q] = narrow(xn);
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) X[(long long)(t - q) * sr] = xb[q];
+  }
+  for (; t >= 0; --t) {
+    xn = fma(-c1[(long long)t * ns], xn, widen(X[(long long)t * sr]));
+    X[(long long)t * sr] = narrow(xn);
   }
 }
 

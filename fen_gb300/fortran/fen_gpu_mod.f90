@@ -204,6 +204,13 @@ module fen_gpu_mod
             type(c_ptr), value :: ctx
             real(c_double), value :: dt
         end function fen_adjoint_forward
+        integer(c_int) function fen_adjoint_backward3(ctx, lam_u, lam_v, lam_w, g_u, g_v, g_w, ms) &
+                bind(C, name='fen_adjoint_backward3')
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(in) :: lam_u(*), lam_v(*), lam_w(*)
+            real(c_double), intent(out) :: g_u(*), g_v(*), g_w(*), ms(2)
+        end function fen_adjoint_backward3
         integer(c_int) function fen_adjoint_backward(ctx, lam_u, lam_v, g_u, g_v, ms) bind(C, name='fen_adjoint_backward')
             import :: c_int, c_ptr, c_double
             type(c_ptr), value :: ctx

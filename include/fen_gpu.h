@@ -158,15 +158,21 @@ int fen_load_state_mf(fen_ctx* ctx, const char* path, double* vof);
  * velocity interpolated to cell centres (face_to_center, src/fields.f90:210-252). */
 int fen_save_fields(fen_ctx* ctx, const char* dir, int step);
 
-/* Discrete adjoint of the step (no counterpart in FEN, which has no differentiation): 2D
- * periodic FP64 contexts with fixed dt.  fen_adjoint_setup sizes an nsteps rollout with a
- * checkpoint every `every` steps; fen_adjoint_forward runs the rollout from the current
- * state (which ends at step nsteps); fen_adjoint_backward takes the sensitivity of a scalar
- * loss to the final (u, v) and returns its gradient with respect to the initial (u, v),
- * recomputing each checkpoint segment.  Arrays use the host field layout; ghost entries of
- * the gradient are zero.  ms (optional, 2 doubles): backward and forward device times. */
+/* Discrete adjoint of the step (no counterpart in FEN, which has no differentiation): FP64
+ * contexts with fixed dt (dt_o = dt), no source field and constant properties, 2D or 3D,
+ * periodic (pp, ppp) or periodic with 'Wall' faces in y (pn, pnp: the channel).
+ * fen_adjoint_setup sizes an nsteps rollout with a checkpoint every `every` steps;
+ * fen_adjoint_forward runs the rollout from the current state (which ends at step nsteps);
+ * fen_adjoint_backward3 takes the sensitivity of a scalar loss to the final velocity and
+ * returns its gradient with respect to the initial velocity, recomputing each checkpoint
+ * segment (lam_w, g_w unused in 2D).  Arrays use the host field layout (gl = 1); ghost
+ * entries of the gradient are zero, as is the upper wall face of v (overwritten by the
+ * boundary value in every step).  ms (optional, 2 doubles): backward and forward device
+ * times.  fen_adjoint_backward is the 2D form. */
 int fen_adjoint_setup(fen_ctx* ctx, int nsteps, int every);
 int fen_adjoint_forward(fen_ctx* ctx, double dt);
+int fen_adjoint_backward3(fen_ctx* ctx, const double* lam_u, const double* lam_v, const double* lam_w, double* g_u,
+                          double* g_v, double* g_w, double* ms);
 int fen_adjoint_backward(fen_ctx* ctx, const double* lam_u, const double* lam_v, double* g_u, double* g_v,
                          double* ms);
 

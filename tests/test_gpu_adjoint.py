@@ -162,10 +162,14 @@ def test_autograd_rollout(fen_lib):
 
 
 def test_adjoint_rejects_unsupported_contexts(fen_lib):
-    g = F.Grid(16, 16, 16, L, L, L)
+    # walls on every side (nnn) and the mixed form are outside the adjoint's scope
+    g = F.Grid(16, 16, 16, L, L, L, bc=["Wall"] * 6)
     s = F.Solver(g)
-    with pytest.raises(F.FenError, match="2D periodic"):
+    with pytest.raises(F.FenError, match="adjoint covers"):
         s.adjoint_setup(4, 2)
+    m = F.Solver(F.Grid(16, 16, 1, L, L, L / 16), precision=F.MIXED)
+    with pytest.raises(F.FenError, match="adjoint covers"):
+        m.adjoint_setup(4, 2)
     s2 = _solver(16, 1e-2)
     s2.adjoint_setup(4, 2)
     s2.set_dt_o(1e-3)
