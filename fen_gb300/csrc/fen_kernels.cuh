@@ -384,6 +384,9 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
     const int work = nl * n;
     F2 rod{0.f, 0.f};
     if (LD == LD_RESID) rod = split_d(a.sc->rho_over_dt);
+    // rho/dt read (and, in FP32 kernels, narrowed) once: the field stores below may alias sc
+    // as far as the compiler knows, which would otherwise reload and convert it per element
+    const T rdt = (LD == LD_DIV || LD == LD_DIVMIX) ? (T)a.sc->rho_over_dt : T(0);
     for (int t = tid; t < work; t += nth) {
       int l, i;
       if (CONTIG) divmod(t, fN, l, i); else divmod(t, fL, i, l);
@@ -396,7 +399,7 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
           else if (LD == LD_DIV) {
             x = div_at<T, DIM>(a, i + 1, j, k);
             if (a.rho_c) x = x * (T)a.rho_c[a.L.idx(i + 1, j, kst<DIM>(k))];
-            x = x * (T)a.sc->rho_over_dt;
+            x = x * rdt;
           }
           else if (LD == LD_DIVMIX) {
             const F2 dd = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
@@ -407,7 +410,7 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
               a.dvh[c] = dd.hi;
               a.dvl[c] = dd.lo;
             }
-            x = (T)(dd.hi + dd.lo) * (T)a.sc->rho_over_dt;
+            x = (T)(dd.hi + dd.lo) * rdt;
           } else {
             // refinement right-hand side r = rho/dt D v* - L_h phi in double-float (phi = fsrc;
             // D v* as formed by this step's first transform)
