@@ -53,6 +53,10 @@ namespace ens {
 #define FEN_ENS_CLUSTER 8
 #endif
 constexpr int kCl = FEN_ENS_CLUSTER;   // CTAs per cluster (above 8: non-portable cluster size)
+// 1: the SMs that kCl-CTA clusters leave idle run a second launch of 4-CTA clusters
+#ifndef FEN_ENS_SPLIT
+#define FEN_ENS_SPLIT 1
+#endif
 constexpr size_t kSmemLimit = 232448;  // opt-in dynamic shared memory per CTA (227 KB)
 constexpr size_t kSmemReserve = 1024;  // static shared memory of the kernel + slack
 
@@ -1005,11 +1009,21 @@ struct fen_ensemble {
   ClassDesc* d_cls = nullptr;
   Pack* d_packs = nullptr;
   int* d_runlist = nullptr;
-  int* d_counter = nullptr;
+  int* d_counter = nullptr;               // [0] the 8-CTA launch, [1] the 4-CTA launch
   int npacks = 0;
   int threads = 1024;
   size_t smem = 0;
   int nclusters = 0;
+  // the SMs that kCl-CTA clusters leave idle take a second, concurrent launch of 4-CTA
+  // clusters over the small grids (classes with G <= 4)
+  Pack* d_packs4 = nullptr;
+  int* d_runlist4 = nullptr;
+  int npacks4 = 0;
+  size_t smem4 = 0;
+  int nclusters4 = 0;
+  bool split = FEN_ENS_SPLIT != 0;
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   cudaStream_t stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -1109,73 +1123,161 @@ const void* kernel_ptr(int threads, int mode = 0) {
 }
 
 // Pack the runs `subset` (all runs when empty) with the current G per class; uploads the
-// class table, the packs and the run list, and sizes the launch.
-int build_packs(fen_ensemble* e, const std::vector<int>& subset) {
-  std::vector<Pack> packs;
-  std::vector<int> list;
-  size_t smem = 0;
-  for (size_t c = 0; c < e->cls_n.size(); ++c) {
-    set_g(e->cls_host[c], e->cls_g[c]);
-    const int G = e->cls_g[c], per = kCl / G;
-    std::vector<int> runs;
-    if (subset.empty()) {
-      for (int q = 0; q < e->nruns; ++q)
-        if (e->run_cls[q] == (int)c) runs.push_back(q);
-    } else {
-      for (int q : subset)
-        if (e->run_cls[q] == (int)c) runs.push_back(q);
-    }
-    if (runs.empty()) continue;
-    smem = std::max(smem, smem_bytes(e->cls_n[c], G, nullptr, e->cls_host[c].tabs != 0));
-    for (size_t s = 0; s < runs.size(); s += per) {
-      Pack p;
-      p.cls = (int)c;
-      p.first = (int)list.size();
-      p.nruns = (int)std::min<size_t>(per, runs.size() - s);
-      p.pad = 0;
-      for (int k = 0; k < p.nruns; ++k) list.push_back(runs[s + k]);
-      packs.push_back(p);
-    }
-  }
-  EK(cudaMemcpy(e->d_cls, e->cls_host.data(), e->cls_host.size() * sizeof(ClassDesc), cudaMemcpyHostToDevice));
-  if (e->d_packs) cudaFree(e->d_packs);
-  if (e->d_runlist) cudaFree(e->d_runlist);
-  e->d_packs = nullptr;
-  e->d_runlist = nullptr;
-  EK(cudaMalloc(&e->d_packs, std::max<size_t>(packs.size(), 1) * sizeof(Pack)));
-  EK(cudaMalloc(&e->d_runlist, std::max<size_t>(list.size(), 1) * sizeof(int)));
-  if (!packs.empty()) EK(cudaMemcpy(e->d_packs, packs.data(), packs.size() * sizeof(Pack), cudaMemcpyHostToDevice));
-  if (!list.empty()) EK(cudaMemcpy(e->d_runlist, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
-  e->npacks = (int)packs.size();
-  e->smem = smem;
-  const void* k = kernel_ptr(e->threads);
-  for (int m = 0; m < 3; ++m) {
-    EK(cudaFuncSetAttribute(kernel_ptr(e->threads, m), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 1)));
-    if (kCl > 8) EK(cudaFuncSetAttribute(kernel_ptr(e->threads, m), cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-  }
+// class table, the packs and the run lists, and sizes the launches.  With the split on, the
+// smallest runs of classes with G <= 4 go to 4-CTA clusters on the SMs the kCl-CTA clusters
+// leave idle, up to that share of the SMs (cost N^2 per run).
+int upload_packs(const std::vector<Pack>& packs, const std::vector<int>& list, Pack** dp, int** dl) {
+  if (*dp) cudaFree(*dp);
+  if (*dl) cudaFree(*dl);
+  *dp = nullptr;
+  *dl = nullptr;
+  EK(cudaMalloc(dp, std::max<size_t>(packs.size(), 1) * sizeof(Pack)));
+  EK(cudaMalloc(dl, std::max<size_t>(list.size(), 1) * sizeof(int)));
+  if (!packs.empty()) EK(cudaMemcpy(*dp, packs.data(), packs.size() * sizeof(Pack), cudaMemcpyHostToDevice));
+  if (!list.empty()) EK(cudaMemcpy(*dl, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int max_clusters(fen_ensemble* e, int csize, size_t smem, int* out) {
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = kCl;
+  at[0].val.clusterDim.x = csize;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
-  cfg.gridDim = dim3(kCl, 1, 1);
+  cfg.gridDim = dim3(csize, 1, 1);
   cfg.blockDim = dim3(e->threads, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.attrs = at;
   cfg.numAttrs = 1;
+  EK(cudaOccupancyMaxActiveClusters(out, kernel_ptr(e->threads), &cfg));
+  return 0;
+}
+
+int build_packs(fen_ensemble* e, const std::vector<int>& subset) {
+  for (size_t c = 0; c < e->cls_n.size(); ++c) set_g(e->cls_host[c], e->cls_g[c]);
+  std::vector<int> runs;
+  if (subset.empty()) {
+    for (int q = 0; q < e->nruns; ++q) runs.push_back(q);
+  } else {
+    runs = subset;
+  }
+  // SMs left idle by the kCl-CTA clusters
+  int sms = 0, dev = 0;
+  EK(cudaGetDevice(&dev));
+  EK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  size_t smem_all = 0;
+  for (int q : runs) {
+    const int c = e->run_cls[q];
+    smem_all = std::max(smem_all, smem_bytes(e->cls_n[c], e->cls_g[c], nullptr, e->cls_host[c].tabs != 0));
+  }
+  for (int m = 0; m < 3; ++m) {
+    EK(cudaFuncSetAttribute(kernel_ptr(e->threads, m), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem_all, 1)));
+    if (kCl > 8) EK(cudaFuncSetAttribute(kernel_ptr(e->threads, m), cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  }
+  // assignment: smallest eligible runs to the 4-CTA launch up to its share of the SMs
+  std::vector<char> small(e->nruns, 0);
+  int n4 = 0;
+  if (e->split && kCl == 8) {
+    int nc = 0;
+    int r;
+    if ((r = max_clusters(e, kCl, smem_all, &nc))) return r;
+    const int idle = sms - kCl * nc;
+    n4 = idle >= 4 ? idle / 4 : 0;
+    if (n4 > 0) {
+      std::vector<int> order(runs);
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return e->n[a] < e->n[b]; });
+      double total = 0.0;
+      for (int q : order) total += (double)e->n[q] * e->n[q];
+      const double target = total * (4.0 * n4) / (4.0 * n4 + (double)kCl * nc);
+      double acc = 0.0;
+      for (int q : order) {
+        const double w = (double)e->n[q] * e->n[q];
+        if (e->cls_g[e->run_cls[q]] > 4 || acc + 0.5 * w > target) continue;
+        small[q] = 1;
+        acc += w;
+      }
+    }
+  }
+  std::vector<Pack> packs[2];
+  std::vector<int> list[2];
+  size_t smem[2] = {0, 0};
+  for (size_t c = 0; c < e->cls_n.size(); ++c) {
+    const int G = e->cls_g[c];
+    for (int part = 0; part < 2; ++part) {
+      const int csize = part ? 4 : kCl, per = csize / G;
+      std::vector<int> rr;
+      for (int q : runs)
+        if (e->run_cls[q] == (int)c && (int)small[q] == part) rr.push_back(q);
+      if (rr.empty()) continue;
+      smem[part] = std::max(smem[part], smem_bytes(e->cls_n[c], G, nullptr, e->cls_host[c].tabs != 0));
+      for (size_t s = 0; s < rr.size(); s += per) {
+        Pack p;
+        p.cls = (int)c;
+        p.first = (int)list[part].size();
+        p.nruns = (int)std::min<size_t>(per, rr.size() - s);
+        p.pad = 0;
+        for (int k = 0; k < p.nruns; ++k) list[part].push_back(rr[s + k]);
+        packs[part].push_back(p);
+      }
+    }
+  }
+  EK(cudaMemcpy(e->d_cls, e->cls_host.data(), e->cls_host.size() * sizeof(ClassDesc), cudaMemcpyHostToDevice));
+  int r;
+  if ((r = upload_packs(packs[0], list[0], &e->d_packs, &e->d_runlist))) return r;
+  if ((r = upload_packs(packs[1], list[1], &e->d_packs4, &e->d_runlist4))) return r;
+  e->npacks = (int)packs[0].size();
+  e->npacks4 = (int)packs[1].size();
+  e->smem = smem[0];
+  e->smem4 = smem[1];
   int nc = 0;
-  EK(cudaOccupancyMaxActiveClusters(&nc, k, &cfg));
-  if (nc < 1)
-    return fen_internal_fail(FEN_ERR_CUDA, ("no cluster of " + std::to_string(kCl) +
-                                            " CTAs fits this device with the ensemble's shared memory").c_str());
+  if (e->npacks) {
+    if ((r = max_clusters(e, kCl, e->smem, &nc))) return r;
+    if (nc < 1)
+      return fen_internal_fail(FEN_ERR_CUDA, ("no cluster of " + std::to_string(kCl) +
+                                              " CTAs fits this device with the ensemble's shared memory").c_str());
+  }
   e->nclusters = nc;
+  e->nclusters4 = e->npacks4 ? std::max(1, n4) : 0;
   if (e->exec) { cudaGraphExecDestroy(e->exec); e->exec = nullptr; }
   if (e->graph) { cudaGraphDestroy(e->graph); e->graph = nullptr; }
   e->exec_steps = -1;
   return 0;
 }
 
+int launch_one(fen_ensemble* e, EnsArgs a, int csize, int nclusters, size_t smem, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(csize * std::max(1, std::min(nclusters, a.npacks)), 1, 1);
+  cfg.blockDim = dim3(e->threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const int mode = a.mode;
+  if (e->threads == 512) {
+    if (mode == 0) EK(cudaLaunchKernelEx(&cfg, k_ensemble<512, 0>, a));
+    else if (mode == 1) EK(cudaLaunchKernelEx(&cfg, k_ensemble<512, 1>, a));
+    else EK(cudaLaunchKernelEx(&cfg, k_ensemble<512, 2>, a));
+  } else {
+    if (mode == 0) EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024, 0>, a));
+    else if (mode == 1) EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024, 1>, a));
+    else EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024, 2>, a));
+  }
+  EK(cudaGetLastError());
+  return 0;
+}
+
+// Kernels one ensemble pass launches.
+int pass_kernels(const fen_ensemble* e) { return (e->npacks ? 1 : 0) + (e->npacks4 ? 1 : 0); }
+
+// One ensemble pass: the kCl-CTA launch on e->stream and, when the split placed runs there,
+// the 4-CTA launch on stream2 beside it (fork/join events, so a captured graph holds the two
+// as parallel nodes).  The runs are independent and no CTA waits on the other launch.
 int launch(fen_ensemble* e, int nsteps, int mode = 0) {
   EnsArgs a;
   memset(&a, 0, sizeof(a));
@@ -1195,29 +1297,23 @@ int launch(fen_ensemble* e, int nsteps, int mode = 0) {
   a.abuf = e->abuf;
   a.aoff = e->d_aoff;
   a.rec = e->rec;
-  EK(cudaMemsetAsync(e->d_counter, 0, sizeof(int), e->stream));
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = kCl;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.gridDim = dim3(kCl * std::max(1, std::min(e->nclusters, e->npacks)), 1, 1);
-  cfg.blockDim = dim3(e->threads, 1, 1);
-  cfg.dynamicSmemBytes = e->smem;
-  cfg.stream = e->stream;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  if (e->threads == 512) {
-    if (mode == 0) EK(cudaLaunchKernelEx(&cfg, k_ensemble<512, 0>, a));
-    else if (mode == 1) EK(cudaLaunchKernelEx(&cfg, k_ensemble<512, 1>, a));
-    else EK(cudaLaunchKernelEx(&cfg, k_ensemble<512, 2>, a));
-  } else {
-    if (mode == 0) EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024, 0>, a));
-    else if (mode == 1) EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024, 1>, a));
-    else EK(cudaLaunchKernelEx(&cfg, k_ensemble<1024, 2>, a));
+  EK(cudaMemsetAsync(e->d_counter, 0, 2 * sizeof(int), e->stream));
+  const bool two = e->npacks4 > 0;
+  if (two) EK(cudaEventRecord(e->fork, e->stream));
+  // the kCl-CTA launch is issued first so that its clusters are placed before the small ones
+  int r;
+  if (e->npacks && (r = launch_one(e, a, kCl, e->nclusters, e->smem, e->stream))) return r;
+  if (two) {
+    EK(cudaStreamWaitEvent(e->stream2, e->fork, 0));
+    EnsArgs b = a;
+    b.packs = e->d_packs4;
+    b.npacks = e->npacks4;
+    b.run_list = e->d_runlist4;
+    b.counter = e->d_counter + 1;
+    if ((r = launch_one(e, b, 4, e->nclusters4, e->smem4, e->stream2))) return r;
+    EK(cudaEventRecord(e->join, e->stream2));
+    EK(cudaStreamWaitEvent(e->stream, e->join, 0));
   }
-  EK(cudaGetLastError());
   return 0;
 }
 
@@ -1261,7 +1357,7 @@ int advance_graph(fen_ensemble* e, int nsteps, float* ms) {
   EK(cudaEventElapsedTime(ms, e0, e1));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  e->launches += 1;
+  e->launches += pass_kernels(e);
   return pull_scal(e);
 }
 
@@ -1347,6 +1443,10 @@ int fen_ensemble_create(int nruns, const int* n, const double* viscosity, double
     return fen_internal_fail(FEN_ERR_CUDA, (std::string(what) + ": " + cudaGetErrorString(err)).c_str());
   };
   if ((ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail_cuda(ce, "stream");
+  if ((ce = cudaStreamCreateWithFlags(&e->stream2, cudaStreamNonBlocking)) != cudaSuccess) return fail_cuda(ce, "stream");
+  if ((ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming)) != cudaSuccess ||
+      (ce = cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming)) != cudaSuccess)
+    return fail_cuda(ce, "events");
   if ((ce = cudaMalloc(&e->state, tot * sizeof(float))) != cudaSuccess) return fail_cuda(ce, "state");
   if ((ce = cudaMemset(e->state, 0, tot * sizeof(float))) != cudaSuccess) return fail_cuda(ce, "state");
   if ((ce = cudaMalloc(&e->d_off, nruns * sizeof(long long))) != cudaSuccess) return fail_cuda(ce, "offsets");
@@ -1354,7 +1454,7 @@ int fen_ensemble_create(int nruns, const int* n, const double* viscosity, double
     return fail_cuda(ce, "offsets");
   if ((ce = cudaMalloc(&e->d_scal, nruns * sizeof(RunScal))) != cudaSuccess) return fail_cuda(ce, "scalars");
   if ((ce = cudaMalloc(&e->d_cls, sizes.size() * sizeof(ClassDesc))) != cudaSuccess) return fail_cuda(ce, "classes");
-  if ((ce = cudaMalloc(&e->d_counter, sizeof(int))) != cudaSuccess) return fail_cuda(ce, "counter");
+  if ((ce = cudaMalloc(&e->d_counter, 2 * sizeof(int))) != cudaSuccess) return fail_cuda(ce, "counter");
   if ((r = build_packs(e, {}))) { fen_ensemble_destroy(e); return r; }
   *out = e;
   return 0;
@@ -1366,9 +1466,14 @@ int fen_ensemble_destroy(fen_ensemble* e) {
   if (e->exec) cudaGraphExecDestroy(e->exec);
   if (e->graph) cudaGraphDestroy(e->graph);
   for (void* b : e->bufs) cudaFree(b);
-  void* ptrs[] = {e->state, e->d_off, e->d_scal, e->d_cls, e->d_packs, e->d_runlist, e->d_counter, e->abuf, e->d_aoff, e->rec};
+  if (e->stream2) cudaStreamSynchronize(e->stream2);
+  void* ptrs[] = {e->state, e->d_off, e->d_scal, e->d_cls, e->d_packs, e->d_runlist, e->d_counter, e->abuf, e->d_aoff, e->rec,
+                  e->d_packs4, e->d_runlist4};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (e->fork) cudaEventDestroy(e->fork);
+  if (e->join) cudaEventDestroy(e->join);
+  if (e->stream2) cudaStreamDestroy(e->stream2);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
   return 0;
@@ -1490,7 +1595,7 @@ int timed_launch(fen_ensemble* e, int nsteps, int mode, float* ms) {
   EK(cudaEventElapsedTime(ms, e0, e1));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  e->launches += 1;
+  e->launches += pass_kernels(e);
   return pull_scal(e);
 }
 }  // namespace
@@ -1653,7 +1758,7 @@ int fen_ensemble_tune(fen_ensemble* e, int steps, const char* cache_path) {
     EK(cudaEventElapsedTime(ms, a0, a1));
     cudaEventDestroy(a0);
     cudaEventDestroy(a1);
-    e->launches += 2;
+    e->launches += 2 * pass_kernels(e);
     return restore();
   };
   e->threads = 1024;

@@ -112,17 +112,6 @@ __device__ __forceinline__ DF dsq(DF a) {
   const float h = p + e;
   return DF{h, e - (h - p)};
 }
-// Second difference a(+) - 2 a(0) + a(-) of a pair field to FP32 accuracy of the difference:
-// the hi differences are exact for neighbouring values of one sign (Sterbenz), the lo parts
-// carry the rest.
-__device__ __forceinline__ float d2f(DF p, DF c, DF m) {
-  return ((p.h - c.h) + (m.h - c.h)) + ((p.l - c.l) + (m.l - c.l));
-}
-// Diffusion of the 3D double-float predictor: 0 = FP32 viscous term from pair differences
-// (d2f), 1 = full double-float.
-#ifndef FEN_DF_DIFFUSION
-#define FEN_DF_DIFFUSION 0
-#endif
 // Second difference a(+) - 2 a(0) + a(-) of a pair field.
 __device__ __forceinline__ DF d2(DF p, DF c, DF m) {
   float s1, e1, s2, e2;
@@ -345,7 +334,6 @@ static __global__ void __launch_bounds__(kDTX * kDTY, FEN_DFTILE_MINB) k_predict
     pww = fww;
     if (act) {
       const DF uc = dfv(U, c), vc = dfv(V, c), wc = dfv(W, c);
-#if FEN_DF_DIFFUSION
       DF lu = dmul(d2(dfv(U, c + 1), uc, dfv(U, c - 1)), mx);
       lu = dadd(lu, dmul(d2(dfv(U, c + sy), uc, dfv(U, c - sy)), my));
       lu = dadd(lu, dmul(d2(dfv(U, c + sz), uc, dfv(U, c - sz)), mz));
@@ -355,21 +343,6 @@ static __global__ void __launch_bounds__(kDTX * kDTY, FEN_DFTILE_MINB) k_predict
       DF lw = dmul(d2(dfv(W, c + 1), wc, dfv(W, c - 1)), mx);
       lw = dadd(lw, dmul(d2(dfv(W, c + sy), wc, dfv(W, c - sy)), my));
       lw = dadd(lw, dmul(d2(dfv(W, c + sz), wc, dfv(W, c - sz)), mz));
-#else
-      // Diffusion to FP32 relative accuracy of the viscous term itself: its second
-      // differences are taken on the pairs (exact up to one rounding of the difference), so
-      // only the term's own FP32 rounding remains, about 1e-7 of a term that is a few
-      // per cent of the advective increment on the workloads here.
-      const DF lu = DF{fmaf(d2f(dfv(U, c + sz), uc, dfv(U, c - sz)), mz.h,
-                            fmaf(d2f(dfv(U, c + sy), uc, dfv(U, c - sy)), my.h, d2f(dfv(U, c + 1), uc, dfv(U, c - 1)) * mx.h)),
-                       0.f};
-      const DF lv = DF{fmaf(d2f(dfv(V, c + sz), vc, dfv(V, c - sz)), mz.h,
-                            fmaf(d2f(dfv(V, c + sy), vc, dfv(V, c - sy)), my.h, d2f(dfv(V, c + 1), vc, dfv(V, c - 1)) * mx.h)),
-                       0.f};
-      const DF lw = DF{fmaf(d2f(dfv(W, c + sz), wc, dfv(W, c - sz)), mz.h,
-                            fmaf(d2f(dfv(W, c + sy), wc, dfv(W, c - sy)), my.h, d2f(dfv(W, c + 1), wc, dfv(W, c - 1)) * mx.h)),
-                       0.f};
-#endif
       DF dx = dsub(lu, ax), dy = dsub(lv, ay), dz = dsub(lw, az);
       if (a.has_S) {
         const DF ir = DF{a.irho.hi, a.irho.lo};
