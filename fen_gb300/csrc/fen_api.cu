@@ -32,6 +32,18 @@
 
 using namespace fen;
 
+// Build knobs (on by default): the mixed form's two-instruction tridiagonal sweep, the mean of
+// phi removed in the correction, the half-spectrum pitch padded to 64 bytes.
+#ifndef FEN_THOMAS_FAST
+#define FEN_THOMAS_FAST 1
+#endif
+#ifndef FEN_DEFER_MEAN
+#define FEN_DEFER_MEAN 1
+#endif
+#ifndef FEN_SPEC_PAD
+#define FEN_SPEC_PAD 1
+#endif
+
 namespace {
 
 thread_local std::string g_err;
@@ -442,7 +454,7 @@ int init_poisson(fen_ctx* c) {
   const int h = nx / 2 + 1;
   // complex pitch along x: the h = nx/2 + 1 half-spectrum columns padded to 64 bytes, so the
   // column transforms and tridiagonal sweeps move whole 64-byte segments of every row
-  const int padc = c->mixed ? 8 : 4;
+  const int padc = FEN_SPEC_PAD ? (c->mixed ? 8 : 4) : 1;
   const long long hp = (h + padc - 1) / padc * padc;
   c->stages.clear();
   c->needs_mean = (s == S_PP || s == S_PN || s == S_PPN || s == S_PNP);
@@ -668,7 +680,7 @@ int launch_thomas(fen_ctx* c, const Stage& s) {
   constexpr int kTh = 128;  // (64-thread CTAs measured no faster)
   // the mixed form's reciprocal-factor (3D) solves take the two-FMA sweep above the pivots'
   // fixed point; the FP64 form keeps the reference's operation order
-  const bool fast = c->mixed && ta.form3;
+  const bool fast = FEN_THOMAS_FAST && c->mixed && ta.form3;
   if (real) {
     const dim3 g(cdiv(ta.ncol, kTh), s.tgrid.y, s.tgrid.z);
     if (fast) k_thomas_mixed<0><<<g, kTh, 0, c->stream>>>(ta);
@@ -761,7 +773,7 @@ bool var_path(const fen_ctx* c) { return c->var_rho || c->var_mu || c->split; }
 
 // Mixed form with refinement: the step keeps the mean of phi (removed in the correction's
 // pressure update instead of by a separate pass over phi).
-bool deferred_mean(const fen_ctx* c) { return c->mixed && c->refine && c->needs_mean; }
+bool deferred_mean(const fen_ctx* c) { return FEN_DEFER_MEAN && c->mixed && c->refine && c->needs_mean; }
 
 // Density of the Poisson scaling rho_over_dt: 1 with a density field (the loader multiplies
 // by rho(i,j,k)), rhomin with the split, else the constant density.
