@@ -300,11 +300,12 @@ def form_mixed(F, steps, scale=1):
         dt = s.set_timestep(start_velocity("channel", cfg))
         ms = s.time_steps(steps, dt)
         out[name] = round(cells * steps / (ms / 1e3) / 1e6, 3)
+        res = {k: s.get_field(fid)[1:-1, 1:-1, 1:-1] for k, fid in (("u", F.U), ("v", F.V), ("w", F.W), ("p", F.P))}
         if name == "mixed":
+            # stage times after the fields are read (profile_step advances the state)
             peak, peak_kind = measured_peaks()
             stage = dict(zip(STAGES, s.profile_step(3, s.status()["dt"])))
             out["roofline"] = roofline_block(3, "mixed", cells, stage, peak, peak_kind)
-        res = {k: s.get_field(fid)[1:-1, 1:-1, 1:-1] for k, fid in (("u", F.U), ("v", F.V), ("w", F.W), ("p", F.P))}
         if name == "fp64":
             ref = res
         else:
