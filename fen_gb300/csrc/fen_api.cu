@@ -607,7 +607,14 @@ int launch_line_t(fen_ctx* c, const Stage& s, const LineArgs<T>& a) {
     CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     return 0;
   }
-  kern<<<s.grid, 256, s.smem, c->stream>>>(a);
+  LineArgs<T> b = a;
+  constexpr bool real_fft = (OP == OP_R2C || OP == OP_C2R || OP == OP_DCT2 || OP == OP_DCT3);
+  const int M = real_fft ? b.n / 2 : b.n;
+  b.mg[0] = fft_magic((unsigned)b.n);
+  b.mg[1] = fft_magic((unsigned)M);
+  b.mg[2] = fft_magic((unsigned)(M + 1));
+  b.mg[3] = fft_magic((unsigned)b.nl);
+  kern<<<s.grid, 256, s.smem, c->stream>>>(b);
   c->launches++;
   CK(cudaGetLastError());
   return 0;
@@ -1324,6 +1331,9 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
   L.off = 3;
   const int planes = (c->dim == 3) ? c->n[2] + 2 : 1;
   L.total = L.off + L.sp * planes + 4;
+  L.fastdiv = (L.n0 <= 4096 && L.n1 <= 4096) ? 1 : 0;
+  L.mg0 = fft_magic((unsigned)L.n0);
+  L.mg1 = fft_magic((unsigned)L.n1);
   int r = 0;
   double** state[] = {&c->u, &c->v, &c->w, &c->p};
   for (double** f : state)
@@ -2277,6 +2287,23 @@ int fen_set_split_pressure(fen_ctx* c, double rhomin) {
   c->split = 1;
   c->rhomin = rhomin;
   drop_graph(c);
+  return 0;
+}
+
+int fen_debug_checks(long long* count, long long* first) {
+  if (!count || !first) return fail(FEN_ERR_ARG, "null argument");
+#ifdef FEN_DEBUG_CHECKS
+  unsigned long long n = 0;
+  long long f = 0;
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpyFromSymbol(&n, g_fen_oob_count, sizeof(n)));
+  CK(cudaMemcpyFromSymbol(&f, g_fen_oob_first, sizeof(f)));
+  *count = (long long)n;
+  *first = n ? f : 0;
+#else
+  *count = -1;
+  *first = 0;
+#endif
   return 0;
 }
 

@@ -211,9 +211,9 @@ __host__ __device__ constexpr int fft_max_radix() {
 // One complex FFT of length P.M on `nl` lines held in shared memory, radix schedule P.R
 // (16, 8, 4, 2, 3; none above MAXR).  Returns the buffer holding the result (a or b).
 template <int DIR, int MAXR, typename T2>
-__device__ T2* smem_fft(T2* a, T2* b, int nl, int ls, int es, const FFTPlan& P, const double2* tw) {
+__device__ T2* smem_fft(T2* a, T2* b, FastDiv fnl, int ls, int es, const FFTPlan& P, const double2* tw) {
   const int M = P.M;
-  const FastDiv fnl{(unsigned)nl, fft_magic((unsigned)nl)};
+  const int nl = (int)fnl.d;
   int Ns = 1;
   for (int s = 0; s < P.nst; ++s) {
     const int R = P.R[s];

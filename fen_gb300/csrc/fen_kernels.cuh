@@ -319,6 +319,10 @@ struct LineArgs {
   // optional tabulated scale/lam for OP_C2C_SOLVE, [(outer * n + pos) * nlines + col]
   const T* inv_lam;
   FFTPlan plan;
+  // fast-division multipliers (fft_magic) of n, M, M + 1 and nl, computed on the host: an
+  // integer division in the kernel runs through conversion instructions, which GB300 issues
+  // on its FP64 pipe (zero: computed in the kernel)
+  unsigned mg[4];
   AxisTw tw;
 };
 
@@ -368,8 +372,10 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   const int nlv = min(nl, a.nlines - line0);  // valid lines in this CTA
   const int tid = threadIdx.x, nth = blockDim.x;
   // element -> (line, position) splits by multiply-high division (no per-element divide)
-  const FastDiv fN{(unsigned)n, fft_magic((unsigned)n)}, fM{(unsigned)M, fft_magic((unsigned)M)};
-  const FastDiv fM1{(unsigned)(M + 1), fft_magic((unsigned)(M + 1))}, fL{(unsigned)nl, fft_magic((unsigned)nl)};
+  const bool hm = a.mg[0] != 0u;  // fft_magic(n) of n >= 2 is never zero
+  const FastDiv fN{(unsigned)n, hm ? a.mg[0] : fft_magic((unsigned)n)}, fM{(unsigned)M, hm ? a.mg[1] : fft_magic((unsigned)M)};
+  const FastDiv fM1{(unsigned)(M + 1), hm ? a.mg[2] : fft_magic((unsigned)(M + 1))},
+      fL{(unsigned)nl, hm ? a.mg[3] : fft_magic((unsigned)nl)};
   // position-major smem: element (l, p) at p*nl + l
   auto S = [&](int l, int p) -> T2& { return bufA[(size_t)p * nl + l]; };
   T* Sr = reinterpret_cast<T*>(bufA);  // real view: real slot r of line l at (r/2 * nl + l)*2 + (r&1)
@@ -522,9 +528,9 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   // ---------------- transform ----------------
   T2* res;
   if (OP == OP_R2C || OP == OP_DCT2 || OP == OP_C2C_F || OP == OP_C2C_SOLVE)
-    res = smem_fft<-1, fft_max_radix<T, CONTIG>()>(bufA, bufB, nl, 1, nl, a.plan, a.tw.wM);
+    res = smem_fft<-1, fft_max_radix<T, CONTIG>()>(bufA, bufB, fL, 1, nl, a.plan, a.tw.wM);
   else
-    res = smem_fft<+1, fft_max_radix<T, CONTIG>()>(bufA, bufB, nl, 1, nl, a.plan, a.tw.wM);
+    res = smem_fft<+1, fft_max_radix<T, CONTIG>()>(bufA, bufB, fL, 1, nl, a.plan, a.tw.wM);
 
   if (OP == OP_C2C_SOLVE) {
     // normalise and divide by the eigenvalue sum, zero mode -> 0 (poisson.f90:458-471, 991-1005)
@@ -549,7 +555,7 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
     }
     __syncthreads();
     T2* other = (res == bufA) ? bufB : bufA;
-    res = smem_fft<+1, fft_max_radix<T, CONTIG>()>(res, other, nl, 1, nl, a.plan, a.tw.wM);
+    res = smem_fft<+1, fft_max_radix<T, CONTIG>()>(res, other, fL, 1, nl, a.plan, a.tw.wM);
   }
 
   // ---------------- store ----------------

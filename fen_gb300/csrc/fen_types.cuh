@@ -10,6 +10,22 @@ enum { FT_PERIODIC = 0, FT_DIRICHLET = 1, FT_NEUMANN = 2 };
 // Faces in the reference order (scalar.f90:24-36).
 enum { F_LEFT = 0, F_RIGHT = 1, F_BOTTOM = 2, F_TOP = 3, F_FRONT = 4, F_BACK = 5 };
 
+#ifdef FEN_DEBUG_CHECKS
+// Debug build (FEN_DEBUG_CHECKS): every field index passes a bounds check against its array.
+// An index outside it is counted, the first one is kept, and element 0 is used instead, so no
+// out-of-range access is made and nothing traps; fen_debug_checks() reports the record of
+// this translation unit (the library's stepping, transfer and operator kernels).
+static __device__ unsigned long long g_fen_oob_count;
+static __device__ long long g_fen_oob_first;
+__device__ __forceinline__ long long fen_checked(long long r, long long total) {
+  if (r < 0 || r >= total) {
+    if (atomicAdd(&g_fen_oob_count, 1ull) == 0ull) g_fen_oob_first = r;
+    return 0;
+  }
+  return r;
+}
+#endif
+
 // Ghosted field in HBM.  Fortran index (i, j, k), i in [0, n0+1], j in [0, n1+1] and, in
 // 3D, k in [0, n2+1] (gl = 1, scalar.f90:79-81).  Rows are padded to a multiple of four
 // elements and shifted by `off` = 3 so the first interior element of every row (i = 1)
@@ -23,8 +39,18 @@ struct Layout {
   long long sp;     // plane pitch, elements
   int off;
   long long total;  // elements to allocate
+  // multipliers m of the division by n0 and n1 as umulhi(x, m) (fft_magic, exact for x * n <
+  // 2^32), set on the host when n0, n1 <= 4096 (fastdiv = 1): CellWalk's start-up divisions
+  // then use no conversion instructions, which GB300 issues on its slow FP64 pipe
+  unsigned mg0 = 0, mg1 = 0;
+  int fastdiv = 0;
   __host__ __device__ __forceinline__ long long idx(int i, int j, int ks) const {
-    return (long long)off + i + (long long)sx * j + sp * ks;
+    const long long r = (long long)off + i + (long long)sx * j + sp * ks;
+#if defined(FEN_DEBUG_CHECKS) && defined(__CUDA_ARCH__)
+    return fen_checked(r, total);
+#else
+    return r;
+#endif
   }
 };
 
@@ -35,6 +61,21 @@ struct CellWalk {
   long long t0, stride;
   int i, j, k, si, sj, sk;
   __device__ __forceinline__ CellWalk(const Layout& L, long long t, long long s) : t0(t), stride(s) {
+    if (L.fastdiv && t < (1LL << 20) && s < (1LL << 20)) {
+      // thread index and stride below 2^20, n0 and n1 at most 4096: the products stay below 2^32
+      const unsigned tt = (unsigned)t, ss = (unsigned)s;
+      const unsigned r = (L.n0 > 1) ? __umulhi(tt, L.mg0) : tt;
+      const unsigned q = (L.n1 > 1) ? __umulhi(r, L.mg1) : r;
+      i = (int)(tt - r * (unsigned)L.n0);
+      j = (int)(r - q * (unsigned)L.n1);
+      k = (int)q;
+      const unsigned r2 = (L.n0 > 1) ? __umulhi(ss, L.mg0) : ss;
+      const unsigned q2 = (L.n1 > 1) ? __umulhi(r2, L.mg1) : r2;
+      si = (int)(ss - r2 * (unsigned)L.n0);
+      sj = (int)(r2 - q2 * (unsigned)L.n1);
+      sk = (int)q2;
+      return;
+    }
     long long r = t / L.n0;
     i = (int)(t - r * L.n0);
     j = (int)(r % L.n1);

@@ -240,6 +240,10 @@ module fen_gpu_mod
         end function fen_get_ibm_force
 
         ! ---- device timing and counters -------------------------------------------------------
+        integer(c_int) function fen_debug_checks(count, first) bind(C, name='fen_debug_checks')
+            import :: c_int, c_long_long
+            integer(c_long_long), intent(out) :: count, first
+        end function fen_debug_checks
         integer(c_int) function fen_sync(ctx) bind(C, name='fen_sync')
             import :: c_int, c_ptr
             type(c_ptr), value :: ctx

@@ -197,6 +197,13 @@ int fen_set_ibm_forcing(fen_ctx* ctx, int comp, int npoints, const int* ijk, con
                         const double* w, const double* c0);
 int fen_get_ibm_force(fen_ctx* ctx, int comp, double* fe);
 
+/* Bounds record of the debug build (libfen_gb300_debug.so, compiled with FEN_DEBUG_CHECKS):
+ * every field index of the library's kernels is checked against its array; an index outside
+ * is counted (count), the first is kept (first, an element offset), and element 0 is used in
+ * its place, so nothing is read or written out of range and nothing traps.  The release
+ * library reports count = -1 (no checks compiled).  No counterpart in FEN, whose debug builds
+ * rely on gfortran's -fcheck=all (src/Makefile.defs:13). */
+int fen_debug_checks(long long* count, long long* first);
 /* Synchronise the context stream. */
 int fen_sync(fen_ctx* ctx);
 /* Number of kernels this library launched on the context since creation. */
