@@ -84,19 +84,21 @@ def device_sms_and_clock():
     return sms, ghz
 
 
-def fp64_issue(instr_per_cell, cells, ms, sms=152, ghz=2.07):
+def fp64_issue(instr_per_cell, cells, ms, sms=None, ghz=None):
     """Achieved FP64 instruction rate of a kernel with `instr_per_cell` FP64 thread
     instructions per cell against the issue peak of 2 FP64 thread instructions per SM per
     cycle (`sms` SMs at `ghz`)."""
     if not instr_per_cell or not ms:
         return None
+    if sms is None or ghz is None:
+        sms, ghz = device_sms_and_clock()
     peak = 2 * sms * ghz
     got = instr_per_cell * cells / (ms / 1e3) / 1e9
     return {"achieved": round(got, 1), "peak": round(peak, 1), "unit": "G FP64 instr/s", "frac": round(got / peak, 4),
             "instr_per_cell": instr_per_cell}
 
 
-def roofline_block(dim, form, cells, stage_ms, peak, peak_kind, sms=152, ghz=2.07):
+def roofline_block(dim, form, cells, stage_ms, peak, peak_kind, sms=None, ghz=None):
     """Roofline of the dominant kernel, the predictor (the largest single kernel of the step in
     both forms): algorithmic bytes per cell x cells / its CUDA-event time against the measured
     HBM copy bandwidth; the whole step's algorithmic bytes beside it."""

@@ -79,7 +79,7 @@ _EXPORTS = [
     "fen_ensemble_adjoint_seed", "fen_ensemble_adjoint_backward", "fen_ensemble_adjoint_gradient",
     "fen_ensemble_adjoint_dts", "fen_set_split_pressure", "fen_set_ibm_forcing", "fen_get_ibm_force",
     "fen_upload_gl", "fen_download_gl", "fen_field_bounds", "fen_gradient", "fen_laplacian", "fen_add_advection",
-    "fen_save_state_mf", "fen_load_state_mf", "fen_adjoint_backward3",
+    "fen_save_state_mf", "fen_load_state_mf", "fen_adjoint_backward3", "fen_debug_checks",
 ]
 
 
@@ -155,6 +155,7 @@ def load_library(path=None):
     L.fen_ensemble_adjoint_backward.argtypes = [vp, dp]
     L.fen_ensemble_adjoint_gradient.argtypes = [vp, ctypes.c_int, dp, dp]
     L.fen_ensemble_adjoint_dts.argtypes = [vp, ctypes.c_int, dp, dp]
+    L.fen_debug_checks.argtypes = [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
     if path == LIB_PATH:
         _lib = L
     return L

@@ -34,6 +34,9 @@ using namespace fen;
 
 // Build knobs (on by default): the mixed form's two-instruction tridiagonal sweep, the mean of
 // phi removed in the correction, the half-spectrum pitch padded to 64 bytes.
+#ifndef FEN_THOMAS_DF
+#define FEN_THOMAS_DF 1  // mixed form, 3D solvers: the double-float sweep (k_thomas_df)
+#endif
 #ifndef FEN_THOMAS_FAST
 #define FEN_THOMAS_FAST 1
 #endif
@@ -148,6 +151,7 @@ struct fen_ctx {
   double *c1 = nullptr, *fac = nullptr;
   int* conv = nullptr;        // first row of the pivots' fixed point per system
   double tri_a = 0.0;         // sub-diagonal of the interior rows
+  int tab_pairs = 0;          // c1 / fac hold (hi, lo) float pairs (the double-float sweep)
   void* specC = nullptr;
   void* specR = nullptr;
   void* inv_lam = nullptr;
@@ -392,6 +396,12 @@ int init_tridiag(fen_ctx* c, int ax, int ncol, int nouter, const double* lamA, c
   k_thomas_tables<<<dim3(cdiv(ncol, 128), nouter), 128>>>(ncol, nouter, n, c->ta, c->tb, c->tc, lamA, lamB, form3, c->c1, c->fac,
                                                         c->conv);
   CK(cudaGetLastError());
+  // the mixed form's 3D solves sweep in double-float and read the tables as float pairs
+  c->tab_pairs = (FEN_THOMAS_DF && c->mixed && form3) ? 1 : 0;
+  if (c->tab_pairs) {
+    k_thomas_pair_tables<<<(int)std::min<long long>(cdiv(nt, 256), 4096), 256>>>(nt, c->c1, c->fac);
+    CK(cudaGetLastError());
+  }
   CK(cudaDeviceSynchronize());
   return 0;
 }
@@ -688,16 +698,24 @@ int launch_thomas(fen_ctx* c, const Stage& s) {
   // the mixed form's reciprocal-factor (3D) solves take the two-FMA sweep above the pivots'
   // fixed point; the FP64 form keeps the reference's operation order
   const bool fast = FEN_THOMAS_FAST && c->mixed && ta.form3;
+  const bool pairs = c->tab_pairs != 0;
+  {
+    const F2 av = split_d(ta.aval);
+    ta.avh = av.hi;
+    ta.avl = av.lo;
+  }
   if (real) {
     const dim3 g(cdiv(ta.ncol, kTh), s.tgrid.y, s.tgrid.z);
-    if (fast) k_thomas_mixed<0><<<g, kTh, 0, c->stream>>>(ta);
+    if (pairs) k_thomas_df<0><<<g, kTh, 0, c->stream>>>(ta);
+    else if (fast) k_thomas_mixed<0><<<g, kTh, 0, c->stream>>>(ta);
     else if (c->mixed) k_thomas<float, double><<<g, kTh, 0, c->stream>>>(ta);
     else k_thomas<double, double><<<g, kTh, 0, c->stream>>>(ta);
   } else {
     // complex right-hand sides: real and imaginary parts as two real systems per column
     ta.split2 = 1;
     const dim3 g(cdiv(2LL * ta.ncol, kTh), s.tgrid.y, s.tgrid.z);
-    if (fast) k_thomas_mixed<1><<<g, kTh, 0, c->stream>>>(ta);
+    if (pairs) k_thomas_df<1><<<g, kTh, 0, c->stream>>>(ta);
+    else if (fast) k_thomas_mixed<1><<<g, kTh, 0, c->stream>>>(ta);
     else if (c->mixed) k_thomas<float, double><<<g, kTh, 0, c->stream>>>(ta);
     else k_thomas<double, double><<<g, kTh, 0, c->stream>>>(ta);
   }

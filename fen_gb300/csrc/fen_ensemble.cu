@@ -57,6 +57,14 @@ constexpr int kCl = FEN_ENS_CLUSTER;   // CTAs per cluster (above 8: non-portabl
 #ifndef FEN_ENS_SPLIT
 #define FEN_ENS_SPLIT 1
 #endif
+// Elements per thread of the Poisson all-to-alls in the backward sweep's adjoint steps and
+// recomputed forward steps (register pressure of the backward kernel, which carries both)
+#ifndef FEN_ENS_ADJ_EPT
+#define FEN_ENS_ADJ_EPT 4
+#endif
+#ifndef FEN_ENS_REC_EPT
+#define FEN_ENS_REC_EPT 10
+#endif
 constexpr size_t kSmemLimit = 232448;  // opt-in dynamic shared memory per CTA (227 KB)
 constexpr size_t kSmemReserve = 1024;  // static shared memory of the kernel + slack
 
@@ -453,8 +461,8 @@ struct Pk {
 
   // ---- the Poisson solve: rhs in Z (real rows of stride 2 SR); returns phi's buffer and
   // leaves the FP64 mean of phi in s_f[4] (poisson.f90:416-505 with the mean removal) ----
+  template <int EPT = Batch<NT>::kElems>
   __device__ float2* poisson() {
-    constexpr int EPT = Batch<NT>::kElems;
     float2* SPEC = ens_fft<-1, NT>(S.Z, S.X, M, D.fM, SR, 1, D.px, S.twx);
     for (int t = threadIdx.x; t < M * npair; t += NT) {
       const int m = fdiv(t, D.fNP), k = t - m * npair;
@@ -569,6 +577,7 @@ struct Pk {
   // ---- one forward step (navier_stokes.f90:50-136, constant CFL) ----
   // rec_step >= 0 replays the recorded (dt, dt_o) of that step instead of the CFL update;
   // rec_out >= 0 records this step's (dt, dt_o).
+  template <int EPT = Batch<NT>::kElems>
   __device__ void fwd_step(int rec_step, int rec_out) {
     constexpr int CPT = Batch<NT>::kCells;
     if (threadIdx.x == 0) {
@@ -660,7 +669,7 @@ struct Pk {
       }
     }
     __syncthreads();
-    float2* PHI = poisson();
+    float2* PHI = poisson<EPT>();
     const float* Phf = reinterpret_cast<const float*>(PHI);
 
     // correction, p update, max(|u| + |v|)
@@ -717,10 +726,20 @@ struct Pk {
   // ---- one adjoint step (the transpose of fwd_step for fixed dt; see fen_adjoint.cuh) ----
   // Adjoint state: u^, v^ (rows with ghosts) in S.u, S.v, p^ in S.p, dv_o^ in HBM (ax, ay);
   // the forward step's input velocity (u, v) in HBM (fu, fv, full N x N arrays).
-  __device__ void adj_step(const float* fu, const float* fv, double dtd, double dt_od, float* ax, float* ay) {
-    const float dt = (float)dtd;
+  // Step s of the record; its forward input (u, v) is slot sl of the segment's step inputs.
+  // The coefficients and the HBM pointers are re-derived after the Poisson solve instead of
+  // being held across it (registers).
+  __device__ void adj_coef(int s, float& dt, float& A, float& B, float& rdt) const {
+    const double dtd = rec ? __ldg(rec + 2 * s) : 1.0, dt_od = rec ? __ldg(rec + 2 * s + 1) : 1.0;
+    dt = (float)dtd;
     const float rf = (float)dtd / (float)dt_od;
-    const float A = 1.0f + 0.5f * rf, B = -0.5f * rf, rdt = 1.0f / dt;
+    A = 1.0f + 0.5f * rf;
+    B = -0.5f * rf;
+    rdt = 1.0f / dt;
+  }
+  __device__ void adj_step(int s, int sl) {
+    float dt, A, B, rdt;
+    adj_coef(s, dt, A, B, rdt);
     // phi^ = p^ + dt D(v^)  -> Z
     for (int t = threadIdx.x; t < cells; t += NT) {
       const int m = fdiv(t, fN), i = t - m * N;
@@ -730,7 +749,14 @@ struct Pk {
     }
     __syncthreads();
     // b^ = P phi^ (symmetric); v*^ = v^ - (rho/dt) G b^  (in place)
-    float2* PHI = poisson();
+    float2* PHI = poisson<FEN_ENS_ADJ_EPT>();
+    adj_coef(s, dt, A, B, rdt);
+    const long long N2 = (long long)N * N;
+    const AdjLayout AL(N2, a.nseg, a.every);
+    float* ax = ablk ? ablk + AL.adj + 3 * N2 : nullptr;
+    float* ay = ablk ? ablk + AL.adj + 4 * N2 : nullptr;
+    const float* fu = ablk ? ablk + AL.seg + (long long)sl * 2 * N2 : nullptr;
+    const float* fv = ablk ? fu + N2 : nullptr;
     {
       const float* Phf = reinterpret_cast<const float*>(PHI);
       const float* Phn = reinterpret_cast<const float*>(peer(PHI, rp));
@@ -748,58 +774,124 @@ struct Pk {
     gsync();
     ghosts(S.u, S.v, nullptr);
     __syncthreads();
-    // p^ += dt D(v*^); dv^ = dv_o^ + dt A v*^ -> X, Y (rows with ghosts); dv_o^ = dt B v*^
-    for (int t = threadIdx.x; t < cells; t += NT) {
-      const int m = fdiv(t, fN), i = t - m * N;
-      const int im = (i == 0) ? N - 1 : -1;
-      const int c = t + N;
-      const float us = S.u[c], vs = S.v[c];
-      S.p[c] = S.p[c] + dt * (((us - S.u[c + im]) + (vs - S.v[c - N])) * idx);
-      float ox = 0.f, oy = 0.f;
-      if (active) {
-        const size_t gi = (size_t)r * M * N + t;
-        ox = ax[gi];
-        oy = ay[gi];
-        ax[gi] = dt * B * us;
-        ay[gi] = dt * B * vs;
+    // p^ += dt D(v*^); dv^ = dv_o^ + dt A v*^ -> X, Y (rows with ghosts); dv_o^ = dt B v*^.
+    // The HBM reads of dv_o^ are issued kAB cells at a time before any is used.
+    constexpr int kAB = (NT >= 1024) ? 4 : 8;
+    for (int b0 = 0; b0 < cells; b0 += kAB * NT) {
+      float ox[kAB], oy[kAB];
+#pragma unroll
+      for (int k = 0; k < kAB; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        ox[k] = 0.f;
+        oy[k] = 0.f;
+        if (active && t < cells) {
+          const size_t gi = (size_t)r * M * N + t;
+          ox[k] = ax[gi];
+          oy[k] = ay[gi];
+        }
       }
-      Xf[c] = ox + dt * A * us;
-      Yf[c] = oy + dt * A * vs;
+#pragma unroll
+      for (int k = 0; k < kAB; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < cells) {
+          const int m = fdiv(t, fN), i = t - m * N;
+          const int im = (i == 0) ? N - 1 : -1;
+          const int c = t + N;
+          const float us = S.u[c], vs = S.v[c];
+          S.p[c] = S.p[c] + dt * (((us - S.u[c + im]) + (vs - S.v[c - N])) * idx);
+          if (active) {
+            const size_t gi = (size_t)r * M * N + t;
+            ax[gi] = dt * B * us;
+            ay[gi] = dt * B * vs;
+          }
+          Xf[c] = ox[k] + dt * A * us;
+          Yf[c] = oy[k] + dt * A * vs;
+        }
+      }
     }
     gsync();
     ghosts(Xf, Yf, nullptr);
     __syncthreads();
-    // v^ = v*^ + N'(v)^T dv^ + mu L dv^   (navier_stokes.f90:297-323 transposed)
+    // v^ = v*^ + N'(v)^T dv^ + mu L dv^   (navier_stokes.f90:297-323 transposed).  The forward
+    // input velocity around (i, j) comes from HBM (periodic in both directions); its reads are
+    // issued kAS cells at a time before any is used, the u and v components in two passes so
+    // each keeps only its own seven forward values per cell live.
+    constexpr int kAS = (NT >= 1024) ? 2 : 4;
     const float mur = mu;
-    for (int t = threadIdx.x; t < cells; t += NT) {
-      const int m = fdiv(t, fN), i = t - m * N;
-      const int ip = (i + 1 == N) ? 1 - N : 1;
-      const int im = (i == 0) ? N - 1 : -1;
-      const int c = t + N;
-      const float* hu = Xf;
-      const float* hv = Yf;
-      // forward input velocity around (i, j) from HBM (periodic in both directions)
-      const int jg = r * M + m;
-      const size_t row = (size_t)jg * N, rowp = (size_t)wrapj(jg + 1) * N, rowm = (size_t)wrapj(jg - 1) * N;
-      const int i_p = i + ip, i_m = i + im;
-      float u0 = 0.f, uip = 0.f, uim = 0.f, ujp = 0.f, uimjp = 0.f, v0 = 0.f, vip = 0.f, vjp = 0.f, vjm = 0.f, vipjm = 0.f;
-      if (active) {
-        u0 = fu[row + i]; uip = fu[row + i_p]; uim = fu[row + i_m]; ujp = fu[rowp + i]; uimjp = fu[rowp + i_m];
-        v0 = fv[row + i]; vip = fv[row + i_p]; vjp = fv[rowp + i]; vjm = fv[rowm + i]; vipjm = fv[rowm + i_p];
+    const float* hu = Xf;
+    const float* hv = Yf;
+    for (int b0 = 0; b0 < cells; b0 += kAS * NT) {
+      float f[kAS][7];
+#pragma unroll
+      for (int k = 0; k < kAS; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+#pragma unroll
+        for (int e = 0; e < 7; ++e) f[k][e] = 0.f;
+        if (active && t < cells) {
+          const int m = fdiv(t, fN), i = t - m * N;
+          const int ip = (i + 1 == N) ? 1 - N : 1;
+          const int im = (i == 0) ? N - 1 : -1;
+          const int jg = r * M + m;
+          const size_t row = (size_t)jg * N, rowm = (size_t)wrapj(jg - 1) * N;
+          f[k][0] = fu[row + i]; f[k][1] = fu[row + i + ip]; f[k][2] = fu[row + i + im];
+          f[k][3] = fv[row + i]; f[k][4] = fv[row + i + ip]; f[k][5] = fv[rowm + i]; f[k][6] = fv[rowm + i + ip];
+        }
       }
-      const float Fu_p = (hu[c + ip] - hu[c]) * idx, Fu_m = (hu[c] - hu[c + im]) * idx;
-      const float Fv_p = (hv[c + N] - hv[c]) * idx, Fv_m = (hv[c] - hv[c - N]) * idx;
-      const float C_ij = (hu[c + N] - hu[c]) * idx + (hv[c + ip] - hv[c]) * idx;
-      const float C_ijm = (hu[c] - hu[c - N]) * idx + (hv[c + ip - N] - hv[c - N]) * idx;
-      const float C_imj = (hu[c + im + N] - hu[c + im]) * idx + (hv[c] - hv[c + im]) * idx;
-      const float gu_ = Fu_p * 0.5f * (uip + u0) + Fu_m * 0.5f * (u0 + uim) + C_ij * 0.25f * (vip + v0) +
-                        C_ijm * 0.25f * (vipjm + vjm);
-      const float gv_ = Fv_p * 0.5f * (vjp + v0) + Fv_m * 0.5f * (v0 + vjm) + C_ij * 0.25f * (ujp + u0) +
-                        C_imj * 0.25f * (uimjp + uim);
-      const float lu = ((hu[c + ip] + hu[c + im]) + (hu[c + N] + hu[c - N]) - 4.0f * hu[c]) * id2;
-      const float lv = ((hv[c + ip] + hv[c + im]) + (hv[c + N] + hv[c - N]) - 4.0f * hv[c]) * id2;
-      S.u[c] = S.u[c] + gu_ + mur * lu;
-      S.v[c] = S.v[c] + gv_ + mur * lv;
+#pragma unroll
+      for (int k = 0; k < kAS; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < cells) {
+          const int m = fdiv(t, fN), i = t - m * N;
+          const int ip = (i + 1 == N) ? 1 - N : 1;
+          const int im = (i == 0) ? N - 1 : -1;
+          const int c = t + N;
+          const float u0 = f[k][0], uip = f[k][1], uim = f[k][2];
+          const float v0 = f[k][3], vip = f[k][4], vjm = f[k][5], vipjm = f[k][6];
+          const float Fu_p = (hu[c + ip] - hu[c]) * idx, Fu_m = (hu[c] - hu[c + im]) * idx;
+          const float C_ij = (hu[c + N] - hu[c]) * idx + (hv[c + ip] - hv[c]) * idx;
+          const float C_ijm = (hu[c] - hu[c - N]) * idx + (hv[c + ip - N] - hv[c - N]) * idx;
+          const float gu_ = Fu_p * 0.5f * (uip + u0) + Fu_m * 0.5f * (u0 + uim) + C_ij * 0.25f * (vip + v0) +
+                            C_ijm * 0.25f * (vipjm + vjm);
+          const float lu = ((hu[c + ip] + hu[c + im]) + (hu[c + N] + hu[c - N]) - 4.0f * hu[c]) * id2;
+          S.u[c] = S.u[c] + gu_ + mur * lu;
+        }
+      }
+    }
+    for (int b0 = 0; b0 < cells; b0 += kAS * NT) {
+      float f[kAS][7];
+#pragma unroll
+      for (int k = 0; k < kAS; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+#pragma unroll
+        for (int e = 0; e < 7; ++e) f[k][e] = 0.f;
+        if (active && t < cells) {
+          const int m = fdiv(t, fN), i = t - m * N;
+          const int im = (i == 0) ? N - 1 : -1;
+          const int jg = r * M + m;
+          const size_t row = (size_t)jg * N, rowp = (size_t)wrapj(jg + 1) * N, rowm = (size_t)wrapj(jg - 1) * N;
+          f[k][0] = fu[row + i]; f[k][1] = fu[row + i + im]; f[k][2] = fu[rowp + i]; f[k][3] = fu[rowp + i + im];
+          f[k][4] = fv[row + i]; f[k][5] = fv[rowp + i]; f[k][6] = fv[rowm + i];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kAS; ++k) {
+        const int t = b0 + threadIdx.x + k * NT;
+        if (t < cells) {
+          const int m = fdiv(t, fN), i = t - m * N;
+          const int ip = (i + 1 == N) ? 1 - N : 1;
+          const int im = (i == 0) ? N - 1 : -1;
+          const int c = t + N;
+          const float u0 = f[k][0], uim = f[k][1], ujp = f[k][2], uimjp = f[k][3];
+          const float v0 = f[k][4], vjp = f[k][5], vjm = f[k][6];
+          const float Fv_p = (hv[c + N] - hv[c]) * idx, Fv_m = (hv[c] - hv[c - N]) * idx;
+          const float C_ij = (hu[c + N] - hu[c]) * idx + (hv[c + ip] - hv[c]) * idx;
+          const float C_imj = (hu[c + im + N] - hu[c + im]) * idx + (hv[c] - hv[c + im]) * idx;
+          const float gv_ = Fv_p * 0.5f * (vjp + v0) + Fv_m * 0.5f * (v0 + vjm) + C_ij * 0.25f * (ujp + u0) +
+                            C_imj * 0.25f * (uimjp + uim);
+          const float lv = ((hv[c + ip] + hv[c + im]) + (hv[c + N] + hv[c - N]) - 4.0f * hv[c]) * id2;
+          S.v[c] = S.v[c] + gv_ + mur * lv;
+        }
+      }
     }
     gsync();
     ghosts(S.u, S.v, nullptr);
@@ -872,18 +964,14 @@ __device__ void run_pack(const EnsArgs& a, const Pack& P, const ClassDesc& D, in
           k.store_rows(S.u, in);
           k.store_rows(S.v, in + N2);
         }
-        k.fwd_step(s, -1);
+        k.template fwd_step<FEN_ENS_REC_EPT>(s, -1);
       }
       k.gsync();  // step inputs of the segment written by every CTA of the run
       k.load_rows(adj, S.u);
       k.load_rows(adj ? adj + N2 : nullptr, S.v);
       k.load_rows(adj ? adj + 2 * N2 : nullptr, S.p);
       __syncthreads();
-      for (int s = s1 - 1; s >= s0; --s) {
-        const float* in = ab ? ab + AL.seg + (long long)(s - s0) * 2 * N2 : nullptr;
-        const double dts = k.rec ? k.rec[2 * s] : 1.0, dto = k.rec ? k.rec[2 * s + 1] : 1.0;
-        k.adj_step(in, in ? in + N2 : nullptr, dts, dto, adj ? adj + 3 * N2 : nullptr, adj ? adj + 4 * N2 : nullptr);
-      }
+      for (int s = s1 - 1; s >= s0; --s) k.adj_step(s, s - s0);
       k.store_rows(S.u, adj);
       k.store_rows(S.v, adj ? adj + N2 : nullptr);
       k.store_rows(S.p, adj ? adj + 2 * N2 : nullptr);

@@ -356,6 +356,12 @@ __device__ __forceinline__ T div_at(const LineArgs<T>& a, int i, int j, int k) {
 #define FEN_LINE_LB 4
 #endif
 constexpr int kLB = FEN_LINE_LB;
+// Elements per thread of the batched FP32 r2c pair loaders (LD_DIVMIX, LD_RESID); 1: the
+// element-at-a-time loop.
+#ifndef FEN_R2C_LB
+#define FEN_R2C_LB 2
+#endif
+constexpr int kLR = FEN_R2C_LB;
 
 template <typename T, int DIM, bool CONTIG, int OP, int LD, int ST>
 __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
@@ -385,7 +391,67 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   const T2* inC = reinterpret_cast<const T2*>(a.in);
 
   // ---------------- load ----------------
-  if (OP == OP_R2C || OP == OP_DCT2) {
+  if (OP == OP_R2C && CONTIG && sizeof(T) == 4 && kLR > 1 && (LD == LD_DIVMIX || LD == LD_RESID)) {
+    // FP32 r2c of the mixed form's pair loaders: kLR elements per thread evaluated before any
+    // store (their loads in flight together; the pair-divergence stores for the refinement
+    // follow in the second pass so they cannot order the loads)
+    const int work = nl * n;
+    F2 rod{0.f, 0.f};
+    if (LD == LD_RESID) rod = split_d(a.sc->rho_over_dt);
+    const T rdt = (LD == LD_DIVMIX) ? (T)a.sc->rho_over_dt : T(0);
+    const float* ph = (const float*)a.fsrc;
+    for (int t0 = tid; t0 < work; t0 += nth * kLR) {
+      F2 v[kLR];
+#pragma unroll
+      for (int b = 0; b < kLR; ++b) {
+        const int t = t0 + b * nth;
+        v[b] = F2{0.f, 0.f};
+        int l = 0, i = 0;
+        if (t < work) divmod(t, fN, l, i);
+        if (t < work && l < nlv) {
+          int j, k;
+          row_jk<DIM>(line0 + l, outer, j, k);
+          const long long c = a.L.idx(i + 1, j, kst<DIM>(k));
+          if (LD == LD_DIVMIX) {
+            v[b] = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
+                               a.ful, a.fvl, a.fwl, a.idp, i + 1, j, k);
+          } else {
+            // refinement right-hand side r = rho/dt D v* - L_h phi in double-float
+            const F2 bb = mul_pair(a.dvh[c], a.dvl[c], rod);
+            F2 lap = add_pair(lap_term(ph, c, 1, a.id2p[0]), lap_term(ph, c, a.L.sx, a.id2p[1]));
+            if (DIM == 3) lap = add_pair(lap, lap_term(ph, c, a.L.sp, a.id2p[2]));
+            float s, e;
+            two_sum(bb.hi, -lap.hi, s, e);
+            v[b] = F2{s, e + (bb.lo - lap.lo)};
+          }
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < kLR; ++b) {
+        const int t = t0 + b * nth;
+        if (t < work) {
+          int l, i;
+          divmod(t, fN, l, i);
+          T x = 0;
+          if (l < nlv) {
+            if (LD == LD_DIVMIX) {
+              if (a.dvh) {  // kept for the refinement's residual
+                int j, k;
+                row_jk<DIM>(line0 + l, outer, j, k);
+                const long long c = a.L.idx(i + 1, j, kst<DIM>(k));
+                a.dvh[c] = v[b].hi;
+                a.dvl[c] = v[b].lo;
+              }
+              x = (T)(v[b].hi + v[b].lo) * rdt;
+            } else {
+              x = (T)(v[b].hi + v[b].lo);
+            }
+          }
+          RS(l, i) = x;
+        }
+      }
+    }
+  } else if (OP == OP_R2C || OP == OP_DCT2) {
     // n reals per line -> packed complex (DCT2 reorders first: v_m = x_2m, v_{n-1-m} = x_2m+1)
     const int work = nl * n;
     F2 rod{0.f, 0.f};
@@ -692,6 +758,7 @@ struct ThomasArgs {
   const int* conv;            // [sys] first interior row of the fixed point (n - 1: none)
   int form3;
   int split2;                 // complex data swept as two real systems: thread 2c + part, part 0 re / 1 im
+  float avh, avl;             // aval as a (hi, lo) float pair (k_thomas_df)
 };
 
 // Elimination arithmetic: r - a d as one fused multiply-add, then the row factor.
@@ -974,6 +1041,168 @@ __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_mixed(ThomasArg
   for (; t >= 0; --t) {
     xn = fma(-c1[(long long)t * ns], xn, widen(X[(long long)t * sr]));
     X[(long long)t * sr] = narrow(xn);
+  }
+}
+
+// Mixed-form sweep in double-float arithmetic (FP32 pairs, about 48 significant bits): the
+// recurrences of k_thomas_mixed with every per-row operation on the FP32 pipe.  GB300 issues
+// FP64 at about 1/64 of its FP32 rate and the FP64 sweep is bound by that pipe; the pair form
+// costs about fourteen FP32 instructions per row and recurrence instead of one FP64 FMA, and
+// its rounding (2^-46 per operation) stays far below the FP32 spectrum it reads and writes.
+// The tables c1 and factor are read as (hi, lo) float pairs of the FP64 values
+// (k_thomas_pair_tables converts them in place at set-up).  FORM3 only.  Per system, the
+// last row's division and the change of variables at the fixed point run in FP64 (a handful
+// of instructions per system, not per row).
+__device__ __forceinline__ DF df_of(float2 v) { return DF{v.x, v.y}; }
+// x - g e for an FP32 x and pairs g, e (FMA-exact leading product, Knuth sum)
+__device__ __forceinline__ DF df_xmy(float x, DF g, DF e) {
+  const float p = g.h * e.h;
+  float pe = fmaf(g.h, e.h, -p);
+  pe = fmaf(g.h, e.l, pe);
+  pe = fmaf(g.l, e.h, pe);
+  float sh, sl;
+  two_sum(x, -p, sh, sl);
+  sl = sl - pe;
+  const float h = sh + sl;
+  return DF{h, sl - (h - sh)};
+}
+__device__ __forceinline__ double df_to_d(DF v) { return (double)v.h + (double)v.l; }
+__device__ __forceinline__ DF df_from_d(double x) {
+  const F2 q = split_d(x);
+  return DF{q.hi, q.lo};
+}
+
+template <int SPLIT2>
+__global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_df(ThomasArgs a) {
+  const int tcol = blockIdx.x * blockDim.x + threadIdx.x;
+  const int col = SPLIT2 ? (tcol >> 1) : tcol;
+  const int outer = blockIdx.y;
+  if (col >= a.ncol) return;
+  const int w = SPLIT2 ? 2 : 1;
+  float* X = reinterpret_cast<float*>(a.x) + ((long long)col * a.s_col + (long long)outer * a.s_outer) * w + (tcol & (w - 1));
+  const long long sys = (long long)outer * a.ncol + col;
+  const long long ns = (long long)a.ncol * a.nouter;
+  const float2* c1 = reinterpret_cast<const float2*>(a.c1) + sys;
+  const float2* f = reinterpret_cast<const float2*>(a.fac) + sys;
+  const int n = a.n;
+  const long long sr = a.s_row * w;
+  const DF av{a.avh, a.avl};
+  const int T = a.conv[sys];
+  const int t0 = (T < n - 1) ? T - 1 : n - 1;  // first row of the fixed point (n - 1: none)
+  // forward sweep, tabulated rows [0, t0): d_t = (r_t - a d_(t-1)) f_t
+  DF d{0.f, 0.f};
+  int t = 0;
+  for (; t + kTB <= t0; t += kTB) {
+    float xb[kTB];
+    float2 fb[kTB];
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      xb[q] = X[(long long)(t + q) * sr];
+      fb[q] = f[(long long)(t + q) * ns];
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      const DF r = (t + q == 0) ? DF{xb[q], 0.f} : df_xmy(xb[q], av, d);
+      d = dmul(r, df_of(fb[q]));
+      xb[q] = d.h;
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) X[(long long)(t + q) * sr] = xb[q];
+  }
+  for (; t < t0; ++t) {
+    const float x = X[(long long)t * sr];
+    const DF r = (t == 0) ? DF{x, 0.f} : df_xmy(x, av, d);
+    d = dmul(r, df_of(f[(long long)t * ns]));
+    X[(long long)t * sr] = d.h;
+  }
+  const double piv = df_to_d(df_of(f[(long long)(n - 1) * ns]));
+  DF xn;
+  if (t0 < n - 1) {
+    const double fsd = df_to_d(df_of(f[(long long)t0 * ns]));
+    const DF cs = df_of(c1[(long long)t0 * ns]);
+    const DF g = df_from_d(df_to_d(av) * fsd);
+    // converged rows [t0, n - 1): e_t = r_t - a d_(t-1) unscaled, e_t = x_t - (a f*) e_(t-1)
+    DF e = (t0 == 0) ? DF{X[0], 0.f} : df_xmy(X[(long long)t0 * sr], av, d);
+    X[(long long)t0 * sr] = e.h;
+    t = t0 + 1;
+    for (; t + kTB <= n - 1; t += kTB) {
+      float xb[kTB];
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) xb[q] = X[(long long)(t + q) * sr];
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) {
+        e = df_xmy(xb[q], g, e);
+        xb[q] = e.h;
+      }
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) X[(long long)(t + q) * sr] = xb[q];
+    }
+    for (; t < n - 1; ++t) {
+      e = df_xmy(X[(long long)t * sr], g, e);
+      X[(long long)t * sr] = e.h;
+    }
+    // last row: a d_(n-2) = (a f*) e_(n-2); the zero mode's pivot is exactly zero
+    const DF r = df_xmy(X[(long long)(n - 1) * sr], g, e);
+    const double xl = (piv != 0.0) ? df_to_d(r) / piv : 0.0;
+    X[(long long)(n - 1) * sr] = (float)xl;
+    // backward sweep on y = x / f*: y_t = e_t - c* y_(t+1); x_t = f* y_t in FP32
+    const float fs32 = (float)fsd;
+    DF y = df_from_d(xl / fsd);
+    t = n - 2;
+    for (; t - kTB + 1 >= t0; t -= kTB) {
+      float xb[kTB];
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) xb[q] = X[(long long)(t - q) * sr];
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) {
+        y = df_xmy(xb[q], cs, y);
+        xb[q] = y.h * fs32;
+      }
+#pragma unroll
+      for (int q = 0; q < kTB; ++q) X[(long long)(t - q) * sr] = xb[q];
+    }
+    for (; t >= t0; --t) {
+      y = df_xmy(X[(long long)t * sr], cs, y);
+      X[(long long)t * sr] = y.h * fs32;
+    }
+    xn = df_from_d(fsd * df_to_d(y));  // x_(t0), the start of the tabulated rows below
+  } else {
+    const DF r = df_xmy(X[(long long)(n - 1) * sr], av, d);
+    const double xl = (piv != 0.0) ? df_to_d(r) / piv : 0.0;
+    X[(long long)(n - 1) * sr] = (float)xl;
+    xn = df_from_d(xl);
+    t = n - 2;
+  }
+  // backward sweep, tabulated rows below t0: x_t = d_t - c1_t x_(t+1)
+  for (t = t0 - 1; t - kTB + 1 >= 0; t -= kTB) {
+    float xb[kTB];
+    float2 cb[kTB];
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      xb[q] = X[(long long)(t - q) * sr];
+      cb[q] = c1[(long long)(t - q) * ns];
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) {
+      xn = df_xmy(xb[q], df_of(cb[q]), xn);
+      xb[q] = xn.h;
+    }
+#pragma unroll
+    for (int q = 0; q < kTB; ++q) X[(long long)(t - q) * sr] = xb[q];
+  }
+  for (; t >= 0; --t) {
+    xn = df_xmy(X[(long long)t * sr], df_of(c1[(long long)t * ns]), xn);
+    X[(long long)t * sr] = xn.h;
+  }
+}
+
+// The FP64 tables c1 and factor rewritten in place as (hi, lo) float pairs (k_thomas_df):
+// hi = the FP64 value rounded to FP32, lo = the remainder rounded to FP32.
+static __global__ void k_thomas_pair_tables(long long nt, double* c1, double* fac) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nt; i += (long long)gridDim.x * blockDim.x) {
+    const F2 p = split_d(c1[i]), q = split_d(fac[i]);
+    reinterpret_cast<float2*>(c1)[i] = make_float2(p.hi, p.lo);
+    reinterpret_cast<float2*>(fac)[i] = make_float2(q.hi, q.lo);
   }
 }
 

@@ -25,7 +25,7 @@ def test_stage_bytes_are_the_algorithmic_totals():
 def test_roofline_block():
     stage = {k: 0.0 for k in bench.STAGES}
     stage.update(predictor=2.6, forward_x=0.8, spectral=1.8, inverse_x=0.6, correct=0.26)
-    r = bench.roofline_block(3, "fp64", 256 ** 3, stage, 6660.6, "measured")
+    r = bench.roofline_block(3, "fp64", 256 ** 3, stage, 6660.6, "measured", sms=152, ghz=2.07)
     assert r["kernel"] == "k_predictor_tile" and r["bytes_per_cell"] == 104
     assert r["achieved"] == pytest.approx(104 * 256 ** 3 / 2.6e-3 / 1e9, rel=1e-3)
     assert r["frac"] == pytest.approx(r["achieved"] / 6660.6, rel=1e-3)
@@ -34,7 +34,7 @@ def test_roofline_block():
     m = bench.roofline_block(3, "mixed", 512 * 256 * 384, stage, 6660.6, "measured")
     assert m["kernel"] == "k_predictor_df_tile" and m["bytes_per_cell"] == 104
     assert m["traffic"] == int(100.4 * 512 * 256 * 384) and "256x128x192" in m["traffic_source"]
-    d2 = bench.roofline_block(2, "fp64", 128 * 128, stage, 6660.6, "measured")
+    d2 = bench.roofline_block(2, "fp64", 128 * 128, stage, 6660.6, "measured", sms=152, ghz=2.07)
     assert d2["bytes_per_cell"] == 72 and d2["step_algorithmic_bytes_per_cell"] == 168
 
 
