@@ -500,7 +500,7 @@ class Ensemble:
     """
 
     def __init__(self, n, viscosity, length=2 * np.pi, CFL=0.4, forcing=(1.0, 4), lib=None):
-        self._L = lib or load_library()
+        self._L = load_library(lib) if (lib is None or isinstance(lib, str)) else lib
         n = np.ascontiguousarray(n, dtype=np.int32)
         nu = np.ascontiguousarray(viscosity, dtype=np.float64)
         if n.shape != nu.shape or n.ndim != 1:

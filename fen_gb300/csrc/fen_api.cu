@@ -34,6 +34,9 @@ using namespace fen;
 
 // Build knobs (on by default): the mixed form's two-instruction tridiagonal sweep, the mean of
 // phi removed in the correction, the half-spectrum pitch padded to 64 bytes.
+#ifndef FEN_CHECK_CTAS_PER_SM
+#define FEN_CHECK_CTAS_PER_SM 16  // 256-thread CTAs per SM of the diagnostics pass (k_checks*; 4: FP64 256^3 0.357 -> 0.337 ms)
+#endif
 #ifndef FEN_THOMAS_DF
 #define FEN_THOMAS_DF 1  // mixed form, 3D solvers: the double-float sweep (k_thomas_df)
 #endif
@@ -1377,7 +1380,7 @@ int fen_ctx_create(const fen_params* P, fen_ctx** out) {
       cudaMallocHost((void**)&c->sc_host, sizeof(StepScalars)) != cudaSuccess) { fen_ctx_destroy(c); return fail(FEN_ERR_NOMEM, "scalars"); }
   memset(c->sc_host, 0, sizeof(StepScalars));
   cudaMemset(c->sc, 0, sizeof(StepScalars));
-  c->nred = 152 * 4;
+  c->nred = 152 * FEN_CHECK_CTAS_PER_SM;
   if ((r = alloc(&c->pdiv, c->nred)) || (r = alloc(&c->pvel, c->nred))) { fen_ctx_destroy(c); return r; }
   if (cudaMalloc((void**)&c->nan_flag, sizeof(int)) != cudaSuccess) { fen_ctx_destroy(c); return fail(FEN_ERR_NOMEM, "flag"); }
   cudaMemset(c->nan_flag, 0, sizeof(int));
