@@ -756,6 +756,7 @@ int ghost(fen_ctx* c, int nf, T* const* ptr, const int* ids, bool homogeneous = 
     GhostCount g = (c->dim == 3) ? ghost_count<3>(c->L, G.bc[q]) : ghost_count<2>(c->L, G.bc[q]);
     G.n[q] = g.a + g.b + g.c;
     G.shift[q] = 0.0;
+    G.gd[q] = (c->dim == 3) ? ghost_div<3>(c->L, G.bc[q]) : ghost_div<2>(c->L, G.bc[q]);
     mx = std::max(mx, G.n[q]);
   }
   dim3 grid(std::min(cdiv(mx, 256), 4096), nf);
@@ -990,6 +991,7 @@ int ghost_pairs(fen_ctx* c, int nf, const int* ids, float* const* hi = nullptr, 
     G.bc[q] = field_bc(c, ids[q]);
     GhostCount g = (c->dim == 3) ? ghost_count<3>(c->L, G.bc[q]) : ghost_count<2>(c->L, G.bc[q]);
     G.n[q] = g.a + g.b + g.c;
+    G.gd[q] = (c->dim == 3) ? ghost_div<3>(c->L, G.bc[q]) : ghost_div<2>(c->L, G.bc[q]);
     mx = std::max(mx, G.n[q]);
   }
   dim3 grid(std::min(cdiv(mx, 256), 4096), nf);

@@ -57,6 +57,12 @@ constexpr int kCl = FEN_ENS_CLUSTER;   // CTAs per cluster (above 8: non-portabl
 #ifndef FEN_ENS_SPLIT
 #define FEN_ENS_SPLIT 1
 #endif
+// Cells given to the 4-CTA launch, in percent of its SMs' proportional share (the small
+// runs it takes cost more per cell; fen_ensemble_tune picks among 60..100 per device).  On the
+// bench ensemble (512 runs, N in 64..256): 60: 34.0, 80: 36.7, 100: 32.6, 120: 28.3 Gcell-steps/s.
+#ifndef FEN_ENS_SHARE
+#define FEN_ENS_SHARE 80
+#endif
 // Elements per thread of the Poisson all-to-alls in the backward sweep's adjoint steps and
 // recomputed forward steps (register pressure of the backward kernel, which carries both)
 #ifndef FEN_ENS_ADJ_EPT
@@ -1110,6 +1116,7 @@ struct fen_ensemble {
   size_t smem4 = 0;
   int nclusters4 = 0;
   bool split = FEN_ENS_SPLIT != 0;
+  int share = FEN_ENS_SHARE;  // percent of the 4-CTA launch's proportional share of the cells
   cudaStream_t stream2 = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
   cudaStream_t stream = nullptr;
@@ -1277,7 +1284,7 @@ int build_packs(fen_ensemble* e, const std::vector<int>& subset) {
       std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return e->n[a] < e->n[b]; });
       double total = 0.0;
       for (int q : order) total += (double)e->n[q] * e->n[q];
-      const double target = total * (4.0 * n4) / (4.0 * n4 + (double)kCl * nc);
+      const double target = 0.01 * e->share * total * (4.0 * n4) / (4.0 * n4 + (double)kCl * nc);
       double acc = 0.0;
       for (int q : order) {
         const double w = (double)e->n[q] * e->n[q];
@@ -1794,7 +1801,7 @@ int fen_ensemble_tune(fen_ensemble* e, int steps, const char* cache_path) {
   if (!e || steps < 1) return fen_internal_fail(FEN_ERR_ARG, "bad argument");
   const std::string key = device_key(e->dev);
   std::map<int, int> cached_g;
-  int cached_t = 0;
+  int cached_t = 0, cached_s = 0;
   if (cache_path && cache_path[0]) {
     std::ifstream f(cache_path);
     std::string line;
@@ -1805,15 +1812,17 @@ int fen_ensemble_tune(fen_ensemble* e, int steps, const char* cache_path) {
       if (!(ss >> k >> what >> a)) continue;
       if (k != key) continue;
       if (what == "threads") cached_t = a;
+      else if (what == "share") cached_s = a;
       else if (what == "N" && (ss >> b)) cached_g[a] = b;
     }
   }
-  bool all = cached_t == 512 || cached_t == 1024;
+  bool all = (cached_t == 512 || cached_t == 1024) && cached_s > 0;
   for (int N : e->cls_n) all = all && cached_g.count(N) && g_feasible(N, cached_g[N]);
   int r;
   if (all) {
     for (size_t c = 0; c < e->cls_n.size(); ++c) e->cls_g[c] = cached_g[e->cls_n[c]];
     e->threads = cached_t;
+    e->share = cached_s;
     return build_packs(e, {});
   }
   // back up the state and the scalars
@@ -1876,6 +1885,19 @@ int fen_ensemble_tune(fen_ensemble* e, int steps, const char* cache_path) {
     if (!r && ms < best_t) { best_t = ms; bt = T; }
   }
   e->threads = bt;
+  // the 4-CTA launch's share of the cells: the two concurrent launches should end together
+  if (!r && e->split && kCl == 8) {
+    float best_s = 1e30f;
+    int bs = e->share;
+    for (int sh : {60, 70, 80, 90, 100}) {
+      e->share = sh;
+      float ms = 0.f;
+      r = trial({}, &ms);
+      if (r) break;
+      if (ms < best_s) { best_s = ms; bs = sh; }
+    }
+    e->share = bs;
+  }
   e->scal = scal0;
   e->scal_dirty = true;
   cudaFree(backup);
@@ -1885,6 +1907,7 @@ int fen_ensemble_tune(fen_ensemble* e, int steps, const char* cache_path) {
     std::ofstream f(cache_path, std::ios::app);
     for (size_t c = 0; c < e->cls_n.size(); ++c) f << key << " N " << e->cls_n[c] << " " << e->cls_g[c] << "\n";
     f << key << " threads " << e->threads << "\n";
+    f << key << " share " << e->share << "\n";
   }
   return 0;
 }

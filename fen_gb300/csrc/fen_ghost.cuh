@@ -9,6 +9,7 @@
 // ghosts of several fields without ordering passes: threads write only ghost cells and
 // overwritten cells and read only interior cells that no thread writes.
 #pragma once
+#include "fen_fft.cuh"
 #include "fen_types.cuh"
 
 namespace fen {
@@ -155,6 +156,69 @@ __device__ __forceinline__ void ghost_target(const Layout& L, const FieldBC& bc,
   (void)nk;
 }
 
+// ghost_target with 32-bit multiply-high divisions (fft_magic multipliers set on the host):
+// the 64-bit divisions by run-time divisors compile to conversion sequences, which GB300
+// issues on its narrow FP64 pipe.  Valid when every quotient's numerator times its divisor
+// stays below 2^32 (ghost_fast_ok); the cell is the same.
+struct GhostDiv {
+  int ok;
+  unsigned a0, a1, b0, b1, c0, c1;  // x faces: 2 + xov, n1 - yov; y faces: n0 + 2, 2 + yov; z faces: n0 + 2, n1 + 2
+};
+__device__ __forceinline__ unsigned gdiv(unsigned x, unsigned d, unsigned m) { return d > 1 ? __umulhi(x, m) : x; }
+
+template <int DIM>
+__host__ inline GhostDiv ghost_div(const Layout& L, const FieldBC& bc) {
+  const int xov = (bc.c == 'x' && bc.type[F_RIGHT] == FT_DIRICHLET);
+  const int yov = (bc.c == 'y' && bc.type[F_TOP] == FT_DIRICHLET);
+  const GhostCount g = ghost_count<DIM>(L, bc);
+  GhostDiv d;
+  const unsigned long long lim = 1ull << 32;
+  const unsigned long long wa = 2 + xov, na = L.n1 - yov, ni = L.n0 + 2, wb = 2 + yov, nj = L.n1 + 2;
+  // numerators: t < g.a (by wa), t / wa (by na); t < g.b (by ni), t / ni (by wb); t < g.c (by ni), t / ni (by nj)
+  d.ok = ((unsigned long long)g.a * wa < lim) && ((unsigned long long)(g.a / wa + 1) * na < lim) &&
+         ((unsigned long long)g.b * ni < lim) && ((unsigned long long)(g.b / ni + 1) * wb < lim) &&
+         ((unsigned long long)g.c * ni < lim) && ((unsigned long long)(g.c / ni + 1) * nj < lim);
+  d.a0 = fft_magic((unsigned)wa); d.a1 = fft_magic((unsigned)na);
+  d.b0 = fft_magic((unsigned)ni); d.b1 = fft_magic((unsigned)wb);
+  d.c0 = fft_magic((unsigned)ni); d.c1 = fft_magic((unsigned)nj);
+  return d;
+}
+
+template <int DIM>
+__device__ __forceinline__ void ghost_target_fast(const Layout& L, const FieldBC& bc, const GhostDiv& D, long long t64,
+                                                  int& i, int& j, int& k) {
+  const unsigned xov = (bc.c == 'x' && bc.type[F_RIGHT] == FT_DIRICHLET);
+  const unsigned yov = (bc.c == 'y' && bc.type[F_TOP] == FT_DIRICHLET);
+  const unsigned zov = (DIM == 3 && bc.c == 'z' && bc.type[F_BACK] == FT_DIRICHLET);
+  const unsigned nk = (DIM == 3) ? (unsigned)L.n2 - zov : 1u;
+  const unsigned wa = 2 + xov, na = (unsigned)L.n1 - yov, ni = (unsigned)L.n0 + 2, wb = 2 + yov, nj = (unsigned)L.n1 + 2;
+  const unsigned ga = wa * na * nk, gb = wb * ni * nk;
+  unsigned t = (unsigned)t64;
+  if (t < ga) {
+    const unsigned r = gdiv(t, wa, D.a0), s = t - r * wa;
+    const unsigned q = gdiv(r, na, D.a1);
+    j = 1 + (int)(r - q * na);
+    k = 1 + (int)q;
+    i = (s == 0) ? 0 : (s == 1) ? L.n0 + 1 : L.n0;
+    return;
+  }
+  t -= ga;
+  if (t < gb) {
+    const unsigned r = gdiv(t, ni, D.b0);
+    i = (int)(t - r * ni);
+    const unsigned q = gdiv(r, wb, D.b1), s = r - q * wb;
+    k = 1 + (int)q;
+    j = (s == 0) ? 0 : (s == 1) ? L.n1 + 1 : L.n1;
+    return;
+  }
+  t -= gb;
+  const unsigned r = gdiv(t, ni, D.c0);
+  i = (int)(t - r * ni);
+  const unsigned q = gdiv(r, nj, D.c1);
+  j = (int)(r - q * nj);
+  k = (q == 0) ? 0 : (q == 1) ? L.n2 + 1 : L.n2;
+}
+
 // Up to four fields per launch (blockIdx.y selects the field).
 template <typename T>
 struct GhostBatch {
@@ -162,6 +226,7 @@ struct GhostBatch {
   FieldBC bc[4];
   long long n[4];
   double shift[4];
+  GhostDiv gd[4];
 };
 
 template <typename T, int DIM>
@@ -171,7 +236,8 @@ __global__ void __launch_bounds__(256) k_ghost_fill(Layout L, GhostBatch<T> G) {
   Resolve<T, DIM> R{PtrSrc<T>{G.f[q]}, L, G.bc[q], G.shift[q]};
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
-    ghost_target<DIM>(L, G.bc[q], t, i, j, k);
+    if (G.gd[q].ok) ghost_target_fast<DIM>(L, G.bc[q], G.gd[q], t, i, j, k);
+    else ghost_target<DIM>(L, G.bc[q], t, i, j, k);
     const T v = R.at(i, j, k);
     G.f[q][L.idx(i, j, kst<DIM>(k))] = v;
   }

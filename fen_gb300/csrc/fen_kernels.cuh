@@ -1053,6 +1053,19 @@ __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_mixed(ThomasArg
 // (k_thomas_pair_tables converts them in place at set-up).  FORM3 only.  Per system, the
 // last row's division and the change of variables at the fixed point run in FP64 (a handful
 // of instructions per system, not per row).
+// Rows per load batch and resident 128-thread CTAs per SM of k_thomas_df.
+// 8 rows in flight per thread at 70 registers (6 CTAs of 128 per SM).  Measured on the mixed
+// channel (spectral stage, two sweeps): 0.52 ms; 4 rows at 40 registers (12 CTAs, the whole
+// grid resident at once) 0.80 ms; 4 rows at 48 registers (10 CTAs) 0.63 ms; with the systems
+// numbered across the outer rows instead of padded per row, 0.55 ms.  The rows in flight
+// matter more than the resident warps.
+#ifndef FEN_THOMAS_DF_TB
+#define FEN_THOMAS_DF_TB 8
+#endif
+#ifndef FEN_THOMAS_DF_MINB
+#define FEN_THOMAS_DF_MINB 6
+#endif
+constexpr int kTBD = FEN_THOMAS_DF_TB;
 __device__ __forceinline__ DF df_of(float2 v) { return DF{v.x, v.y}; }
 // x - g e for an FP32 x and pairs g, e (FMA-exact leading product, Knuth sum)
 __device__ __forceinline__ DF df_xmy(float x, DF g, DF e) {
@@ -1073,7 +1086,7 @@ __device__ __forceinline__ DF df_from_d(double x) {
 }
 
 template <int SPLIT2>
-__global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_df(ThomasArgs a) {
+__global__ void __launch_bounds__(128, FEN_THOMAS_DF_MINB) k_thomas_df(ThomasArgs a) {
   const int tcol = blockIdx.x * blockDim.x + threadIdx.x;
   const int col = SPLIT2 ? (tcol >> 1) : tcol;
   const int outer = blockIdx.y;
@@ -1092,22 +1105,22 @@ __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_df(ThomasArgs a
   // forward sweep, tabulated rows [0, t0): d_t = (r_t - a d_(t-1)) f_t
   DF d{0.f, 0.f};
   int t = 0;
-  for (; t + kTB <= t0; t += kTB) {
-    float xb[kTB];
-    float2 fb[kTB];
+  for (; t + kTBD <= t0; t += kTBD) {
+    float xb[kTBD];
+    float2 fb[kTBD];
 #pragma unroll
-    for (int q = 0; q < kTB; ++q) {
+    for (int q = 0; q < kTBD; ++q) {
       xb[q] = X[(long long)(t + q) * sr];
       fb[q] = f[(long long)(t + q) * ns];
     }
 #pragma unroll
-    for (int q = 0; q < kTB; ++q) {
+    for (int q = 0; q < kTBD; ++q) {
       const DF r = (t + q == 0) ? DF{xb[q], 0.f} : df_xmy(xb[q], av, d);
       d = dmul(r, df_of(fb[q]));
       xb[q] = d.h;
     }
 #pragma unroll
-    for (int q = 0; q < kTB; ++q) X[(long long)(t + q) * sr] = xb[q];
+    for (int q = 0; q < kTBD; ++q) X[(long long)(t + q) * sr] = xb[q];
   }
   for (; t < t0; ++t) {
     const float x = X[(long long)t * sr];
@@ -1125,17 +1138,17 @@ __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_df(ThomasArgs a
     DF e = (t0 == 0) ? DF{X[0], 0.f} : df_xmy(X[(long long)t0 * sr], av, d);
     X[(long long)t0 * sr] = e.h;
     t = t0 + 1;
-    for (; t + kTB <= n - 1; t += kTB) {
-      float xb[kTB];
+    for (; t + kTBD <= n - 1; t += kTBD) {
+      float xb[kTBD];
 #pragma unroll
-      for (int q = 0; q < kTB; ++q) xb[q] = X[(long long)(t + q) * sr];
+      for (int q = 0; q < kTBD; ++q) xb[q] = X[(long long)(t + q) * sr];
 #pragma unroll
-      for (int q = 0; q < kTB; ++q) {
+      for (int q = 0; q < kTBD; ++q) {
         e = df_xmy(xb[q], g, e);
         xb[q] = e.h;
       }
 #pragma unroll
-      for (int q = 0; q < kTB; ++q) X[(long long)(t + q) * sr] = xb[q];
+      for (int q = 0; q < kTBD; ++q) X[(long long)(t + q) * sr] = xb[q];
     }
     for (; t < n - 1; ++t) {
       e = df_xmy(X[(long long)t * sr], g, e);
@@ -1149,17 +1162,17 @@ __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_df(ThomasArgs a
     const float fs32 = (float)fsd;
     DF y = df_from_d(xl / fsd);
     t = n - 2;
-    for (; t - kTB + 1 >= t0; t -= kTB) {
-      float xb[kTB];
+    for (; t - kTBD + 1 >= t0; t -= kTBD) {
+      float xb[kTBD];
 #pragma unroll
-      for (int q = 0; q < kTB; ++q) xb[q] = X[(long long)(t - q) * sr];
+      for (int q = 0; q < kTBD; ++q) xb[q] = X[(long long)(t - q) * sr];
 #pragma unroll
-      for (int q = 0; q < kTB; ++q) {
+      for (int q = 0; q < kTBD; ++q) {
         y = df_xmy(xb[q], cs, y);
         xb[q] = y.h * fs32;
       }
 #pragma unroll
-      for (int q = 0; q < kTB; ++q) X[(long long)(t - q) * sr] = xb[q];
+      for (int q = 0; q < kTBD; ++q) X[(long long)(t - q) * sr] = xb[q];
     }
     for (; t >= t0; --t) {
       y = df_xmy(X[(long long)t * sr], cs, y);
@@ -1174,21 +1187,21 @@ __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_df(ThomasArgs a
     t = n - 2;
   }
   // backward sweep, tabulated rows below t0: x_t = d_t - c1_t x_(t+1)
-  for (t = t0 - 1; t - kTB + 1 >= 0; t -= kTB) {
-    float xb[kTB];
-    float2 cb[kTB];
+  for (t = t0 - 1; t - kTBD + 1 >= 0; t -= kTBD) {
+    float xb[kTBD];
+    float2 cb[kTBD];
 #pragma unroll
-    for (int q = 0; q < kTB; ++q) {
+    for (int q = 0; q < kTBD; ++q) {
       xb[q] = X[(long long)(t - q) * sr];
       cb[q] = c1[(long long)(t - q) * ns];
     }
 #pragma unroll
-    for (int q = 0; q < kTB; ++q) {
+    for (int q = 0; q < kTBD; ++q) {
       xn = df_xmy(xb[q], df_of(cb[q]), xn);
       xb[q] = xn.h;
     }
 #pragma unroll
-    for (int q = 0; q < kTB; ++q) X[(long long)(t - q) * sr] = xb[q];
+    for (int q = 0; q < kTBD; ++q) X[(long long)(t - q) * sr] = xb[q];
   }
   for (; t >= 0; --t) {
     xn = df_xmy(X[(long long)t * sr], df_of(c1[(long long)t * ns]), xn);

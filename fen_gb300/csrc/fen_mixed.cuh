@@ -568,6 +568,7 @@ struct GhostDFBatch {
   float* lo[4];
   FieldBC bc[4];
   long long n[4];
+  GhostDiv gd[4];
 };
 
 template <int DIM>
@@ -577,7 +578,8 @@ __global__ void __launch_bounds__(256) k_ghost_fill_df(Layout L, GhostDFBatch G)
   Resolve<double, DIM, PairSrc> R{PairSrc{G.hi[q], G.lo[q]}, L, G.bc[q], 0.0};
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
-    ghost_target<DIM>(L, G.bc[q], t, i, j, k);
+    if (G.gd[q].ok) ghost_target_fast<DIM>(L, G.bc[q], G.gd[q], t, i, j, k);
+    else ghost_target<DIM>(L, G.bc[q], t, i, j, k);
     const double v = R.at(i, j, k);
     const long long o = L.idx(i, j, kst<DIM>(k));
     const float h = (float)v;

@@ -187,3 +187,89 @@ def test_order_preserving_keys_and_nan_bits():
     nan = np.array([0x7FF8000000000000, 0x7FF0000000000001, 0xFFF8000000000000 - 2 ** 64,
                     0xFFFFFFFFFFFFFFFF - 2 ** 64], dtype=np.int64)
     assert nan_bits(nan).all() and np.isnan(nan.view(np.float64)).all()
+
+
+# ---- ghost fill: work index -> ghost cell (ghost_count / ghost_target / ghost_div /
+# ghost_target_fast in fen_gb300/csrc/fen_ghost.cuh) ----
+
+def _ghost_count(dim, n0, n1, n2, c, right, top, back):
+    xov = int(c == "x" and right == "D")
+    yov = int(c == "y" and top == "D")
+    zov = int(dim == 3 and c == "z" and back == "D")
+    nk = n2 - zov if dim == 3 else 1
+    a = (2 + xov) * (n1 - yov) * nk
+    b = (2 + yov) * (n0 + 2) * nk
+    cc = (2 + zov) * (n0 + 2) * (n1 + 2) if dim == 3 else 0
+    return a, b, cc, xov, yov, zov, nk
+
+
+def _ghost_target(dim, n0, n1, n2, c, right, top, back, t):
+    a, b, cc, xov, yov, zov, nk = _ghost_count(dim, n0, n1, n2, c, right, top, back)
+    if t < a:
+        w = 2 + xov
+        s, r = t % w, t // w
+        j, k = 1 + r % (n1 - yov), 1 + r // (n1 - yov)
+        return (0 if s == 0 else n0 + 1 if s == 1 else n0), j, k
+    t -= a
+    if t < b:
+        ni = n0 + 2
+        i, r = t % ni, t // ni
+        w = 2 + yov
+        s, k = r % w, 1 + r // w
+        return i, (0 if s == 0 else n1 + 1 if s == 1 else n1), k
+    t -= b
+    ni, nj = n0 + 2, n1 + 2
+    i, r = t % ni, t // ni
+    j, s = r % nj, r // nj
+    return i, j, (0 if s == 0 else n2 + 1 if s == 1 else n2)
+
+
+def _ghost_fast(dim, n0, n1, n2, c, right, top, back):
+    """ghost_div's validity test and ghost_target_fast's 32-bit multiply-high mapping."""
+    a, b, cc, xov, yov, zov, nk = _ghost_count(dim, n0, n1, n2, c, right, top, back)
+    wa, na, ni, wb, nj = 2 + xov, n1 - yov, n0 + 2, 2 + yov, n1 + 2
+    lim = 2 ** 32
+    ok = (a * wa < lim and (a // wa + 1) * na < lim and b * ni < lim and (b // ni + 1) * wb < lim
+          and cc * ni < lim and (cc // ni + 1) * nj < lim)
+
+    def target(t):
+        if t < a:
+            r = fdiv(t, wa)
+            s = t - r * wa
+            q = fdiv(r, na)
+            return (0 if s == 0 else n0 + 1 if s == 1 else n0), 1 + r - q * na, 1 + q
+        t -= a
+        if t < b:
+            r = fdiv(t, ni)
+            q = fdiv(r, wb)
+            s = r - q * wb
+            return t - r * ni, (0 if s == 0 else n1 + 1 if s == 1 else n1), 1 + q
+        t -= b
+        r = fdiv(t, ni)
+        q = fdiv(r, nj)
+        return t - r * ni, r - q * nj, (0 if q == 0 else n2 + 1 if q == 1 else n2)
+
+    return ok, a + b + cc, target
+
+
+@pytest.mark.parametrize("dim,n", [(3, (12, 16, 10)), (3, (24, 6, 9)), (2, (32, 24, 1)), (3, (2, 2, 2)),
+                                   (2, (3, 2, 1))])
+@pytest.mark.parametrize("c", ["x", "y", "z", "c"])
+@pytest.mark.parametrize("walls", ["PPP", "DDD", "PDP", "DPD"])
+def test_ghost_target_fast_matches(dim, n, c, walls):
+    right, top, back = walls
+    ok, total, fast = _ghost_fast(dim, *n, c, right, top, back)
+    assert ok
+    for t in range(total):
+        assert fast(t) == _ghost_target(dim, *n, c, right, top, back, t), t
+
+
+def test_ghost_fast_bound_covers_bench_grids():
+    # the 512 x 256 x 384 channel and the 256^3 box take the fast mapping; 4096^3 does not
+    for n in [(512, 256, 384), (256, 256, 256), (1024, 1024, 1024)]:
+        for c in "xyzc":
+            ok, total, fast = _ghost_fast(3, *n, c, "P", "D", "P")
+            assert ok
+            for t in [0, 1, total // 3, total // 2, total - 1]:
+                assert fast(t) == _ghost_target(3, *n, c, "P", "D", "P", t)
+    assert not _ghost_fast(3, 4096, 4096, 4096, "x", "P", "P", "P")[0]

@@ -88,7 +88,7 @@ CASES = {
     "channel3d": dict(dim=3, n=(24, 16, 12), L=(2 * np.pi, 2.0, np.pi),
                       bc=["Periodic", "Periodic", "Wall", "Wall", "Periodic", "Periodic"]),
     "periodic3d": dict(dim=3, n=(16, 12, 18), L=(2 * np.pi, 1.5 * np.pi, 2.25 * np.pi), bc=["Periodic"] * 6),
-    "cavity3d": dict(dim=3, n=(12, 16, 10), L=(1.0, 1.0, 1.0), bc=["Wall"] * 6),
+    "cavity3d": dict(dim=3, n=(12, 16, 8), L=(1.0, 1.0, 1.0), bc=["Wall"] * 6),
     "channel2d": dict(dim=2, n=(32, 24, 1), L=(2.0, 1.0, 1.0 / 24), bc=["Periodic", "Periodic", "Wall", "Wall"]),
 }
 
