@@ -110,7 +110,9 @@ def roofline_block(dim, form, cells, stage_ms, peak, peak_kind, sms=None, ghz=No
     tr = ncu["dram_bytes_per_cell"]
     step_w = sum(words.values())
     step_ms = sum(stage_ms.values())
-    out = {"bound": "hbm", "kernel": "k_predictor_tile" if form == "fp64" else "k_predictor_df_tile",
+    kern = ("k_predictor_tile" if form == "fp64" else "k_predictor_df_tile") if dim == 3 else \
+        ("k_predictor<2>" if form == "fp64" else "k_predictor_df<2>")
+    out = {"bound": "hbm", "kernel": kern,
            "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
            "traffic": int(tr * cells) if tr and dim == 3 else None, "peak_source": peak_kind,
            "bytes_per_cell": bpc, "stage_ms": {k: round(v, 4) for k, v in stage_ms.items()},
@@ -382,7 +384,88 @@ def form_adjoint(F, ndir=16, nsteps=500, every=50):
         worst = max(worst, abs(fd - ad) / abs(ad))
     return {"ratio_backward_over_forward": round(statistics.median(ratios), 3), "forward_ms": round(ms[1], 3),
             "backward_ms": round(ms[0], 3), "fd_directions": ndir, "fd_max_rel_err": worst,
-            "workload": "2D decaying turbulence 256^2, nu=2e-3, dt=2e-3, 500 steps, checkpoints every 50, FP64"}
+            "workload": "2D decaying turbulence 256^2, nu=2e-3, dt=2e-3, 500 steps, checkpoints every 50, FP64",
+            "tgv3d_64": form_adjoint3d(F)}
+
+
+def form_adjoint3d(F, ndir=4, nsteps=100, every=10):
+    """Adjoint of a 3D rollout: Taylor-Green 64^3 (ppp), nu = 1/1600, fixed dt = 5e-3 = dt_o,
+    100 steps, checkpoints every 10, loss 1/2 |v_T - v_target|^2 with a seeded smooth target:
+    backward/forward time ratio (median of 3) and central differences along `ndir` seeded
+    smooth directions, eps = 1e-6 |v_0|."""
+    from tests import cases as C
+
+    N, L, dt = 64, 2 * np.pi, 5e-3
+    g = F.Grid(N, N, N, L, L, L)
+    x0 = [C.interior(a, 3) for a in C.tgv3d_fields(N, L)]
+    rng = np.random.Generator(np.random.PCG64(31))
+    grid = np.meshgrid(*[np.arange(N) / N] * 3, indexing="ij")
+
+    def smooth(kmax=3):
+        f = np.zeros((N, N, N))
+        for _ in range(6):
+            k = rng.integers(0, kmax + 1, size=3)
+            ph = rng.uniform(0, 2 * np.pi, size=3)
+            term = rng.uniform(-1, 1) * np.ones((N, N, N))
+            for d in range(3):
+                term = term * np.cos(2 * np.pi * k[d] * grid[d] + ph[d])
+            f += term
+        return f
+
+    target = [smooth() for _ in range(3)]
+    vel = (F.U, F.V, F.W)
+
+    def load(s, x):
+        for fid, a in zip(vel + (F.P,), x):
+            f = s.zeros(fid)
+            f[1:-1, 1:-1, 1:-1] = a
+            s.set_field(fid, f)
+            s.update_ghost_nodes(fid)
+        for q in range(3):
+            s.set_field(F.DVO_X + q, s.zeros(F.DVO_X + q))
+        s.set_dt_o(dt)
+
+    def final(s):
+        return [C.interior(s.get_field(fid), 3) for fid in vel]
+
+    def loss(vT):
+        return 0.5 * sum(np.sum((a - b) ** 2) for a, b in zip(vT, target))
+
+    s = F.Solver(g, viscosity=1.0 / 1600)
+    s.adjoint_setup(nsteps, every)
+    ratios = []
+    for _ in range(3):
+        load(s, x0)
+        s.adjoint_forward(dt)
+        vT = final(s)
+        lam = []
+        for a, b in zip(vT, target):
+            f = s.zeros()
+            f[1:-1, 1:-1, 1:-1] = a - b
+            lam.append(f)
+        out = s.adjoint_backward(*lam)
+        ms = out[-1]
+        ratios.append(ms[0] / ms[1])
+    grads = [C.interior(a, 3) for a in out[:-1]]
+    f = F.Solver(g, viscosity=1.0 / 1600)
+    norm = np.sqrt(sum(np.sum(a ** 2) for a in x0[:-1]))
+    eps = 1e-6
+    worst = 0.0
+    for _ in range(ndir):
+        d = [smooth(kmax=6) for _ in range(3)]
+        dn = np.sqrt(sum(np.sum(a ** 2) for a in d))
+        d = [a * norm / dn for a in d]
+        Js = []
+        for sgn in (1.0, -1.0):
+            load(f, [a + sgn * eps * b for a, b in zip(x0[:-1], d)] + [x0[-1]])
+            f.advance_n(nsteps, dt)
+            Js.append(loss(final(f)))
+        fd = (Js[0] - Js[1]) / (2 * eps)
+        ad = sum(float(np.sum(gq * b)) for gq, b in zip(grads, d))
+        worst = max(worst, abs(fd - ad) / abs(ad))
+    return {"ratio_backward_over_forward": round(statistics.median(ratios), 3), "forward_ms": round(ms[1], 3),
+            "backward_ms": round(ms[0], 3), "fd_directions": ndir, "fd_max_rel_err": worst,
+            "workload": "3D Taylor-Green 64^3, nu=1/1600, dt=5e-3, 100 steps, checkpoints every 10, FP64"}
 
 
 def form_ensemble(F, steps=2000, nruns=512, tune_steps=10, sizes=(64, 96, 128, 192, 256), adjoint=True):
@@ -471,10 +554,14 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="arithmetic form of the headline run (mixed: FP32 stencils/transforms, FP64 "
                          "tridiagonal, zero mode, refinement residual and reductions)")
+    ap.add_argument("--shape", default="", help="grid override NXxNYxNZ of the headline run (profiling runs)")
     args = ap.parse_args()
     cfg_name = args.config
     cfg = dict(CONFIGS[cfg_name])
-    if args.grid:
+    if args.shape:
+        cfg["n"] = tuple(int(x) for x in args.shape.lower().split("x"))
+        cfg["desc"] = cfg["desc"] + f" (grid override {cfg['n']})"
+    elif args.grid:
         g0 = args.grid
         cfg["n"] = (g0, g0, g0 if cfg["dim"] == 3 else 1) if cfg_name != "channel" else (2 * g0, g0, (3 * g0) // 2)
         cfg["desc"] = cfg["desc"] + f" (grid override {cfg['n']})"

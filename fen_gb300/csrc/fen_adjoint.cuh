@@ -34,6 +34,18 @@ struct AdjScales {
   double id2[3];  // 1/delta^2 per axis
 };
 
+// The forward input velocity of the step being transposed, when the step is a graph replay:
+// entry *slot of a device table of the segment's stored inputs (nv fields per entry).
+struct AdjIn {
+  const double* const* tab;
+  const int* slot;
+  int nv;
+};
+// *slot = value (value >= 0) or *slot - 1: the replays walk the segment backwards.
+static __global__ void k_adj_slot(int* slot, int value) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *slot = (value >= 0) ? value : *slot - 1;
+}
+
 // Ghost layer of an adjoint field along one axis: periodic copies, or zeros (walls).  Axes
 // are filled x, then y, then z, each over the full extent of the others.
 template <int DIM>
@@ -155,7 +167,7 @@ __global__ void __launch_bounds__(256) k_adj_sum(Layout L, const double* __restr
 // wall-edge flux and the wall-normal diffusion read them (the dv^ of the ghost rows and of
 // the wall faces is zero).
 template <int DIM>
-__global__ void __launch_bounds__(256) k_adj_state(Layout L, const double* __restrict__ U, const double* __restrict__ V,
+__global__ void __launch_bounds__(256) k_adj_state(Layout L, AdjIn in, const double* __restrict__ U, const double* __restrict__ V,
                                                    const double* __restrict__ W, const double* __restrict__ us,
                                                    const double* __restrict__ vs, const double* __restrict__ ws,
                                                    const double* __restrict__ hu, const double* __restrict__ hv,
@@ -164,6 +176,12 @@ __global__ void __launch_bounds__(256) k_adj_state(Layout L, const double* __res
   const long long ncell = (long long)L.n0 * L.n1 * L.n2;
   const long long sy = L.sx, sz = L.sp;
   const double idx = q.id[0], idy = q.id[1], idz = q.id[2];
+  if (in.tab) {
+    const int e = *in.slot;
+    U = in.tab[(long long)e * in.nv];
+    V = in.tab[(long long)e * in.nv + 1];
+    if (DIM == 3) W = in.tab[(long long)e * in.nv + 2];
+  }
   CellWalk cw(L, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
   for (long long t = cw.t0; t < ncell; t += cw.stride, cw.next(L)) {
     const int j = 1 + cw.j;

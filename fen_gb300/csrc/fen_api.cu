@@ -191,6 +191,8 @@ struct fen_ctx {
     double *uh = nullptr, *vh = nullptr, *wh = nullptr, *ph = nullptr, *dou = nullptr, *dov = nullptr, *dow = nullptr;
     double *fh = nullptr, *bh = nullptr, *ush = nullptr, *vsh = nullptr, *wsh = nullptr;
     double *dhu = nullptr, *dhv = nullptr, *dhw = nullptr, *part = nullptr;
+    const double** dtab = nullptr;  // device copy of `inputs` (the graph-replayed step reads its entry)
+    int* dslot = nullptr;           // entry of the step being transposed
     double fwd_ms = 0, bwd_ms = 0;
     bool ready = false;
   } adj;
@@ -1283,6 +1285,8 @@ int fen_ctx_destroy(fen_ctx* c) {
   if (c->sc_host) cudaFreeHost(c->sc_host);
   for (double* b : c->adj.ckpt) if (b) cudaFree(b);
   for (double* b : c->adj.inputs) if (b) cudaFree(b);
+  if (c->adj.dtab) cudaFree(c->adj.dtab);
+  if (c->adj.dslot) cudaFree(c->adj.dslot);
   double* ab[] = {c->adj.uh, c->adj.vh, c->adj.wh, c->adj.ph, c->adj.dou, c->adj.dov, c->adj.dow, c->adj.fh,
                   c->adj.bh, c->adj.ush, c->adj.vsh, c->adj.wsh, c->adj.dhu, c->adj.dhv, c->adj.dhw, c->adj.part};
   for (double* b : ab) if (b) cudaFree(b);
@@ -2051,8 +2055,9 @@ AdjScales adj_scales(const fen_ctx* c) {
   return q;
 }
 
-// One adjoint step with the stored forward input velocity (u, v, w) of that step.
-int adj_step(fen_ctx* c, const double* u, const double* v, const double* w) {
+// One adjoint step with the stored forward input velocity (u, v, w) of that step, or, when
+// in.tab is set, the entry *in.slot of the table of stored inputs.
+int adj_step(fen_ctx* c, const double* u, const double* v, const double* w, AdjIn in) {
   auto& A = c->adj;
   int r;
   const long long ncell = (long long)c->n[0] * c->n[1] * c->n[2];
@@ -2097,7 +2102,7 @@ int adj_step(fen_ctx* c, const double* u, const double* v, const double* w) {
   ADJ_LAUNCH(k_adj_dv, c->L, A.ush, A.vsh, A.wsh, A.dou, A.dov, A.dow, dt * Acoef, dt * Bcoef, A.dhu, A.dhv, A.dhw);
   // v^ = v*^ + E^T (N'^T dv^ + mu/rhof L dv^)
   if ((r = adj_ghost(c, {A.dhu, A.dhv, d3 ? A.dhw : nullptr}))) return r;
-  ADJ_LAUNCH(k_adj_state, c->L, u, v, w, A.ush, A.vsh, A.wsh, A.dhu, A.dhv, A.dhw, q, c->prm.viscosity / rhof, wall,
+  ADJ_LAUNCH(k_adj_state, c->L, in, u, v, w, A.ush, A.vsh, A.wsh, A.dhu, A.dhv, A.dhw, q, c->prm.viscosity / rhof, wall,
              A.uh, A.vh, A.wh);
 #undef ADJ_LAUNCH
   CK(cudaGetLastError());
@@ -2130,6 +2135,13 @@ int fen_adjoint_setup(fen_ctx* c, int nsteps, int every) {
   for (auto& b : A.ckpt) if ((r = alloc(&b, c->L.total))) return r;
   A.inputs.assign((size_t)A.nv * A.every, nullptr);
   for (auto& b : A.inputs) if ((r = alloc(&b, c->L.total))) return r;
+  if (A.dtab) cudaFree(A.dtab);
+  if (A.dslot) cudaFree(A.dslot);
+  A.dtab = nullptr;
+  A.dslot = nullptr;
+  CK(cudaMalloc(&A.dtab, A.inputs.size() * sizeof(double*)));
+  CK(cudaMalloc(&A.dslot, sizeof(int)));
+  CK(cudaMemcpy(A.dtab, A.inputs.data(), A.inputs.size() * sizeof(double*), cudaMemcpyHostToDevice));
   double** ab[] = {&A.uh, &A.vh, &A.wh, &A.ph, &A.dou, &A.dov, &A.dow, &A.fh, &A.bh, &A.ush, &A.vsh, &A.wsh,
                    &A.dhu, &A.dhv, &A.dhw};
   for (double** b : ab)
@@ -2191,25 +2203,53 @@ int fen_adjoint_backward3(fen_ctx* c, const double* lam_u, const double* lam_v, 
     else k_adj_wall_face<2><<<cdiv(nf, 256), 256, 0, c->stream>>>(c->L, A.vh);
     c->launches++;
   }
+  // the adjoint step as one graph (a step of small grids is a few dozen short launches): its
+  // forward input comes from the entry *dslot of the stored inputs, stepped down per replay
+  cudaGraphExec_t ag = nullptr;
+  long long per_adj = 0;
+  {
+    cudaGraph_t g;
+    const long long before = c->launches;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    r = adj_step(c, nullptr, nullptr, nullptr, AdjIn{A.dtab, A.dslot, A.nv});
+    if (!r) {
+      k_adj_slot<<<1, 32, 0, c->stream>>>(A.dslot, -1);
+      c->launches++;
+    }
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (r) return r;
+    if (e != cudaSuccess) return fail(FEN_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    CK(cudaGraphInstantiate(&ag, g, 0));
+    CK(cudaGraphDestroy(g));
+    per_adj = c->launches - before;
+    c->launches = before;
+  }
   // ghost entries of the seed carry no sensitivity: the first adjoint step overwrites them
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   CK(cudaEventRecord(e0, c->stream));
-  for (int seg = A.nckpt - 1; seg >= 0; --seg) {
+  for (int seg = A.nckpt - 1; seg >= 0 && !r; --seg) {
     const int s0 = seg * A.every, s1 = std::min(A.nsteps, s0 + A.every);
-    if ((r = adj_restore(c, seg))) return r;
-    for (int s = s0; s < s1; ++s) {
+    if ((r = adj_restore(c, seg))) break;
+    for (int s = s0; s < s1 && !r; ++s) {
       const double* cur[3] = {c->u, c->v, c->w};  // the step's input velocity, kept for its adjoint
-      for (int q = 0; q < A.nv; ++q)
-        if ((r = adj_copy(c, A.inputs[(size_t)A.nv * (s - s0) + q], cur[q]))) return r;
-      CK(cudaGraphLaunch(c->graph, c->stream));
+      for (int q = 0; q < A.nv && !r; ++q) r = adj_copy(c, A.inputs[(size_t)A.nv * (s - s0) + q], cur[q]);
+      if (!r && cudaGraphLaunch(c->graph, c->stream) != cudaSuccess) r = fail(FEN_ERR_CUDA, "graph launch");
     }
+    if (r) break;
     c->launches += c->launches_per_step * (s1 - s0);
-    for (int s = s1 - 1; s >= s0; --s) {
-      double* const* in = &A.inputs[(size_t)A.nv * (s - s0)];
-      if ((r = adj_step(c, in[0], in[1], d3 ? in[2] : nullptr))) return r;
-    }
+    k_adj_slot<<<1, 32, 0, c->stream>>>(A.dslot, s1 - 1 - s0);
+    c->launches++;
+    for (int s = s1 - 1; s >= s0 && !r; --s)
+      if (cudaGraphLaunch(ag, c->stream) != cudaSuccess) r = fail(FEN_ERR_CUDA, "graph launch");
+    c->launches += per_adj * (s1 - s0);
+  }
+  cudaGraphExecDestroy(ag);
+  if (r) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return r;
   }
   CK(cudaEventRecord(e1, c->stream));
   CK(cudaEventSynchronize(e1));

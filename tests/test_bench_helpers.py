@@ -36,6 +36,7 @@ def test_roofline_block():
     assert m["traffic"] == int(100.4 * 512 * 256 * 384) and "256x128x192" in m["traffic_source"]
     d2 = bench.roofline_block(2, "fp64", 128 * 128, stage, 6660.6, "measured", sms=152, ghz=2.07)
     assert d2["bytes_per_cell"] == 72 and d2["step_algorithmic_bytes_per_cell"] == 168
+    assert d2["kernel"] == "k_predictor<2>"
 
 
 def test_measured_peaks_file_and_fallback(tmp_path, monkeypatch):
