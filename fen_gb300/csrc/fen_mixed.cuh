@@ -122,6 +122,56 @@ __device__ __forceinline__ DF d2(DF p, DF c, DF m) {
   return DF{h, e - (h - s2)};
 }
 
+// Unnormalised forms for the intermediate values of the tiled predictor: the same error-free
+// leading operations without the closing renormalisation (h = s + e, l = e - (h - s)).  A
+// pair (s, e) whose e has not been folded into s represents the same value, and the next
+// operation's error-free sum or product takes it as it is: e is at most a few ulp(s) (or,
+// after an exact cancellation of the leading words, of the order of the operands' ulp), so
+// each result keeps an absolute error of the order of 2^-46 of its operands, as the
+// normalised forms do.  Pairs that are stored (v*, dv_o) are normalised first (dnorm).
+// About a fifth fewer FP32 instructions in a kernel that is issue-bound once its planes are
+// prefetched: channel 512x256x384 predictor 2.24 -> 1.85 ms, 500-step errors unchanged.
+#ifndef FEN_DF_LAZY
+#define FEN_DF_LAZY 1
+#endif
+__device__ __forceinline__ DF dnorm(DF a) {
+  const float h = a.h + a.l;
+  return DF{h, a.l - (h - a.h)};
+}
+#if FEN_DF_LAZY
+__device__ __forceinline__ DF daddq(DF a, DF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  return DF{s, e + (a.l + b.l)};
+}
+__device__ __forceinline__ DF dsubq(DF a, DF b) { return daddq(a, DF{-b.h, -b.l}); }
+__device__ __forceinline__ DF dmulq(DF a, DF b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return DF{p, e};
+}
+__device__ __forceinline__ DF dsqq(DF a) {
+  const float p = a.h * a.h;
+  float e = fmaf(a.h, a.h, -p);
+  e = fmaf(2.0f * a.h, a.l, e);
+  return DF{p, e};
+}
+__device__ __forceinline__ DF d2q(DF p, DF c, DF m) {
+  float s1, e1, s2, e2;
+  two_sum(p.h, m.h, s1, e1);
+  two_sum(s1, -2.0f * c.h, s2, e2);
+  return DF{s2, (e1 + e2) + ((p.l + m.l) - 2.0f * c.l)};
+}
+#else
+__device__ __forceinline__ DF daddq(DF a, DF b) { return dadd(a, b); }
+__device__ __forceinline__ DF dsubq(DF a, DF b) { return dsub(a, b); }
+__device__ __forceinline__ DF dmulq(DF a, DF b) { return dmul(a, b); }
+__device__ __forceinline__ DF dsqq(DF a) { return dsq(a); }
+__device__ __forceinline__ DF d2q(DF p, DF c, DF m) { return d2(p, c, m); }
+#endif
+
 // ------------------------------------------------------------------------------------
 // Predictor (mixed): v* = v + dt * rhs and dv_o, both as pairs.  Every term of
 // navier_stokes.f90:140-404 (advection in divergence form, diffusion, body force, pressure
@@ -255,36 +305,36 @@ __device__ __forceinline__ void pf_line(const float* p) {
 __device__ __forceinline__ void dflux6(const DFField& U, const DFField& V, const DFField& W, long long c, long long sy,
                                        long long sz, DF& fuu, DF& fvv, DF& fww, DF& euv, DF& euw, DF& evw) {
   const DF uc = dfv(U, c), vc = dfv(V, c), wc = dfv(W, c);
-  fuu = dsq(dadd(dfv(U, c + 1), uc));
-  fvv = dsq(dadd(dfv(V, c + sy), vc));
-  fww = dsq(dadd(dfv(W, c + sz), wc));
-  euv = dmul(dadd(dfv(U, c + sy), uc), dadd(dfv(V, c + 1), vc));
-  euw = dmul(dadd(dfv(U, c + sz), uc), dadd(dfv(W, c + 1), wc));
-  evw = dmul(dadd(dfv(V, c + sz), vc), dadd(dfv(W, c + sy), wc));
+  fuu = dsqq(daddq(dfv(U, c + 1), uc));
+  fvv = dsqq(daddq(dfv(V, c + sy), vc));
+  fww = dsqq(daddq(dfv(W, c + sz), wc));
+  euv = dmulq(daddq(dfv(U, c + sy), uc), daddq(dfv(V, c + 1), vc));
+  euw = dmulq(daddq(dfv(U, c + sz), uc), daddq(dfv(W, c + 1), wc));
+  evw = dmulq(daddq(dfv(V, c + sz), vc), daddq(dfv(W, c + sy), wc));
 }
 // The three products a cell's +x neighbour needs (fuu, euv, euw of cell c).
 __device__ __forceinline__ void dflux_x(const DFField& U, const DFField& V, const DFField& W, long long c, long long sy,
                                         long long sz, DF& fuu, DF& euv, DF& euw) {
   const DF uc = dfv(U, c);
-  fuu = dsq(dadd(dfv(U, c + 1), uc));
-  euv = dmul(dadd(dfv(U, c + sy), uc), dadd(dfv(V, c + 1), dfv(V, c)));
-  euw = dmul(dadd(dfv(U, c + sz), uc), dadd(dfv(W, c + 1), dfv(W, c)));
+  fuu = dsqq(daddq(dfv(U, c + 1), uc));
+  euv = dmulq(daddq(dfv(U, c + sy), uc), daddq(dfv(V, c + 1), dfv(V, c)));
+  euw = dmulq(daddq(dfv(U, c + sz), uc), daddq(dfv(W, c + 1), dfv(W, c)));
 }
 // ... its +y neighbour needs (euv, fvv, evw of cell c).
 __device__ __forceinline__ void dflux_y(const DFField& U, const DFField& V, const DFField& W, long long c, long long sy,
                                         long long sz, DF& euv, DF& fvv, DF& evw) {
   const DF vc = dfv(V, c);
-  fvv = dsq(dadd(dfv(V, c + sy), vc));
-  euv = dmul(dadd(dfv(U, c + sy), dfv(U, c)), dadd(dfv(V, c + 1), vc));
-  evw = dmul(dadd(dfv(V, c + sz), vc), dadd(dfv(W, c + sy), dfv(W, c)));
+  fvv = dsqq(daddq(dfv(V, c + sy), vc));
+  euv = dmulq(daddq(dfv(U, c + sy), dfv(U, c)), daddq(dfv(V, c + 1), vc));
+  evw = dmulq(daddq(dfv(V, c + sz), vc), daddq(dfv(W, c + sy), dfv(W, c)));
 }
 // ... its +z neighbour needs (euw, evw, fww of cell c).
 __device__ __forceinline__ void dflux_z(const DFField& U, const DFField& V, const DFField& W, long long c, long long sy,
                                         long long sz, DF& euw, DF& evw, DF& fww) {
   const DF wc = dfv(W, c);
-  fww = dsq(dadd(dfv(W, c + sz), wc));
-  euw = dmul(dadd(dfv(U, c + sz), dfv(U, c)), dadd(dfv(W, c + 1), wc));
-  evw = dmul(dadd(dfv(V, c + sz), dfv(V, c)), dadd(dfv(W, c + sy), wc));
+  fww = dsqq(daddq(dfv(W, c + sz), wc));
+  euw = dmulq(daddq(dfv(U, c + sz), dfv(U, c)), daddq(dfv(W, c + 1), wc));
+  evw = dmulq(daddq(dfv(V, c + sz), dfv(V, c)), daddq(dfv(W, c + sy), wc));
 }
 __device__ __forceinline__ DF shfl_up_df(DF v) {
   return DF{__shfl_up_sync(0xffffffffu, v.h, 1), __shfl_up_sync(0xffffffffu, v.l, 1)};
@@ -334,46 +384,49 @@ static __global__ void __launch_bounds__(kDTX * kDTY, FEN_DFTILE_MINB) k_predict
     } else {
       dflux_y(U, V, W, c - sy, sy, sz, yuv, yvv, yvw);
     }
-    DF ax = dmul(dsub(fuu, xuu), qx);
-    ax = dadd(ax, dmul(dsub(euv, yuv), qy));
-    ax = dadd(ax, dmul(dsub(euw, puw), qz));
-    DF ay = dmul(dsub(euv, xuv), qx);
-    ay = dadd(ay, dmul(dsub(fvv, yvv), qy));
-    ay = dadd(ay, dmul(dsub(evw, pvw), qz));
-    DF az = dmul(dsub(euw, xuw), qx);
-    az = dadd(az, dmul(dsub(evw, yvw), qy));
-    az = dadd(az, dmul(dsub(fww, pww), qz));
+    DF ax = dmulq(dsubq(fuu, xuu), qx);
+    ax = daddq(ax, dmulq(dsubq(euv, yuv), qy));
+    ax = daddq(ax, dmulq(dsubq(euw, puw), qz));
+    DF ay = dmulq(dsubq(euv, xuv), qx);
+    ay = daddq(ay, dmulq(dsubq(fvv, yvv), qy));
+    ay = daddq(ay, dmulq(dsubq(evw, pvw), qz));
+    DF az = dmulq(dsubq(euw, xuw), qx);
+    az = daddq(az, dmulq(dsubq(evw, yvw), qy));
+    az = daddq(az, dmulq(dsubq(fww, pww), qz));
     puw = euw;
     pvw = evw;
     pww = fww;
     if (act) {
       const DF uc = dfv(U, c), vc = dfv(V, c), wc = dfv(W, c);
-      DF lu = dmul(d2(dfv(U, c + 1), uc, dfv(U, c - 1)), mx);
-      lu = dadd(lu, dmul(d2(dfv(U, c + sy), uc, dfv(U, c - sy)), my));
-      lu = dadd(lu, dmul(d2(dfv(U, c + sz), uc, dfv(U, c - sz)), mz));
-      DF lv = dmul(d2(dfv(V, c + 1), vc, dfv(V, c - 1)), mx);
-      lv = dadd(lv, dmul(d2(dfv(V, c + sy), vc, dfv(V, c - sy)), my));
-      lv = dadd(lv, dmul(d2(dfv(V, c + sz), vc, dfv(V, c - sz)), mz));
-      DF lw = dmul(d2(dfv(W, c + 1), wc, dfv(W, c - 1)), mx);
-      lw = dadd(lw, dmul(d2(dfv(W, c + sy), wc, dfv(W, c - sy)), my));
-      lw = dadd(lw, dmul(d2(dfv(W, c + sz), wc, dfv(W, c - sz)), mz));
-      DF dx = dsub(lu, ax), dy = dsub(lv, ay), dz = dsub(lw, az);
+      DF lu = dmulq(d2q(dfv(U, c + 1), uc, dfv(U, c - 1)), mx);
+      lu = daddq(lu, dmulq(d2q(dfv(U, c + sy), uc, dfv(U, c - sy)), my));
+      lu = daddq(lu, dmulq(d2q(dfv(U, c + sz), uc, dfv(U, c - sz)), mz));
+      DF lv = dmulq(d2q(dfv(V, c + 1), vc, dfv(V, c - 1)), mx);
+      lv = daddq(lv, dmulq(d2q(dfv(V, c + sy), vc, dfv(V, c - sy)), my));
+      lv = daddq(lv, dmulq(d2q(dfv(V, c + sz), vc, dfv(V, c - sz)), mz));
+      DF lw = dmulq(d2q(dfv(W, c + 1), wc, dfv(W, c - 1)), mx);
+      lw = daddq(lw, dmulq(d2q(dfv(W, c + sy), wc, dfv(W, c - sy)), my));
+      lw = daddq(lw, dmulq(d2q(dfv(W, c + sz), wc, dfv(W, c - sz)), mz));
+      DF dx = dsubq(lu, ax), dy = dsubq(lv, ay), dz = dsubq(lw, az);
       if (a.has_S) {
         const DF ir = DF{a.irho.hi, a.irho.lo};
-        dx = dadd(dx, dmul(DF{a.Sx[c], 0.f}, ir));
-        dy = dadd(dy, dmul(DF{a.Sy[c], 0.f}, ir));
-        dz = dadd(dz, dmul(DF{a.Sz[c], 0.f}, ir));
+        dx = daddq(dx, dmulq(DF{a.Sx[c], 0.f}, ir));
+        dy = daddq(dy, dmulq(DF{a.Sy[c], 0.f}, ir));
+        dz = daddq(dz, dmulq(DF{a.Sz[c], 0.f}, ir));
       }
       // AB2 with the pressure gradient (fields.f90:55-58, navier_stokes.f90:169-198)
       const DF pc = dfv(P, c);
-      DF rx = dsub(DF{a.g[0].hi, a.g[0].lo}, dmul(dsub(dfv(P, c + 1), pc), DF{a.gx.hi, a.gx.lo}));
-      DF ry = dsub(DF{a.g[1].hi, a.g[1].lo}, dmul(dsub(dfv(P, c + sy), pc), DF{a.gy.hi, a.gy.lo}));
-      DF rz = dsub(DF{a.g[2].hi, a.g[2].lo}, dmul(dsub(dfv(P, c + sz), pc), DF{a.gz.hi, a.gz.lo}));
-      rx = dadd(rx, dadd(dmul(A, dx), dmul(B, DF{a.dox[c], a.doxl[c]})));
-      ry = dadd(ry, dadd(dmul(A, dy), dmul(B, DF{a.doy[c], a.doyl[c]})));
-      rz = dadd(rz, dadd(dmul(A, dz), dmul(B, DF{a.doz[c], a.dozl[c]})));
-      // v* = v + dt rhs as a pair
-      const DF ix = dadd(uc, dmul(DT, rx)), iy = dadd(vc, dmul(DT, ry)), iz = dadd(wc, dmul(DT, rz));
+      DF rx = dsubq(DF{a.g[0].hi, a.g[0].lo}, dmulq(dsubq(dfv(P, c + 1), pc), DF{a.gx.hi, a.gx.lo}));
+      DF ry = dsubq(DF{a.g[1].hi, a.g[1].lo}, dmulq(dsubq(dfv(P, c + sy), pc), DF{a.gy.hi, a.gy.lo}));
+      DF rz = dsubq(DF{a.g[2].hi, a.g[2].lo}, dmulq(dsubq(dfv(P, c + sz), pc), DF{a.gz.hi, a.gz.lo}));
+      rx = daddq(rx, daddq(dmulq(A, dx), dmulq(B, DF{a.dox[c], a.doxl[c]})));
+      ry = daddq(ry, daddq(dmulq(A, dy), dmulq(B, DF{a.doy[c], a.doyl[c]})));
+      rz = daddq(rz, daddq(dmulq(A, dz), dmulq(B, DF{a.doz[c], a.dozl[c]})));
+      // v* = v + dt rhs as a pair; the stored pairs normalised
+      const DF ix = dnorm(daddq(uc, dmulq(DT, rx))), iy = dnorm(daddq(vc, dmulq(DT, ry))), iz = dnorm(daddq(wc, dmulq(DT, rz)));
+      dx = dnorm(dx);
+      dy = dnorm(dy);
+      dz = dnorm(dz);
       a.du[c] = ix.h; a.dul[c] = ix.l;
       a.dv[c] = iy.h; a.dvl[c] = iy.l;
       a.dw[c] = iz.h; a.dwl[c] = iz.l;
