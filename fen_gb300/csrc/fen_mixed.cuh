@@ -350,6 +350,7 @@ __device__ __forceinline__ DF shfl_up_df(DF v) {
 static __global__ void __launch_bounds__(kDTX * kDTY, FEN_DFTILE_MINB) k_predictor_df_tile(Layout L, const StepScalars* __restrict__ sc,
                                                                         PredDFArgs a) {
   __shared__ DF sh[2][3][kDTY][kDTX];
+  __shared__ DF xsh[2][3][kDTY];  // x-minus products of each row's first lane
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i0 = 1 + blockIdx.x * kDTX + tx, j0 = 1 + blockIdx.y * kDTY + ty;
   const bool act = (i0 <= L.n0) && (j0 <= L.n1);
@@ -368,14 +369,27 @@ static __global__ void __launch_bounds__(kDTX * kDTY, FEN_DFTILE_MINB) k_predict
     const long long c = L.idx(i, j, k);
     DF fuu, fvv, fww, euv, euw, evw;
     dflux6(U, V, W, c, sy, sz, fuu, fvv, fww, euv, euw, evw);
-    // x-minus: the lane to the left; lane 0 forms its own
+    // x-minus: the lane to the left; for the first lane of every row, lanes 0 .. kDTY-1 of
+    // row 0 form the products at i - 1 (one divergent pass per tile instead of one per row)
     DF xuu = shfl_up_df(fuu), xuv = shfl_up_df(euv), xuw = shfl_up_df(euw);
-    if (tx == 0) dflux_x(U, V, W, c - 1, sy, sz, xuu, xuv, xuw);
+    if (ty == 0 && tx < kDTY) {
+      const long long cx = L.idx(blockIdx.x * kDTX, min(1 + (int)blockIdx.y * kDTY + tx, L.n1), k);
+      DF a0, a1, a2;
+      dflux_x(U, V, W, cx, sy, sz, a0, a1, a2);
+      xsh[buf][0][tx] = a0;
+      xsh[buf][1][tx] = a1;
+      xsh[buf][2][tx] = a2;
+    }
     // y-minus: the row below through shared memory; row 0 forms its own
     sh[buf][0][ty][tx] = euv;
     sh[buf][1][ty][tx] = fvv;
     sh[buf][2][ty][tx] = evw;
     __syncthreads();
+    if (tx == 0) {
+      xuu = xsh[buf][0][ty];
+      xuv = xsh[buf][1][ty];
+      xuw = xsh[buf][2][ty];
+    }
     DF yuv, yvv, yvw;
     if (ty > 0) {
       yuv = sh[buf][0][ty - 1][tx];
