@@ -362,6 +362,12 @@ constexpr int kLB = FEN_LINE_LB;
 #define FEN_R2C_LB 2
 #endif
 constexpr int kLR = FEN_R2C_LB;
+// Strided (column) transforms: element addresses advanced by a constant stride per thread
+// instead of divided out per element (needs nl | threads, true for the column tiles).
+#ifndef FEN_STRIDED_IDX
+#define FEN_STRIDED_IDX 1
+#endif
+constexpr bool kStridedIdx = FEN_STRIDED_IDX != 0;
 
 template <typename T, int DIM, bool CONTIG, int OP, int LD, int ST>
 __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
@@ -562,6 +568,26 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
       }
       S(l, kk) = z;
     }
+  } else if (kStridedIdx && !CONTIG && nth % nl == 0) {
+    // complex in, strided lines with nl dividing the thread count: every element a thread
+    // loads belongs to the same line l = tid % nl, at positions p0, p0 + dp, ... (dp = nth / nl),
+    // so the address advances by a constant stride (no per-element division or multiply)
+    constexpr int B = (sizeof(T) == 4) ? kLB : 1;
+    int l, p0;
+    divmod(tid, fL, p0, l);
+    const int dp = nth / nl;
+    const bool lok = l < nlv;
+    const T2* src = inC + (long long)(line0 + (lok ? l : 0)) * a.in_line + (long long)outer * a.in_outer +
+                    (long long)p0 * a.in_pos;
+    const long long step = (long long)dp * a.in_pos;
+    for (int p1 = p0; p1 < M; p1 += dp * B, src += step * B) {
+      T2 zb[B];
+#pragma unroll
+      for (int b = 0; b < B; ++b) zb[b] = (p1 + b * dp < M && lok) ? src[step * b] : mk<T2>(0, 0);
+#pragma unroll
+      for (int b = 0; b < B; ++b)
+        if (p1 + b * dp < M) S(l, p1 + b * dp) = zb[b];
+    }
   } else {  // complex in: kLB loads in flight per thread (FP32; one in the FP64 kernels)
     const int work = nl * M;
     constexpr int B = (sizeof(T) == 4) ? kLB : 1;
@@ -703,6 +729,19 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
         __syncthreads();
       }
       if (tid == 0) a.partial[(long long)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+    }
+  } else if (kStridedIdx && !CONTIG && nth % nl == 0) {  // complex out, strided lines (as the strided load)
+    int l, p0;
+    divmod(tid, fL, p0, l);
+    if (l < nlv) {
+      const int dp = nth / nl;
+      T2* dst = outC + (long long)(line0 + l) * a.out_line + (long long)outer * a.out_outer + (long long)p0 * a.out_pos;
+      const long long step = (long long)dp * a.out_pos;
+      for (int p = p0; p < M; p += dp, dst += step) {
+        T2 z = R(l, p);
+        if (do_scale) z = mk<T2>(z.x * scale, z.y * scale);
+        *dst = z;
+      }
     }
   } else {  // complex out
     const int work = nl * M;
