@@ -104,18 +104,21 @@ __device__ __forceinline__ void divmod(int t, FastDiv f, int& q, int& r) {
   r = t - q * (int)f.d;
 }
 
-// cos(2 pi m/16), m = 0..15 (the in-register radix-8/16 rotations).
-__device__ __forceinline__ double cos16d(int m) {
+// cos(2 pi m/16), m = 0..15 (the in-register radix-8/16 rotations), as a constant of the
+// kernel's own type: a double narrowed at run time would be a conversion on the FP64 pipe
+// wherever the unrolled index is not folded.
+template <typename T>
+__device__ __forceinline__ T cos16(int m) {
   switch (m & 15) {
-    case 0: return 1.0;
-    case 1: case 15: return 0.92387953251128674;
-    case 2: case 14: return 0.70710678118654752;
-    case 3: case 13: return 0.38268343236508977;
-    case 4: case 12: return 0.0;
-    case 5: case 11: return -0.38268343236508977;
-    case 6: case 10: return -0.70710678118654752;
-    case 8: return -1.0;
-    default: return -0.92387953251128674;  // 7, 9
+    case 0: return T(1.0);
+    case 1: case 15: return T(0.92387953251128674);
+    case 2: case 14: return T(0.70710678118654752);
+    case 3: case 13: return T(0.38268343236508977);
+    case 4: case 12: return T(0.0);
+    case 5: case 11: return T(-0.38268343236508977);
+    case 6: case 10: return T(-0.70710678118654752);
+    case 8: return T(-1.0);
+    default: return T(-0.92387953251128674);  // 7, 9
   }
 }
 
@@ -128,7 +131,7 @@ __device__ __forceinline__ T2 rot16(T2 v, int m) {
   if (e == 4) return DIR < 0 ? mk<T2>(v.y, -v.x) : mk<T2>(-v.y, v.x);
   if (e == 8) return mk<T2>(-v.x, -v.y);
   if (e == 12) return DIR < 0 ? mk<T2>(-v.y, v.x) : mk<T2>(v.y, -v.x);
-  const T c = (T)cos16d(e), s = (T)DIR * (T)cos16d(e + 12);
+  const T c = cos16<T>(e), s = (T)DIR * cos16<T>(e + 12);
   return mk<T2>(fmx(v.x, c, -(v.y * s)), fmx(v.x, s, v.y * c));
 }
 

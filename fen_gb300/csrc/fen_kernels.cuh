@@ -321,7 +321,7 @@ struct LineArgs {
   FFTPlan plan;
   // fast-division multipliers (fft_magic) of n, M, M + 1 and nl, computed on the host: an
   // integer division in the kernel runs through conversion instructions, which GB300 issues
-  // on its FP64 pipe (zero: computed in the kernel)
+  // on its FP64 pipe (every launcher sets them)
   unsigned mg[4];
   AxisTw tw;
 };
@@ -383,11 +383,10 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   const int outer = blockIdx.y;
   const int nlv = min(nl, a.nlines - line0);  // valid lines in this CTA
   const int tid = threadIdx.x, nth = blockDim.x;
-  // element -> (line, position) splits by multiply-high division (no per-element divide)
-  const bool hm = a.mg[0] != 0u;  // fft_magic(n) of n >= 2 is never zero
-  const FastDiv fN{(unsigned)n, hm ? a.mg[0] : fft_magic((unsigned)n)}, fM{(unsigned)M, hm ? a.mg[1] : fft_magic((unsigned)M)};
-  const FastDiv fM1{(unsigned)(M + 1), hm ? a.mg[2] : fft_magic((unsigned)(M + 1))},
-      fL{(unsigned)nl, hm ? a.mg[3] : fft_magic((unsigned)nl)};
+  // element -> (line, position) splits by multiply-high division with the host's multipliers
+  // (a division here, even once per thread, compiles to conversions on the FP64 pipe)
+  const FastDiv fN{(unsigned)n, a.mg[0]}, fM{(unsigned)M, a.mg[1]};
+  const FastDiv fM1{(unsigned)(M + 1), a.mg[2]}, fL{(unsigned)nl, a.mg[3]};
   // position-major smem: element (l, p) at p*nl + l
   auto S = [&](int l, int p) -> T2& { return bufA[(size_t)p * nl + l]; };
   T* Sr = reinterpret_cast<T*>(bufA);  // real view: real slot r of line l at (r/2 * nl + l)*2 + (r&1)
@@ -719,16 +718,35 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
       }
     }
     if (want_sum) {
-      if constexpr (sizeof(T) == 4) lsum = (double)lsh + (double)lsl;
-      // deterministic CTA sum (fixed tree order)
-      __shared__ double red[256];
-      red[tid] = lsum;
-      __syncthreads();
-      for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (tid < s) red[tid] += red[tid + s];
+      // deterministic CTA sum (fixed order)
+      if constexpr (sizeof(T) == 4) {
+        // FP32 pairs through a warp butterfly, one FP64 value per warp, the warps summed
+        // in order by thread 0 (the FP64 work of an FP32 kernel kept to a few instructions)
+        for (int o = 16; o > 0; o >>= 1) {
+          const float oh = __shfl_xor_sync(0xffffffffu, lsh, o), ol = __shfl_xor_sync(0xffffffffu, lsl, o);
+          float s2, e2;
+          two_sum(lsh, oh, s2, e2);
+          lsh = s2;
+          lsl = e2 + (lsl + ol);
+        }
+        __shared__ double redw[32];
+        if ((tid & 31) == 0) redw[tid >> 5] = (double)lsh + (double)lsl;
         __syncthreads();
+        if (tid == 0) {
+          double t = 0.0;
+          for (int w = 0; w < (nth + 31) / 32; ++w) t += redw[w];
+          a.partial[(long long)blockIdx.y * gridDim.x + blockIdx.x] = t;
+        }
+      } else {
+        __shared__ double red[256];
+        red[tid] = lsum;
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+          if (tid < s) red[tid] += red[tid + s];
+          __syncthreads();
+        }
+        if (tid == 0) a.partial[(long long)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
       }
-      if (tid == 0) a.partial[(long long)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
     }
   } else if (kStridedIdx && !CONTIG && nth % nl == 0) {  // complex out, strided lines (as the strided load)
     int l, p0;

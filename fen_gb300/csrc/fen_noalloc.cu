@@ -167,6 +167,8 @@ extern "C" int fen_poisson_pp2d_noalloc(const double* rhs, double* phi, int nx, 
   ax.out = spec; ax.out_line = hp; ax.out_pos = 1; ax.out_outer = hp * ny;
   ax.plan = half;
   ax.tw.wM = wM; ax.tw.wN = wN; ax.tw.wD = nullptr;
+  ax.mg[0] = fft_magic((unsigned)nx); ax.mg[1] = fft_magic((unsigned)Mx);
+  ax.mg[2] = fft_magic((unsigned)(Mx + 1)); ax.mg[3] = fft_magic((unsigned)nlx);
   const dim3 gx(cdiv(ny, nlx), 1);
   const size_t smx = 2 * (size_t)nlx * Mx * sizeof(double2);
   k_line<double, 2, true, OP_R2C, LD_FIELD, ST_CPLX><<<gx, 256, smx, st>>>(ax);
@@ -181,6 +183,8 @@ extern "C" int fen_poisson_pp2d_noalloc(const double* rhs, double* phi, int nx, 
   ay.lamA = lamx; ay.lamB = nullptr; ay.lamC = lamy;
   ay.plan = fully;
   ay.tw.wM = wY;
+  ay.mg[0] = fft_magic((unsigned)ny); ay.mg[1] = fft_magic((unsigned)ny);
+  ay.mg[2] = fft_magic((unsigned)(ny + 1)); ay.mg[3] = fft_magic((unsigned)nly);
   const dim3 gy(cdiv(h, nly), 1);
   const size_t smy = 2 * (size_t)nly * ny * sizeof(double2);
   k_line<double, 3, false, OP_C2C_SOLVE, LD_CPLX, ST_CPLX><<<gy, 256, smy, st>>>(ay);
