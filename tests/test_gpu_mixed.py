@@ -145,14 +145,27 @@ def test_mixed_2d_and_refinement(fen_lib):
         assert errs[1][fid] > errs[0][fid], errs
 
 
-def test_mixed_ghost_pairs_keep_fp64_values(fen_lib):
-    # pairs carry ~48 bits: an FP64 upload, ghost fill and download round-trip to ~1e-14
-    n = (12, 8, 6)
-    bc = ["Periodic", "Periodic", "Wall", "Wall", "Periodic", "Periodic"]
-    s32 = _solver(3, n, (1.0, 1.0, 1.0), bc, F.MIXED)
-    s64 = _solver(3, n, (1.0, 1.0, 1.0), bc, F.FP64)
+GHOST_SETS = {
+    "pnp": (3, ["Periodic", "Periodic", "Wall", "Wall", "Periodic", "Periodic"]),
+    "ppp": (3, ["Periodic"] * 6),
+    "nnn": (3, ["Wall"] * 6),
+    "npn": (3, ["Wall", "Wall", "Periodic", "Periodic", "Wall", "Wall"]),
+    "pp": (2, ["Periodic"] * 4),
+    "nn": (2, ["Wall"] * 4),
+    "pn_io": (2, ["Periodic", "Periodic", "Inflow", "Outflow"]),
+}
+
+
+@pytest.mark.parametrize("name", list(GHOST_SETS))
+def test_mixed_ghost_pairs_keep_fp64_values(fen_lib, name):
+    # pairs carry ~48 bits: an FP64 upload, ghost fill and download round-trip to ~1e-14; the
+    # pair fill copies pairs where the rule is a copy and evaluates it in FP64 elsewhere
+    dim, bc = GHOST_SETS[name]
+    n = (12, 8, 6) if dim == 3 else (12, 8, 1)
+    s32 = _solver(dim, n, (1.0, 1.0, 1.0), bc, F.MIXED)
+    s64 = _solver(dim, n, (1.0, 1.0, 1.0), bc, F.FP64)
     rng = np.random.Generator(np.random.PCG64(8))
-    for fid in (F.U, F.V, F.W, F.P):
+    for fid in ((F.U, F.V, F.W, F.P) if dim == 3 else (F.U, F.V, F.P)):
         a = rng.standard_normal(s32.grid.shape)
         for s in (s32, s64):
             s.set_field(fid, a)
