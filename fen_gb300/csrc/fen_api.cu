@@ -37,6 +37,9 @@ using namespace fen;
 #ifndef FEN_CHECK_CTAS_PER_SM
 #define FEN_CHECK_CTAS_PER_SM 16  // 256-thread CTAs per SM of the diagnostics pass (k_checks*; 4: FP64 256^3 0.357 -> 0.337 ms)
 #endif
+#ifndef FEN_VSTAR_LOW
+#define FEN_VSTAR_LOW 1  // 1: the ghost fill of v* covers only the faces the divergence reads
+#endif
 #ifndef FEN_THOMAS_DF
 #define FEN_THOMAS_DF 1  // mixed form, 3D solvers: the double-float sweep (k_thomas_df)
 #endif
@@ -748,7 +751,7 @@ FieldBC field_bc(fen_ctx* c, int f, bool homogeneous = false) {
 // Fill ghosts of up to four ghosted fields; `ids` give the bc set of each pointer.
 // `homogeneous` uses zero Dirichlet values (increments of fields that satisfy the BCs).
 template <typename T>
-int ghost(fen_ctx* c, int nf, T* const* ptr, const int* ids, bool homogeneous = false) {
+int ghost(fen_ctx* c, int nf, T* const* ptr, const int* ids, bool homogeneous = false, bool low_only = false) {
   GhostBatch<T> G;
   memset(&G, 0, sizeof(G));
   long long mx = 0;
@@ -759,6 +762,8 @@ int ghost(fen_ctx* c, int nf, T* const* ptr, const int* ids, bool homogeneous = 
     G.n[q] = g.a + g.b + g.c;
     G.shift[q] = 0.0;
     G.gd[q] = (c->dim == 3) ? ghost_div<3>(c->L, G.bc[q]) : ghost_div<2>(c->L, G.bc[q]);
+    G.low[q] = (low_only && G.bc[q].c != 'c') ? 1 : 0;
+    if (G.low[q]) G.n[q] = ghost_low_count(c->L, G.bc[q]);
     mx = std::max(mx, G.n[q]);
   }
   dim3 grid(std::min(cdiv(mx, 256), 4096), nf);
@@ -978,7 +983,8 @@ int pair_convert(fen_ctx* c, int f, int dir) {
 // Ghost fill of up to four pair fields.
 // Ghost fill of pair fields: the state pairs of `ids`, or the pairs (hi[q], lo[q]) with the
 // boundary rules of ids[q] when hi is given.
-int ghost_pairs(fen_ctx* c, int nf, const int* ids, float* const* hi = nullptr, float* const* lo = nullptr) {
+int ghost_pairs(fen_ctx* c, int nf, const int* ids, float* const* hi = nullptr, float* const* lo = nullptr,
+                bool low_only = false) {
   GhostDFBatch G;
   memset(&G, 0, sizeof(G));
   long long mx = 0;
@@ -994,6 +1000,8 @@ int ghost_pairs(fen_ctx* c, int nf, const int* ids, float* const* hi = nullptr, 
     GhostCount g = (c->dim == 3) ? ghost_count<3>(c->L, G.bc[q]) : ghost_count<2>(c->L, G.bc[q]);
     G.n[q] = g.a + g.b + g.c;
     G.gd[q] = (c->dim == 3) ? ghost_div<3>(c->L, G.bc[q]) : ghost_div<2>(c->L, G.bc[q]);
+    G.low[q] = (low_only && G.bc[q].c != 'c') ? 1 : 0;
+    if (G.low[q]) G.n[q] = ghost_low_count(c->L, G.bc[q]);
     mx = std::max(mx, G.n[q]);
   }
   dim3 grid(std::min(cdiv(mx, 256), 4096), nf);
@@ -1017,16 +1025,21 @@ int enqueue_step(fen_ctx* c, cudaEvent_t* ev) {
   c->launches++;
   if ((r = launch_predictor(c, c->sc))) return r;
   mark();  // 1: predictor
+  // v* takes the velocity boundary rules (update_ghost_nodes on v*).  Of its ghosts only the
+  // divergence's minus neighbours are read -- u*(0, j, k), v*(i, 0, k), w*(i, j, 0) -- besides
+  // the last face a wall overwrites, so only those are filled, unless the IBM hook or the
+  // variable-property path runs, whose stencils may read others.  Every ghost of the new
+  // velocity is filled after the correction.
+  const bool v_low = FEN_VSTAR_LOW && !var_path(c) && (c->ibm[0].n + c->ibm[1].n + c->ibm[2].n == 0);
   if (c->mixed) {
-    // v* pairs take the velocity boundary rules (update_ghost_nodes on v*)
     float* f[3] = {c->d32[0], c->d32[1], c->d32[2]};
     float* fl[3] = {c->d32l[0], c->d32l[1], c->d32l[2]};
     int ids[3] = {FEN_U, FEN_V, FEN_W};
-    if ((r = ghost_pairs(c, c->dim, ids, f, fl))) return r;
+    if ((r = ghost_pairs(c, c->dim, ids, f, fl, v_low))) return r;
   } else {
     double* f[3] = {c->us, c->vs, c->ws};
     int ids[3] = {FEN_U, FEN_V, FEN_W};
-    if ((r = ghost<double>(c, c->dim, f, ids))) return r;
+    if ((r = ghost<double>(c, c->dim, f, ids, false, v_low))) return r;
     if (c->ibm[0].n + c->ibm[1].n + c->ibm[2].n > 0) {
       // apply_ibm_forcing (navier_stokes.f90:106-108), then the boundary conditions again
       for (int q = 0; q < c->dim; ++q) {

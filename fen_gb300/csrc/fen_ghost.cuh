@@ -227,7 +227,39 @@ struct GhostBatch {
   long long n[4];
   double shift[4];
   GhostDiv gd[4];
+  int low[4];  // 1: only the ghosts of v* the divergence reads (ghost_low_target)
 };
+
+// The ghosts of v* the divergence reads (its minus neighbours) and the faces a wall overwrites:
+// the low face of a velocity component's own axis, interior extent -- u(0, j, k), v(i, 0, k),
+// w(i, j, 0) -- and, where that axis' high face is Dirichlet, the overwritten last face
+// u(n0, j, k), v(i, n1, k), w(i, j, n2) (the face-normal rule of Resolve).
+__host__ __device__ inline long long ghost_low_count(const Layout& L, const FieldBC& bc) {
+  const char c = bc.c;
+  const long long face = c == 'x' ? (long long)L.n1 * L.n2 : c == 'y' ? (long long)L.n0 * L.n2 : (long long)L.n0 * L.n1;
+  const int hi = c == 'x' ? F_RIGHT : c == 'y' ? F_TOP : F_BACK;
+  return face * (bc.type[hi] == FT_DIRICHLET ? 2 : 1);
+}
+__device__ __forceinline__ void ghost_low_target(const Layout& L, const FieldBC& bc, long long t, int& i, int& j, int& k) {
+  const char c = bc.c;
+  const unsigned face = c == 'x' ? (unsigned)(L.n1 * L.n2) : c == 'y' ? (unsigned)(L.n0 * L.n2) : (unsigned)(L.n0 * L.n1);
+  unsigned u = (unsigned)t;
+  const bool high = u >= face;  // the overwritten last face
+  if (high) u -= face;
+  if (c == 'x') {
+    i = high ? L.n0 : 0;
+    j = 1 + (int)(u % (unsigned)L.n1);
+    k = 1 + (int)(u / (unsigned)L.n1);
+  } else if (c == 'y') {
+    i = 1 + (int)(u % (unsigned)L.n0);
+    j = high ? L.n1 : 0;
+    k = 1 + (int)(u / (unsigned)L.n0);
+  } else {
+    i = 1 + (int)(u % (unsigned)L.n0);
+    j = 1 + (int)(u / (unsigned)L.n0);
+    k = high ? L.n2 : 0;
+  }
+}
 
 template <typename T, int DIM>
 __global__ void __launch_bounds__(256) k_ghost_fill(Layout L, GhostBatch<T> G) {
@@ -236,7 +268,8 @@ __global__ void __launch_bounds__(256) k_ghost_fill(Layout L, GhostBatch<T> G) {
   Resolve<T, DIM> R{PtrSrc<T>{G.f[q]}, L, G.bc[q], G.shift[q]};
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
-    if (G.gd[q].ok) ghost_target_fast<DIM>(L, G.bc[q], G.gd[q], t, i, j, k);
+    if (G.low[q]) ghost_low_target(L, G.bc[q], t, i, j, k);
+    else if (G.gd[q].ok) ghost_target_fast<DIM>(L, G.bc[q], G.gd[q], t, i, j, k);
     else ghost_target<DIM>(L, G.bc[q], t, i, j, k);
     const T v = R.at(i, j, k);
     G.f[q][L.idx(i, j, kst<DIM>(k))] = v;

@@ -636,6 +636,7 @@ struct GhostDFBatch {
   FieldBC bc[4];
   long long n[4];
   GhostDiv gd[4];
+  int low[4];  // 1: only the ghosts of v* the divergence reads (ghost_low_target)
 };
 
 template <int DIM>
@@ -645,7 +646,8 @@ __global__ void __launch_bounds__(256) k_ghost_fill_df(Layout L, GhostDFBatch G)
   Resolve<double, DIM, PairSrc> R{PairSrc{G.hi[q], G.lo[q]}, L, G.bc[q], 0.0};
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
-    if (G.gd[q].ok) ghost_target_fast<DIM>(L, G.bc[q], G.gd[q], t, i, j, k);
+    if (G.low[q]) ghost_low_target(L, G.bc[q], t, i, j, k);
+    else if (G.gd[q].ok) ghost_target_fast<DIM>(L, G.bc[q], G.gd[q], t, i, j, k);
     else ghost_target<DIM>(L, G.bc[q], t, i, j, k);
     const double v = R.at(i, j, k);
     const long long o = L.idx(i, j, kst<DIM>(k));

@@ -102,6 +102,43 @@ def test_mixed_channel_matches_fp64(fen_lib):
     assert e[F.P] < 1e-6, e
 
 
+WALL_FAMILIES = {
+    # solver: (dim, n, bc); smooth random fields, walls with the reference's Wall rules
+    "nnn": (3, (12, 16, 8), [O.WALL] * 6),
+    "npn": (3, (16, 12, 8), [O.WALL, O.WALL, O.PERIODIC, O.PERIODIC, O.WALL, O.WALL]),
+    "ppn": (3, (16, 12, 8), [O.PERIODIC] * 4 + [O.WALL] * 2),
+    "pn": (2, (32, 24, 1), [O.PERIODIC, O.PERIODIC, O.WALL, O.WALL]),
+    "nn": (2, (24, 32, 1), [O.WALL] * 4),
+}
+
+
+@pytest.mark.parametrize("name", list(WALL_FAMILIES))
+def test_mixed_steps_vs_oracle_walled(fen_lib, name):
+    # ten mixed steps (double-float sweeps, real systems for nnn) against the FP64 oracle
+    dim, n, bc = WALL_FAMILIES[name]
+    L = (1.0, 1.0, 1.0) if dim == 3 else (1.0, 1.0, 1.0 / n[1])
+    o = O.Oracle(dim, n, L, bc=bc, viscosity=0.01)
+    s = _solver(dim, n, L, bc, F.MIXED, viscosity=0.01)
+    rng = np.random.Generator(np.random.PCG64(40))
+    vel = [O.U, O.V] + ([O.W] if dim == 3 else [])
+    for fid in vel:
+        a = 0.1 * C.random_interior(s.grid.shape, rng, dim)
+        o.field(fid)[...] = a
+        s.set_field(fid, a)
+        o.update_ghost_nodes(fid)
+        s.update_ghost_nodes(fid)
+    dt = 1e-3
+    o.dt_o = dt
+    s.set_dt_o(dt)
+    o.run(10, dt)
+    s.advance_n(10, dt)
+    for fid in vel + [O.P]:
+        got, want = C.interior(s.get_field(fid), dim), C.interior(o.field(fid), dim)
+        if fid == O.P:
+            got, want = got - got.mean(), want - want.mean()
+        assert C.rel_l2(got, want) < 1e-6, (name, fid, C.rel_l2(got, want))
+
+
 def test_mixed_partial_tiles_match_fp64(fen_lib):
     # 3D sizes that leave partial predictor tiles in x (48 = 32 + 16), y (12 = 8 + 4) and z
     # (18 = 16 + 2 planes per walk), anisotropic spacing; start: a few seeded Fourier modes
