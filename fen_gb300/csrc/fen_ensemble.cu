@@ -326,11 +326,10 @@ __device__ __forceinline__ void fft_pass(const float2* __restrict__ src0, float2
 // Complex FFT of length P.M on nl lines; returns the buffer holding the result (a or b).
 template <int DIR, int NT>
 __device__ float2* ens_fft(float2* a, float2* b, int nl, FDiv fnl, int ls, int es, const FFTPlan& P, const float2* tw) {
-  const int L = P.M;
   int Ns = 1;
   for (int s = 0; s < P.nst; ++s) {
     const int R = P.R[s];
-    const int nb = L / R, tstep = L / (Ns * R);
+    const int nb = P.nb[s], tstep = P.ts[s];  // host-computed spans (no run-time division)
     const int work = nl * nb;
     switch (R) {
       case 16: fft_pass<DIR, 16, NT>(a, b, work, fnl, ls, es, Ns, nb, tstep, tw); break;
@@ -1153,6 +1152,7 @@ bool plan_len(int M, FFTPlan& P) {
   if (m % 4 == 0) { P.R[P.nst++] = 4; m /= 4; }
   if (m % 2 == 0) { P.R[P.nst++] = 2; m /= 2; }
   if (m % 3 == 0) { P.R[P.nst++] = 3; m /= 3; }
+  fft_plan_magic(P);
   return m == 1 && P.nst <= kMaxStages;
 }
 

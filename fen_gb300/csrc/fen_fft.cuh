@@ -18,6 +18,9 @@ constexpr int kMaxStages = 16;
 #ifndef FEN_FFT_MAXR64
 #define FEN_FFT_MAXR64 8
 #endif
+#ifndef FEN_FFT_MAXR32_ROW
+#define FEN_FFT_MAXR32_ROW 4
+#endif
 #ifndef FEN_FFT_MAXR32_COL
 #define FEN_FFT_MAXR32_COL 16
 #endif
@@ -28,6 +31,8 @@ struct FFTPlan {
   int nst;                     // stages
   int R[kMaxStages];           // radices: 16s or 8s first, then at most one 4 and one 2, then 3s
   unsigned nsm[kMaxStages];    // fast-division multiplier of the stage's span Ns (fft_magic)
+  int nb[kMaxStages];          // M / R: butterflies of the stage per line
+  int ts[kMaxStages];          // M / (Ns R): the stage's twiddle stride
 };
 
 // Multiplier m of the fast division n / d = umulhi(n, m), m = floor(2^32 / d) + 1 (0 for
@@ -42,6 +47,8 @@ inline void fft_plan_magic(FFTPlan& P) {
   unsigned ns = 1;
   for (int s = 0; s < P.nst; ++s) {
     P.nsm[s] = fft_magic(ns);
+    P.nb[s] = P.M / P.R[s];
+    P.ts[s] = P.M / ((int)ns * P.R[s]);
     ns *= (unsigned)P.R[s];
   }
 }
@@ -204,7 +211,7 @@ __device__ __forceinline__ void fft_pass_r(const T2* __restrict__ src0, T2* __re
 // FP32 column transforms take radix 16; FP32 x-line transforms stay at radix 4, whose low
 // register count keeps the SM fully occupied for their memory-bound load and store phases.
 constexpr int kFftMaxR64 = FEN_FFT_MAXR64;
-constexpr int kFftMaxR32Row = 4;
+constexpr int kFftMaxR32Row = FEN_FFT_MAXR32_ROW;
 constexpr int kFftMaxR32Col = FEN_FFT_MAXR32_COL;
 template <typename T, bool CONTIG>
 __host__ __device__ constexpr int fft_max_radix() {
@@ -215,13 +222,14 @@ __host__ __device__ constexpr int fft_max_radix() {
 // (16, 8, 4, 2, 3; none above MAXR).  Returns the buffer holding the result (a or b).
 template <int DIR, int MAXR, typename T2>
 __device__ T2* smem_fft(T2* a, T2* b, FastDiv fnl, int ls, int es, const FFTPlan& P, const double2* tw) {
-  const int M = P.M;
   const int nl = (int)fnl.d;
   int Ns = 1;
   for (int s = 0; s < P.nst; ++s) {
+    // per-stage spans come from the host plan: a run-time division here would compile to
+    // conversions on the FP64 pipe, issued by every thread at every stage
     const int R = P.R[s];
-    const int nb = M / R;
-    const int tstep = M / (Ns * R);
+    const int nb = P.nb[s];
+    const int tstep = P.ts[s];
     const int work = nl * nb;
     const bool p2 = (Ns & (Ns - 1)) == 0;
     const FastDiv fns{(unsigned)Ns, P.nsm[s]};

@@ -387,6 +387,8 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   // (a division here, even once per thread, compiles to conversions on the FP64 pipe)
   const FastDiv fN{(unsigned)n, a.mg[0]}, fM{(unsigned)M, a.mg[1]};
   const FastDiv fM1{(unsigned)(M + 1), a.mg[2]}, fL{(unsigned)nl, a.mg[3]};
+  const int nth_l = fdivi(nth, fL);            // threads per line of the strided branches
+  const bool nl_divides = nth_l * nl == nth;   // nl | threads
   // position-major smem: element (l, p) at p*nl + l
   auto S = [&](int l, int p) -> T2& { return bufA[(size_t)p * nl + l]; };
   T* Sr = reinterpret_cast<T*>(bufA);  // real view: real slot r of line l at (r/2 * nl + l)*2 + (r&1)
@@ -567,14 +569,14 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
       }
       S(l, kk) = z;
     }
-  } else if (kStridedIdx && !CONTIG && nth % nl == 0) {
+  } else if (kStridedIdx && !CONTIG && nl_divides) {
     // complex in, strided lines with nl dividing the thread count: every element a thread
     // loads belongs to the same line l = tid % nl, at positions p0, p0 + dp, ... (dp = nth / nl),
     // so the address advances by a constant stride (no per-element division or multiply)
     constexpr int B = (sizeof(T) == 4) ? kLB : 1;
     int l, p0;
     divmod(tid, fL, p0, l);
-    const int dp = nth / nl;
+    const int dp = nth_l;
     const bool lok = l < nlv;
     const T2* src = inC + (long long)(line0 + (lok ? l : 0)) * a.in_line + (long long)outer * a.in_outer +
                     (long long)p0 * a.in_pos;
@@ -748,11 +750,11 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
         if (tid == 0) a.partial[(long long)blockIdx.y * gridDim.x + blockIdx.x] = red[0];
       }
     }
-  } else if (kStridedIdx && !CONTIG && nth % nl == 0) {  // complex out, strided lines (as the strided load)
+  } else if (kStridedIdx && !CONTIG && nl_divides) {  // complex out, strided lines (as the strided load)
     int l, p0;
     divmod(tid, fL, p0, l);
     if (l < nlv) {
-      const int dp = nth / nl;
+      const int dp = nth_l;
       T2* dst = outC + (long long)(line0 + l) * a.out_line + (long long)outer * a.out_outer + (long long)p0 * a.out_pos;
       const long long step = (long long)dp * a.out_pos;
       for (int p = p0; p < M; p += dp, dst += step) {
@@ -782,8 +784,11 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
 
 // FP32 x-line transforms are memory-latency bound: compiled for 6 resident CTAs per SM
 // (<= 40 registers), where the default register choice would leave 4.
+#ifndef FEN_ROW32_MINB
+#define FEN_ROW32_MINB 6
+#endif
 template <int DIM, int OP, int LD, int ST>
-__global__ void __launch_bounds__(256, 6) k_line_row32(LineArgs<float> a) {
+__global__ void __launch_bounds__(256, FEN_ROW32_MINB) k_line_row32(LineArgs<float> a) {
   line_body<float, DIM, true, OP, LD, ST>(a);
 }
 
