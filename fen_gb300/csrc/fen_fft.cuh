@@ -19,7 +19,7 @@ constexpr int kMaxStages = 16;
 #define FEN_FFT_MAXR64 8
 #endif
 #ifndef FEN_FFT_MAXR32_ROW
-#define FEN_FFT_MAXR32_ROW 4
+#define FEN_FFT_MAXR32_ROW 8
 #endif
 #ifndef FEN_FFT_MAXR32_COL
 #define FEN_FFT_MAXR32_COL 16
@@ -208,8 +208,9 @@ __device__ __forceinline__ void fft_pass_r(const T2* __restrict__ src0, T2* __re
 
 // Largest radix compiled per kernel; the host's plans (make_plan's maxr) match.  FP64
 // transforms are FP64-issue bound and gain from radix 8 (fewer twiddle products and adds).
-// FP32 column transforms take radix 16; FP32 x-line transforms stay at radix 4, whose low
-// register count keeps the SM fully occupied for their memory-bound load and store phases.
+// FP32 column transforms take radix 16; FP32 x-line transforms radix 8 at 5 CTAs per SM
+// (measured on the mixed channel step, 512-point rows: radix 4 at 6 CTAs 5.31 ms, radix 8 at
+// 5 CTAs 5.22, at 4 CTAs 5.27, radix 16 at 3 CTAs 5.50).
 constexpr int kFftMaxR64 = FEN_FFT_MAXR64;
 constexpr int kFftMaxR32Row = FEN_FFT_MAXR32_ROW;
 constexpr int kFftMaxR32Col = FEN_FFT_MAXR32_COL;

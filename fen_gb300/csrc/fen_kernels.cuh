@@ -782,10 +782,10 @@ __global__ void __launch_bounds__(256) k_line(LineArgs<T> a) {
   line_body<T, DIM, CONTIG, OP, LD, ST>(a);
 }
 
-// FP32 x-line transforms are memory-latency bound: compiled for 6 resident CTAs per SM
-// (<= 40 registers), where the default register choice would leave 4.
+// FP32 x-line transforms: compiled for 5 resident CTAs per SM (<= 48 registers, room for
+// the radix-8 passes), where the default register choice would leave 4.
 #ifndef FEN_ROW32_MINB
-#define FEN_ROW32_MINB 6
+#define FEN_ROW32_MINB 5
 #endif
 template <int DIM, int OP, int LD, int ST>
 __global__ void __launch_bounds__(256, FEN_ROW32_MINB) k_line_row32(LineArgs<float> a) {
