@@ -604,6 +604,8 @@ LineArgs<float> typed_args<float>(const Stage& s) {
   a.L = d.L;
   a.partial = d.partial;
   a.scale = d.scale;
+  a.scale32 = (float)d.scale;
+  a.scaled = d.scale != 1.0;
   a.sc = d.sc;
   for (int q = 0; q < 3; ++q) a.id[q] = d.id[q];
   a.iso = d.iso; a.dim = d.dim;

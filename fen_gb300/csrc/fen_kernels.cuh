@@ -311,6 +311,8 @@ struct LineArgs {
   T* fdst;                // ST_FIELD destination
   double* partial;        // ST_FIELD: per-CTA line sums (mean removal), may be null
   double scale;
+  float scale32;          // FP32 kernels: scale rounded on the host, and whether it is not 1
+  int scaled;
   const StepScalars* sc;  // LD_DIV scaling rho/dt
   double id[3];
   int iso, dim;
@@ -404,8 +406,8 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
     // follow in the second pass so they cannot order the loads)
     const int work = nl * n;
     F2 rod{0.f, 0.f};
-    if (LD == LD_RESID) rod = split_d(a.sc->rho_over_dt);
-    const T rdt = (LD == LD_DIVMIX) ? (T)a.sc->rho_over_dt : T(0);
+    if (LD == LD_RESID) rod = F2{a.sc->rdtp[0], a.sc->rdtp[1]};  // rho/dt as the prologue's pair
+    const T rdt = (LD == LD_DIVMIX) ? (T)a.sc->rdtp[0] : T(0);
     const float* ph = (const float*)a.fsrc;
     for (int t0 = tid; t0 < work; t0 += nth * kLR) {
       F2 v[kLR];
@@ -462,10 +464,14 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
     // n reals per line -> packed complex (DCT2 reorders first: v_m = x_2m, v_{n-1-m} = x_2m+1)
     const int work = nl * n;
     F2 rod{0.f, 0.f};
-    if (LD == LD_RESID) rod = split_d(a.sc->rho_over_dt);
-    // rho/dt read (and, in FP32 kernels, narrowed) once: the field stores below may alias sc
-    // as far as the compiler knows, which would otherwise reload and convert it per element
-    const T rdt = (LD == LD_DIV || LD == LD_DIVMIX) ? (T)a.sc->rho_over_dt : T(0);
+    if (LD == LD_RESID) rod = F2{a.sc->rdtp[0], a.sc->rdtp[1]};
+    // rho/dt read once (FP32 kernels: the prologue's FP32 rounding of it, so no conversion
+    // is issued here): the field stores below may alias sc as far as the compiler knows
+    T rdt = T(0);
+    if (LD == LD_DIV || LD == LD_DIVMIX) {
+      if constexpr (sizeof(T) == 4) rdt = a.sc->rdtp[0];
+      else rdt = (T)a.sc->rho_over_dt;
+    }
     for (int t = tid; t < work; t += nth) {
       int l, i;
       if (CONTIG) divmod(t, fN, l, i); else divmod(t, fL, i, l);
@@ -652,8 +658,17 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   }
 
   // ---------------- store ----------------
-  const T scale = (T)a.scale;
-  const bool do_scale = (a.scale != 1.0) && (OP != OP_C2C_SOLVE);
+  // FP32 kernels take the scale as rounded on the host: a conversion or FP64 compare here
+  // would be re-issued per element on the FP64 pipe wherever the compiler rematerialises it
+  T scale;
+  bool do_scale;
+  if constexpr (sizeof(T) == 4) {
+    scale = a.scale32;
+    do_scale = a.scaled && (OP != OP_C2C_SOLVE);
+  } else {
+    scale = (T)a.scale;
+    do_scale = (a.scale != 1.0) && (OP != OP_C2C_SOLVE);
+  }
   T2* outC = reinterpret_cast<T2*>(a.out);
   T* outR = reinterpret_cast<T*>(a.out);
   auto R = [&](int l, int p) -> const T2& { return res[(size_t)p * nl + l]; };
