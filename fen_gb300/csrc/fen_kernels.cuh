@@ -1135,8 +1135,8 @@ __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_mixed(ThomasArg
 // channel (spectral stage, two sweeps): 0.52 ms; 4 rows at 40 registers (12 CTAs, the whole
 // grid resident at once) 0.80 ms; 4 rows at 48 registers (10 CTAs) 0.63 ms; with the systems
 // numbered across the outer rows instead of padded per row, 0.55 ms; with the rows 8, 16 or
-// 32 ahead prefetched into L2, unchanged.  The rows in flight matter more than the resident
-// warps.
+// 32 ahead prefetched into L2, unchanged; 12 or 16 rows in flight at 86-112 registers (4-5
+// CTAs), 0.49-0.52 ms.  Eight rows in flight at six CTAs is the balance.
 #ifndef FEN_THOMAS_DF_TB
 #define FEN_THOMAS_DF_TB 8
 #endif
