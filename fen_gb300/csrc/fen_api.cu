@@ -344,8 +344,11 @@ Stage s_stage(fen_ctx* c, int op, int ld, int st, int ax, int ncol, int nouter, 
 #ifndef FEN_COL64_NL
 #define FEN_COL64_NL 4
 #endif
+  // long columns take fewer per CTA, down to one (two ping-pong buffers of nl * M complex
+  // values in at most 200 KB of shared memory): FP64 columns up to 6144 points, FP32 up to
+  // 12288 (x lines: FP64 12288 points, FP32 24576)
   int nl = c->mixed ? FEN_COL32_NL : FEN_COL64_NL;
-  while (nl > 2 && 2 * (size_t)nl * M * cplx_size(c) > 200 * 1024) nl /= 2;
+  while (nl > 1 && 2 * (size_t)nl * M * cplx_size(c) > 200 * 1024) nl /= 2;
   s.la.n = n;
   s.la.nl = nl;
   s.la.nlines = ncol;

@@ -40,6 +40,23 @@ def test_mixed_poisson_vs_oracle(fen_lib, name):
     assert C.rel_l2(got, want) < RTOL_POISSON
 
 
+def test_mixed_poisson_long_columns(fen_lib):
+    # FP32 periodic columns of 8192 points (one column per CTA) against the FP64 oracle
+    n = (8, 8192, 1)
+    L = (8 / 8192, 1.0, 1.0)
+    bc = [O.PERIODIC] * 4
+    o = O.Oracle(2, n, L, bc=bc)
+    s = _solver(2, n, L, bc, F.MIXED)
+    rng = np.random.Generator(np.random.PCG64(17))
+    rhs = C.random_interior(s.grid.shape, rng, 2)
+    o.field(O.PHI)[...] = rhs
+    o.solve_poisson()
+    got = C.interior(s.solve_poisson(rhs), 2)
+    want = C.interior(o.field(O.PHI), 2)
+    got, want = got - got.mean(), want - want.mean()
+    assert C.rel_l2(got, want) < RTOL_POISSON, C.rel_l2(got, want)
+
+
 def _run_pair(dim, n, L, bc, init, nsteps, U=1.0, **kw):
     out = []
     for prec in (F.FP64, F.MIXED):

@@ -122,6 +122,29 @@ def test_poisson_matches_oracle(fen_lib, name):
     assert C.rel_l2(got, want) < RTOL_OP, C.rel_l2(got, want)
 
 
+@pytest.mark.parametrize("dim,n", [(2, (8, 4096, 1)), (3, (8, 4, 6144))])
+def test_poisson_long_columns(fen_lib, dim, n):
+    # periodic columns too long for two per CTA (4096 and 6144 points: one column per CTA,
+    # two FP64 buffers of the whole line in shared memory) against the oracle
+    h = 1.0 / max(n)
+    L = tuple(m * h for m in n)
+    bc = [O.PERIODIC] * (2 * dim)
+    o, s = pair(dim, n, L, bc=bc)
+    rng = np.random.Generator(np.random.PCG64(17))
+    rhs = C.random_interior(s.grid.shape, rng, dim)
+    load_both(o, s, O.PHI, rhs)
+    o.solve_poisson()
+    got = C.interior(s.solve_poisson(rhs), dim)
+    want = C.interior(o.field(O.PHI), dim)
+    assert C.rel_l2(got, want) < RTOL_OP, C.rel_l2(got, want)
+
+
+def test_transform_length_limit(fen_lib):
+    # an FP64 column of 8192 points (256 KB of buffers) exceeds one CTA: refused at set-up
+    with pytest.raises(F.FenError, match="too large"):
+        F.Solver(F.Grid(8, 8192, 1, 8 / 8192, 1.0, 1.0 / 8192))
+
+
 @pytest.mark.parametrize("name", ["pp", "pn", "nn", "ppp", "ppn", "npn", "nnn", "pnp"])
 def test_poisson_second_order_gpu(fen_lib, name):
     # test/small_test/poisson/convergence_rate through the C ABI: slope > 1.8
