@@ -1136,7 +1136,9 @@ __global__ void __launch_bounds__(128, FEN_THOMAS_MINB) k_thomas_mixed(ThomasArg
 // grid resident at once) 0.80 ms; 4 rows at 48 registers (10 CTAs) 0.63 ms; with the systems
 // numbered across the outer rows instead of padded per row, 0.55 ms; with the rows 8, 16 or
 // 32 ahead prefetched into L2, unchanged; 12 or 16 rows in flight at 86-112 registers (4-5
-// CTAs), 0.49-0.52 ms.  Eight rows in flight at six CTAs is the balance.
+// CTAs), 0.49-0.52 ms; both parts of a complex system in one thread (two interleaved chains,
+// 77 registers, the whole spectrum resident in one wave), 0.48 ms against 0.474.  Eight rows
+// in flight at six CTAs is the balance.
 #ifndef FEN_THOMAS_DF_TB
 #define FEN_THOMAS_DF_TB 8
 #endif
