@@ -80,7 +80,11 @@ typedef struct {
 } fen_status;
 
 /* grid%setup + init_solver: allocate_navier_stokes_fields + init_poisson_solver
- * (src/solver.f90:34-99, src/navier_stokes.f90:752-1067, src/poisson.f90:57-113). */
+ * (src/solver.f90:34-99, src/navier_stokes.f90:752-1067, src/poisson.f90:57-113).
+ * Sizes: every axis 2^a 3^b with a >= 1.  Each line transform holds its lines in shared
+ * memory, so an axis is limited to 12288 points for FP64 x lines (24576 in FEN_MIXED) and
+ * to 6144 for FP64 periodic columns (12288 in FEN_MIXED); beyond that the call returns
+ * FEN_ERR_ARG ("transform length too large for one CTA"). */
 int fen_ctx_create(const fen_params* params, fen_ctx** out);
 /* destroy_solver (src/solver.f90:333-357) + destroy_poisson_solver (poisson.f90:1456). */
 int fen_ctx_destroy(fen_ctx* ctx);
