@@ -40,10 +40,12 @@ def test_mixed_poisson_vs_oracle(fen_lib, name):
     assert C.rel_l2(got, want) < RTOL_POISSON
 
 
-def test_mixed_poisson_long_columns(fen_lib):
-    # FP32 periodic columns of 8192 points (one column per CTA) against the FP64 oracle
-    n = (8, 8192, 1)
-    L = (8 / 8192, 1.0, 1.0)
+@pytest.mark.parametrize("n", [(8, 8192, 1), (16384, 8, 1)])
+def test_mixed_poisson_long_lines(fen_lib, n):
+    # FP32 periodic columns of 8192 points and x lines of 16384 points (one line per CTA)
+    # against the FP64 oracle
+    h = 1.0 / max(n)
+    L = (n[0] * h, n[1] * h, 1.0)
     bc = [O.PERIODIC] * 4
     o = O.Oracle(2, n, L, bc=bc)
     s = _solver(2, n, L, bc, F.MIXED)

@@ -122,10 +122,11 @@ def test_poisson_matches_oracle(fen_lib, name):
     assert C.rel_l2(got, want) < RTOL_OP, C.rel_l2(got, want)
 
 
-@pytest.mark.parametrize("dim,n", [(2, (8, 4096, 1)), (3, (8, 4, 6144))])
-def test_poisson_long_columns(fen_lib, dim, n):
+@pytest.mark.parametrize("dim,n", [(2, (8, 4096, 1)), (3, (8, 4, 6144)), (2, (8192, 8, 1)), (3, (12288, 4, 4))])
+def test_poisson_long_lines(fen_lib, dim, n):
     # periodic columns too long for two per CTA (4096 and 6144 points: one column per CTA,
-    # two FP64 buffers of the whole line in shared memory) against the oracle
+    # two FP64 buffers of the whole line in shared memory) and x lines of 8192 and 12288
+    # points (one line per CTA) against the oracle
     h = 1.0 / max(n)
     L = tuple(m * h for m in n)
     bc = [O.PERIODIC] * (2 * dim)
