@@ -398,6 +398,15 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
 
   const T* inR = reinterpret_cast<const T*>(a.in);
   const T2* inC = reinterpret_cast<const T2*>(a.in);
+  // x lines: field index of (i + 1, row line0 + l) is rowbase + l*sx + i (the CTA's rows are
+  // consecutive rows of one plane), formed without a per-element 64-bit index product
+  long long rowbase = 0;
+  if (CONTIG) {
+    int j0, k0;
+    row_jk<DIM>(line0, outer, j0, k0);
+    rowbase = a.L.idx(1, j0, kst<DIM>(k0));
+  }
+  auto rc = [&](int l, int i) -> long long { return a.L.at(rowbase + (long long)(l * a.L.sx + i)); };
 
   // ---------------- load ----------------
   if (OP == OP_R2C && CONTIG && sizeof(T) == 4 && kLR > 1 && (LD == LD_DIVMIX || LD == LD_RESID)) {
@@ -418,12 +427,10 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
         int l = 0, i = 0;
         if (t < work) divmod(t, fN, l, i);
         if (t < work && l < nlv) {
-          int j, k;
-          row_jk<DIM>(line0 + l, outer, j, k);
-          const long long c = a.L.idx(i + 1, j, kst<DIM>(k));
+          const long long c = rc(l, i);
           if (LD == LD_DIVMIX) {
-            v[b] = div_df<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
-                               a.ful, a.fvl, a.fwl, a.idp, i + 1, j, k);
+            v[b] = div_df_at<DIM>(a.L, a.pu, a.pv, a.pw, (const float*)a.fu, (const float*)a.fv, (const float*)a.fw,
+                                  a.ful, a.fvl, a.fwl, a.idp, c);
           } else {
             // refinement right-hand side r = rho/dt D v* - L_h phi in double-float
             const F2 bb = mul_pair(a.dvh[c], a.dvl[c], rod);
@@ -445,9 +452,7 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
           if (l < nlv) {
             if (LD == LD_DIVMIX) {
               if (a.dvh) {  // kept for the refinement's residual
-                int j, k;
-                row_jk<DIM>(line0 + l, outer, j, k);
-                const long long c = a.L.idx(i + 1, j, kst<DIM>(k));
+                const long long c = rc(l, i);
                 a.dvh[c] = v[b].hi;
                 a.dvl[c] = v[b].lo;
               }
@@ -716,9 +721,13 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
         T x = (q & 1) ? zz.y : zz.x;
         if (do_scale) x = x * scale;
         if (ST == ST_FIELD) {
-          int j, k;
-          row_jk<DIM>(line0 + l, outer, j, k);
-          a.fdst[a.L.idx(i + 1, j, kst<DIM>(k))] = x;
+          if constexpr (CONTIG) {
+            a.fdst[rc(l, i)] = x;
+          } else {
+            int j, k;
+            row_jk<DIM>(line0 + l, outer, j, k);
+            a.fdst[a.L.idx(i + 1, j, kst<DIM>(k))] = x;
+          }
           if (want_sum) {
             if constexpr (sizeof(T) == 8) {
               lsum += x;

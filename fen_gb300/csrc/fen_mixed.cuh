@@ -482,15 +482,21 @@ __device__ __forceinline__ F2 div_term(const DFField& V, const float* d, const f
   return mul_pair(s, e, id);
 }
 
-// div at (i, j, k) of the pair field V plus, when given, a second pair field (d, dl).
+// div at cell index c (div_df: at (i, j, k)) of the pair field V plus, when given, a second
+// pair field (d, dl).
+template <int DIM>
+__device__ __forceinline__ F2 div_df_at(const Layout& L, const DFField& U, const DFField& V, const DFField& W,
+                                        const float* du, const float* dv, const float* dw, const float* dul,
+                                        const float* dvl, const float* dwl, const F2* id, long long c) {
+  F2 r = add_pair(div_term(U, du, dul, c, c - 1, id[0]), div_term(V, dv, dvl, c, c - L.sx, id[1]));
+  if (DIM == 3) r = add_pair(r, div_term(W, dw, dwl, c, c - L.sp, id[2]));
+  return r;
+}
 template <int DIM>
 __device__ __forceinline__ F2 div_df(const Layout& L, const DFField& U, const DFField& V, const DFField& W,
                                      const float* du, const float* dv, const float* dw, const float* dul,
                                      const float* dvl, const float* dwl, const F2* id, int i, int j, int k) {
-  const long long c = L.idx(i, j, kst<DIM>(k));
-  F2 r = add_pair(div_term(U, du, dul, c, c - 1, id[0]), div_term(V, dv, dvl, c, c - L.sx, id[1]));
-  if (DIM == 3) r = add_pair(r, div_term(W, dw, dwl, c, c - L.sp, id[2]));
-  return r;
+  return div_df_at<DIM>(L, U, V, W, du, dv, dw, dul, dvl, dwl, id, L.idx(i, j, kst<DIM>(k)));
 }
 
 // ------------------------------------------------------------------------------------

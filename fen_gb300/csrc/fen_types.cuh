@@ -44,6 +44,14 @@ struct Layout {
   // then use no conversion instructions, which GB300 issues on its slow FP64 pipe
   unsigned mg0 = 0, mg1 = 0;
   int fastdiv = 0;
+  // an index formed by the caller (a row base plus offsets), checked as idx checks its own
+  __host__ __device__ __forceinline__ long long at(long long r) const {
+#if defined(FEN_DEBUG_CHECKS) && defined(__CUDA_ARCH__)
+    return fen_checked(r, total);
+#else
+    return r;
+#endif
+  }
   __host__ __device__ __forceinline__ long long idx(int i, int j, int ks) const {
     const long long r = (long long)off + i + (long long)sx * j + sp * ks;
 #if defined(FEN_DEBUG_CHECKS) && defined(__CUDA_ARCH__)
