@@ -407,6 +407,18 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
     rowbase = a.L.idx(1, j0, kst<DIM>(k0));
   }
   auto rc = [&](int l, int i) -> long long { return a.L.at(rowbase + (long long)(l * a.L.sx + i)); };
+  // spectrum offsets of line l: x lines in 32-bit arithmetic from the CTA's base (a few rows
+  // of one plane), strided lines in 64-bit
+  const long long ibase = CONTIG ? (long long)line0 * a.in_line + (long long)outer * a.in_outer : 0;
+  const long long obase = CONTIG ? (long long)line0 * a.out_line + (long long)outer * a.out_outer : 0;
+  auto irow = [&](int l) -> long long {
+    return CONTIG ? ibase + (long long)(l * (int)a.in_line) : (long long)(line0 + l) * a.in_line + (long long)outer * a.in_outer;
+  };
+  auto orow = [&](int l) -> long long {
+    return CONTIG ? obase + (long long)(l * (int)a.out_line) : (long long)(line0 + l) * a.out_line + (long long)outer * a.out_outer;
+  };
+  auto ipos = [&](int p) -> long long { return CONTIG ? (long long)(p * (int)a.in_pos) : (long long)p * a.in_pos; };
+  auto opos = [&](int p) -> long long { return CONTIG ? (long long)(p * (int)a.out_pos) : (long long)p * a.out_pos; };
 
   // ---------------- load ----------------
   if (OP == OP_R2C && CONTIG && sizeof(T) == 4 && kLR > 1 && (LD == LD_DIVMIX || LD == LD_RESID)) {
@@ -535,9 +547,9 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
           if (CONTIG) divmod(t, fM, l, kk); else divmod(t, fL, kk, l);
         }
         if (t < work && l < nlv) {
-          const long long base = (long long)(line0 + l) * a.in_line + (long long)outer * a.in_outer;
-          xk[b] = inC[base + (long long)kk * a.in_pos];
-          xm[b] = inC[base + (long long)(M - kk) * a.in_pos];
+          const long long base = irow(l);
+          xk[b] = inC[base + ipos(kk)];
+          xm[b] = inC[base + ipos(M - kk)];
         } else {
           xk[b] = mk<T2>(0, 0);
           xm[b] = xk[b];
@@ -561,11 +573,11 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
       if (CONTIG) divmod(t, fM, l, kk); else divmod(t, fL, kk, l);
       T2 z = mk<T2>(0, 0);
       if (l < nlv) {
-        const long long base = (long long)(line0 + l) * a.in_line + (long long)outer * a.in_outer;
+        const long long base = irow(l);
         T2 xk, xm;
         if (OP == OP_C2R) {
-          xk = inC[base + (long long)kk * a.in_pos];
-          xm = inC[base + (long long)(M - kk) * a.in_pos];
+          xk = inC[base + ipos(kk)];
+          xm = inC[base + ipos(M - kk)];
         } else {
           // V_k = (Y_k - i Y_{n-k}) exp(+i pi k / 2n), Y_n = 0  (Makhoul's DCT-III)
           auto Vk = [&](int q) -> T2 {
@@ -685,7 +697,7 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
       if (l < nlv) {
         T2 X = r2c_post(res + l, nl, M, kk, a.tw.wN);
         if (do_scale) X = mk<T2>(X.x * scale, X.y * scale);
-        outC[(long long)(line0 + l) * a.out_line + (long long)kk * a.out_pos + (long long)outer * a.out_outer] = X;
+        outC[orow(l) + opos(kk)] = X;
       }
     }
   } else if (OP == OP_DCT2) {
@@ -696,11 +708,11 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
       if (l < nlv) {
         const T2 Vk = r2c_post(res + l, nl, M, kk, a.tw.wN);
         const T2 qv = cmul(ldtw<T2>(a.tw.wD, kk), Vk);
-        const long long base = (long long)(line0 + l) * a.out_line + (long long)outer * a.out_outer;
+        const long long base = orow(l);
         T y0 = T(2) * qv.x, y1 = T(-2) * qv.y;
         if (do_scale) { y0 = y0 * scale; y1 = y1 * scale; }
-        if (kk < n) outR[base + (long long)kk * a.out_pos] = y0;
-        if (kk >= 1 && kk <= M - 1) outR[base + (long long)(n - kk) * a.out_pos] = y1;
+        if (kk < n) outR[base + opos(kk)] = y0;
+        if (kk >= 1 && kk <= M - 1) outR[base + opos(n - kk)] = y1;
       }
     }
   } else if (OP == OP_C2R || OP == OP_DCT3) {
