@@ -11,7 +11,9 @@ them against exact references:
   rotations, against numpy.fft for every length 2^a 3^b the line kernels take;
 * the incremental cell walk of the grid-stride loops (CellWalk in fen_types.cuh);
 * the order-preserving int64 keys and NaN test of the FP64 diagnostics (okey / nan_bits in
-  fen_kernels.cuh).
+  fen_kernels.cuh);
+* the ghost fills' work-index mappings (ghost_target, ghost_target_fast, and the v* fill of
+  only the faces the divergence reads, ghost_low_target, in fen_ghost.cuh).
 """
 import cmath
 import math
@@ -273,3 +275,57 @@ def test_ghost_fast_bound_covers_bench_grids():
             for t in [0, 1, total // 3, total // 2, total - 1]:
                 assert fast(t) == _ghost_target(3, *n, c, "P", "D", "P", t)
     assert not _ghost_fast(3, 4096, 4096, 4096, "x", "P", "P", "P")[0]
+
+
+# ---- ghosts of v* after the predictor (ghost_low_count / ghost_low_target in
+# fen_gb300/csrc/fen_ghost.cuh): the divergence's minus neighbours plus the last face a
+# wall overwrites ----
+
+def _ghost_low_count(dim, n0, n1, n2, c, right, top, back):
+    face = {"x": n1 * n2, "y": n0 * n2, "z": n0 * n1}[c]
+    hi = {"x": right, "y": top, "z": back}[c]
+    return face * (2 if hi == "D" else 1)
+
+
+def _ghost_low_target(n0, n1, n2, c, t):
+    face = {"x": n1 * n2, "y": n0 * n2, "z": n0 * n1}[c]
+    high = t >= face
+    u = t - face if high else t
+    if c == "x":
+        return (n0 if high else 0), 1 + u % n1, 1 + u // n1
+    if c == "y":
+        return 1 + u % n0, (n1 if high else 0), 1 + u // n0
+    return 1 + u % n0, 1 + u // n0, (n2 if high else 0)
+
+
+@pytest.mark.parametrize("dim,n", [(3, (12, 16, 10)), (3, (24, 6, 9)), (2, (32, 24, 1)), (2, (3, 2, 1))])
+@pytest.mark.parametrize("walls", ["PPP", "DDD", "PDP", "DPD"])
+def test_ghost_low_faces_cover_what_the_divergence_reads(dim, n, walls):
+    # the cells filled are exactly the minus neighbours the divergence of cell (1..n0, 1..n1,
+    # 1..n2) reads outside the interior computed by the predictor, plus the face-normal wall
+    # face, each once; all of them are ghosts of the full fill (the same rule evaluates there)
+    right, top, back = walls
+    n0, n1, n2 = n
+    comps = ["x", "y"] + (["z"] if dim == 3 else [])
+    for c in comps:
+        total = _ghost_low_count(dim, n0, n1, n2, c, right, top, back)
+        cells = [_ghost_low_target(n0, n1, n2, c, t) for t in range(total)]
+        assert len(set(cells)) == total
+        ks = range(1, n2 + 1) if dim == 3 else [1]
+        want = set()
+        for k in ks:
+            for j in range(1, n1 + 1):
+                for i in range(1, n0 + 1):
+                    m = {"x": (i - 1, j, k), "y": (i, j - 1, k), "z": (i, j, k - 1)}[c]
+                    if m[{"x": 0, "y": 1, "z": 2}[c]] == 0:
+                        want.add(m)
+        hi = {"x": right, "y": top, "z": back}[c]
+        if hi == "D":
+            for k in ks:
+                for j in range(1, n1 + 1):
+                    for i in range(1, n0 + 1):
+                        want.add({"x": (n0, j, k), "y": (i, n1, k), "z": (i, j, n2)}[c])
+        assert set(cells) == want, c
+        full_total = sum(_ghost_count(dim, n0, n1, n2, c, right, top, back)[:3])
+        full = {_ghost_target(dim, n0, n1, n2, c, right, top, back, t) for t in range(full_total)}
+        assert set(cells) <= full, c
