@@ -364,6 +364,12 @@ constexpr int kLB = FEN_LINE_LB;
 #define FEN_R2C_LB 2
 #endif
 constexpr int kLR = FEN_R2C_LB;
+// ... of the pair-divergence loader (LD_DIVMIX): 3 (mixed channel forward x 0.514 -> 0.487
+// ms; 3 in the residual loader spills and slows it, 4 in either spills more)
+#ifndef FEN_R2C_LB_DIV
+#define FEN_R2C_LB_DIV 3
+#endif
+constexpr int kLRD = FEN_R2C_LB_DIV;
 // Strided (column) transforms: element addresses advanced by a constant stride per thread
 // instead of divided out per element (needs nl | threads, true for the column tiles).
 #ifndef FEN_STRIDED_IDX
@@ -421,8 +427,10 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
   auto opos = [&](int p) -> long long { return CONTIG ? (long long)(p * (int)a.out_pos) : (long long)p * a.out_pos; };
 
   // ---------------- load ----------------
-  if (OP == OP_R2C && CONTIG && sizeof(T) == 4 && kLR > 1 && (LD == LD_DIVMIX || LD == LD_RESID)) {
-    // FP32 r2c of the mixed form's pair loaders: kLR elements per thread evaluated before any
+  if (OP == OP_R2C && CONTIG && sizeof(T) == 4 && (LD == LD_DIVMIX ? kLRD : kLR) > 1 &&
+      (LD == LD_DIVMIX || LD == LD_RESID)) {
+    constexpr int kB = (LD == LD_DIVMIX) ? kLRD : kLR;
+    // FP32 r2c of the mixed form's pair loaders: kB elements per thread evaluated before any
     // store (their loads in flight together; the pair-divergence stores for the refinement
     // follow in the second pass so they cannot order the loads)
     const int work = nl * n;
@@ -430,10 +438,10 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
     if (LD == LD_RESID) rod = F2{a.sc->rdtp[0], a.sc->rdtp[1]};  // rho/dt as the prologue's pair
     const T rdt = (LD == LD_DIVMIX) ? (T)a.sc->rdtp[0] : T(0);
     const float* ph = (const float*)a.fsrc;
-    for (int t0 = tid; t0 < work; t0 += nth * kLR) {
-      F2 v[kLR];
+    for (int t0 = tid; t0 < work; t0 += nth * kB) {
+      F2 v[kB];
 #pragma unroll
-      for (int b = 0; b < kLR; ++b) {
+      for (int b = 0; b < kB; ++b) {
         const int t = t0 + b * nth;
         v[b] = F2{0.f, 0.f};
         int l = 0, i = 0;
@@ -455,7 +463,7 @@ __device__ __forceinline__ void line_body(const LineArgs<T>& a) {
         }
       }
 #pragma unroll
-      for (int b = 0; b < kLR; ++b) {
+      for (int b = 0; b < kB; ++b) {
         const int t = t0 + b * nth;
         if (t < work) {
           int l, i;
